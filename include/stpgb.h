@@ -1,0 +1,291 @@
+/*
+ * stpgb.h — C ABI of the GB300-native SuperTerrain+ heightfield pipeline.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (STPGB_OK on success) and, on failure, leaves a message readable through
+ * stpgb_last_error() on the calling thread.  Device pointers are CUDA device
+ * addresses on the current device; `stream` is a cudaStream_t passed as a
+ * void* so that this header needs no CUDA include.  Nothing here is globally
+ * synchronous unless it says so: kernels are enqueued on `stream`.
+ *
+ * Status codes map onto the reference's exception types:
+ *   STPGB_EINVAL   -> STPException::STPNumericDomainError / STPInvalidEnvironment
+ *   STPGB_ECUDA    -> STPException::STPCUDAError
+ *   STPGB_ETIMEOUT -> (new) a device loop hit its iteration cap
+ *   STPGB_ENOMEM   -> allocation failure or an HBM budget refusal
+ *   STPGB_ECAPACITY-> a caller-sized output or workspace was too small
+ */
+#ifndef STPGB_H_
+#define STPGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define STPGB_API __attribute__((visibility("default")))
+#else
+#define STPGB_API
+#endif
+
+enum {
+	STPGB_OK = 0,
+	STPGB_EINVAL = 1,
+	STPGB_ECUDA = 2,
+	STPGB_ETIMEOUT = 3,
+	STPGB_ENOMEM = 4,
+	STPGB_ECAPACITY = 5
+};
+
+/* ---------------------------------------------------------------- types -- */
+
+/* STPSingleHistogram::STPBin — SuperTerrain+/SuperAlgorithm+/Host/Public/
+ * SuperAlgorithm+Host/STPSingleHistogram.hpp:23-33,35.  8 bytes: Item at 0,
+ * two padding bytes, Weight at 4. */
+typedef struct stpgb_bin {
+	uint16_t Item;
+	float Weight;
+} stpgb_bin;
+
+/* STPNearestNeighbourInformation —
+ * SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/World/Chunk/
+ * STPNearestNeighbourInformation.hpp:13-25. */
+typedef struct stpgb_nn_info {
+	uint32_t MapSize[2];
+	uint32_t ChunkNearestNeighbour[2];
+	uint32_t TotalMapSize[2];
+} stpgb_nn_info;
+
+/* STPEnvironment::STPSimplexNoiseSetting —
+ * SuperTerrain+/SuperAlgorithm+/Host/Public/SuperAlgorithm+Host/
+ * STPSimplexNoiseSetting.h:13-27. */
+typedef struct stpgb_simplex_setting {
+	uint64_t Seed;
+	uint32_t Distribution;
+	double Offset;
+} stpgb_simplex_setting;
+
+/* STPEnvironment::STPRainDropSetting — SuperTerrain+/SuperTerrain+/Public/
+ * SuperTerrain+/Environment/STPRainDropSetting.h:15-53 (same field order). */
+typedef struct stpgb_raindrop_setting {
+	uint64_t Seed;
+	uint32_t RainDropCount;
+	float Inertia;
+	float SedimentCapacityFactor;
+	float minSedimentCapacity;
+	float initWaterVolume;
+	float minWaterVolume;
+	float Friction;
+	float initSpeed;
+	float ErodeSpeed;
+	float DepositSpeed;
+	float EvaporateSpeed;
+	float Gravity;
+	uint32_t ErosionBrushRadius;
+} stpgb_raindrop_setting;
+
+/* STPDemo::STPBiomeProperty — SuperDemo+/World/Biomes/STPBiomeProperty.hpp:10-27. */
+typedef struct stpgb_biome_property {
+	float Scale;
+	uint32_t Octave;
+	float Persistence;
+	float Lacunarity;
+	float Depth;
+	float Variation;
+} stpgb_biome_property;
+
+/* STPAlgorithm::STPPermutation — .../SuperAlgorithm+Host/STPPermutation.hpp:9-22.
+ * Both pointers are device addresses. */
+typedef struct stpgb_permutation {
+	const uint8_t* Permutation;
+	const float* Gradient2D;
+	uint32_t Gradient2DSize;
+} stpgb_permutation;
+
+/* Settings of one heightfield generator: the subset of STPChunkSetting
+ * (SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/Environment/
+ * STPChunkSetting.h:15-45) the heightfield path reads. */
+typedef struct stpgb_chunk_setting {
+	uint32_t MapSize[2];
+	uint32_t DiversityNearestNeighbour[2];
+	uint32_t ErosionNearestNeighbour[2];
+} stpgb_chunk_setting;
+
+/* ------------------------------------------------------------- errors --- */
+
+/* Message of the last failure on this thread ("" if none). */
+STPGB_API const char* stpgb_last_error(void);
+/* Library version string. */
+STPGB_API const char* stpgb_version(void);
+
+/* --------------------------------------------------- host-side tables --- */
+
+/* Validation of STPSimplexNoiseSetting
+ * (SuperTerrain+/SuperAlgorithm+/Host/Private/STPAlgorithmEnvironment.cpp:13-17). */
+STPGB_API int stpgb_simplex_setting_validate(const stpgb_simplex_setting* setting);
+
+/* Validation of STPRainDropSetting
+ * (SuperTerrain+/SuperTerrain+/Private/STPEnvironment.cpp:48-66). */
+STPGB_API int stpgb_raindrop_setting_validate(const stpgb_raindrop_setting* setting);
+
+/* Replaces STPPermutationGenerator::generate
+ * (SuperTerrain+/SuperAlgorithm+/Host/Private/STPPermutationGenerator.cpp:40-94),
+ * host half: writes the 512-byte permutation and 2*Distribution gradient
+ * floats to host memory.  `grad_capacity` is the number of floats `grad`
+ * holds (>= 2*Distribution).  The gradient loop of the reference runs one
+ * extra time for some Distribution values and writes past its table; here the
+ * extra entry is dropped. */
+STPGB_API int stpgb_permutation_generate(const stpgb_simplex_setting* setting,
+	uint8_t* perm512, float* grad, uint32_t grad_capacity);
+
+/* Replaces generateErosionBrush
+ * (SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPHeightfieldGenerator.cpp:44-99),
+ * host half: `index` / `weight` receive up to `capacity` entries, `*size` the
+ * brush size.  Returns STPGB_ECAPACITY (and the needed size) if too small. */
+STPGB_API int stpgb_erosion_brush_generate(uint32_t dimension_x, uint32_t radius,
+	int32_t* index, float* weight, uint32_t capacity, uint32_t* size);
+
+/* minWaterVolume that makes the droplet loop of
+ * SuperTerrain+/SuperTerrain+/Private/GPGPU/STPRainDrop.cu:74 run exactly
+ * `lifetime` steps (unless the droplet leaves the map first). */
+STPGB_API float stpgb_lifetime_min_water_volume(float init_water_volume,
+	float evaporate_speed, uint32_t lifetime);
+
+/* ----------------------------------------------- single histogram filter -- */
+
+/* Workspace bytes stpgb_shf_filter needs for a chunk of `nn`, `radius`, and
+ * at most `max_items` distinct sample values in any filter window
+ * (0 = the library maximum, 256). */
+STPGB_API int stpgb_shf_workspace_size(const stpgb_nn_info* nn, uint32_t radius,
+	uint32_t max_items, size_t* bytes);
+
+/* Replaces STPSingleHistogramFilter::operator()
+ * (SuperTerrain+/SuperAlgorithm+/Host/Private/STPSingleHistogramFilter.cpp:870-902),
+ * on the GPU.  Input: `samplemap` (device, TotalMapSize row-major uint16).
+ * Output (device): `offsets` (MapSize.x*MapSize.y+1 uint32, the reference's
+ * HistogramStartOffset) and `bins` (capacity `bins_capacity`), bit-identical to
+ * the reference including bin order.  Radius must be positive, even and no
+ * larger than the central chunk's start coordinate (reference :874-880).
+ * A too-small `bins_capacity` or a window with more than `max_items` distinct
+ * values is reported by stpgb_shf_check on `status` (device uint32, may be
+ * NULL; it is cleared by this call).  Asynchronous on `stream`. */
+STPGB_API int stpgb_shf_filter(const uint16_t* samplemap, const stpgb_nn_info* nn,
+	uint32_t radius, uint32_t max_items, void* workspace, size_t workspace_bytes,
+	uint32_t* offsets, stpgb_bin* bins, uint64_t bins_capacity, uint32_t* status,
+	void* stream);
+
+/* Synchronous convenience: runs the filter into library-owned device memory
+ * and copies offsets (W*H+1) and bins to HOST memory.  `*nbins` receives the
+ * bin count; if `bins_capacity` is too small nothing is copied to `bins`
+ * and STPGB_ECAPACITY is returned with `*nbins` set.  Input is HOST memory. */
+STPGB_API int stpgb_shf_filter_host(const uint16_t* samplemap_host, const stpgb_nn_info* nn,
+	uint32_t radius, uint32_t* offsets_host, stpgb_bin* bins_host, uint64_t bins_capacity,
+	uint64_t* nbins);
+
+/* Reads and decodes a device status word written by the kernels
+ * (synchronises `stream`).  Returns STPGB_OK, STPGB_ECAPACITY or STPGB_ETIMEOUT. */
+STPGB_API int stpgb_status_check(const uint32_t* status, void* stream);
+
+/* ------------------------------------------------ multi-biome heightfield -- */
+
+/* Replaces generateMultiBiomeHeightmap + sampleSimplexNoise
+ * (SuperDemo+/Script/STPMultiHeightGenerator.cu:35-72) and
+ * STPSimplexNoise::simplex2D / simplex2DFractal
+ * (SuperTerrain+/SuperAlgorithm+/Device/Private/STPSimplexNoise.cu:18-110).
+ * For every pixel (x,y) of a MapSize chunk:
+ *   h = sum over its bins of Weight * (fractal_biome(x,y) * Variation + Depth)
+ * `heightmap` is written with row pitch `pitch` floats (>= MapSize.x).
+ * `perm` holds device pointers; `biome_table` is a device array of
+ * `biome_count` entries indexed by bin Item. */
+STPGB_API int stpgb_multibiome_heightmap(float* heightmap, uint32_t pitch,
+	const uint32_t* offsets, const stpgb_bin* bins, uint32_t map_x, uint32_t map_y,
+	float offset_x, float offset_y, const stpgb_permutation* perm,
+	const stpgb_biome_property* biome_table, uint32_t biome_count, void* stream);
+
+/* ------------------------------------------------------------- erosion --- */
+
+/* Replaces the droplet-start draw of hydraulicErosionKERNEL
+ * (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPHeightfieldKernel.cu:93-104):
+ * `count` (x,y) float pairs uniform in the central chunk, from a
+ * Philox4x32-10 stream (Salmon et al., SC'11) keyed by `seed`, counter =
+ * droplet index + `counter_base`. Device output. */
+STPGB_API int stpgb_droplet_starts(float* starts_xy, uint32_t count, uint64_t seed,
+	uint64_t counter_base, const stpgb_nn_info* nn, void* stream);
+
+/* Replaces STPHeightfieldKernel::hydraulicErosion
+ * (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPHeightfieldKernel.cu:37-49,80-108)
+ * and STPRainDrop (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPRainDrop.cu:18-165):
+ * free-slip particle erosion of the merged map `heightmap` (device,
+ * TotalMapSize row-major float) by `count` droplets starting at `starts_xy`
+ * (device).  `setting` is host memory.  `brush_index` / `brush_weight` are
+ * device arrays of `brush_size` entries.  `residual_sediment` (device double,
+ * may be NULL) accumulates the sediment that left with dying droplets, so
+ * that sum(h_before) - sum(h_after) == *residual_sediment up to rounding.
+ * `status` (device uint32, may be NULL) reports a droplet that hit the step
+ * cap.  Asynchronous on `stream`. */
+STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
+	const stpgb_raindrop_setting* setting, const float* starts_xy, uint32_t count,
+	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,
+	double* residual_sediment, uint32_t* status, void* stream);
+
+/* Replaces STPHeightfieldKernel::formatHeightmap
+ * (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPHeightfieldKernel.cu:51-57,112-122):
+ * out[i] = uint16(rint(saturate(in[i]) * 65535)). Device buffers. */
+STPGB_API int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x,
+	uint32_t map_y, void* stream);
+
+/* ---------------------------------------------------- synthetic inputs --- */
+
+/* Seeded Voronoi biome map over global pixel coordinates: nearest jittered
+ * site of a `cell`-pixel grid, biome = hash(site) % biome_count.  Writes a
+ * width x height uint16 tile whose top-left pixel is (origin_x, origin_y),
+ * row pitch `pitch` elements.  Device output. Integer-only, so the CPU and
+ * GPU agree bit for bit. */
+STPGB_API int stpgb_voronoi_biomemap(uint16_t* out, uint32_t pitch, uint32_t width,
+	uint32_t height, int64_t origin_x, int64_t origin_y, uint32_t cell,
+	uint32_t biome_count, uint64_t seed, void* stream);
+
+/* ------------------------------------- plain per-chunk drop-in generator -- */
+
+typedef struct stpgb_generator stpgb_generator;
+
+/* Replaces STPHeightfieldGenerator::STPHeightfieldGenerator
+ * (SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPHeightfieldGenerator.cpp:115-150)
+ * together with the demo diversity plugin STPBiomefieldGenerator
+ * (SuperDemo+/World/Biomes/STPBiomefieldGenerator.cpp:44-65): validates the
+ * settings, builds the erosion brush and permutation on the device. */
+STPGB_API int stpgb_generator_create(const stpgb_chunk_setting* chunk,
+	const stpgb_raindrop_setting* raindrop, const stpgb_simplex_setting* simplex,
+	const stpgb_biome_property* biome_table, uint32_t biome_count,
+	uint32_t interpolation_radius, stpgb_generator** out);
+STPGB_API int stpgb_generator_destroy(stpgb_generator* gen);
+
+/* Replaces STPHeightfieldGenerator::generate (…/STPHeightfieldGenerator.cpp:158-169):
+ * HOST arrays; `biomemap` holds DiversityNearestNeighbour.x*y chunk pointers
+ * (MapSize uint16 each, row-major chunk order); `heightfield` receives the
+ * MapSize float chunk.  Synchronous, like the reference. */
+STPGB_API int stpgb_generator_generate(stpgb_generator* gen, float* heightfield,
+	const uint16_t* const* biomemap, float offset_x, float offset_y);
+
+/* Replaces STPHeightfieldGenerator::erode (…/STPHeightfieldGenerator.cpp:171-197):
+ * HOST arrays, ErosionNearestNeighbour.x*y chunk pointers each.  Droplet
+ * starts come from stpgb_droplet_starts keyed by the raindrop Seed, with the
+ * counter advanced by RainDropCount on every call.  Synchronous. */
+STPGB_API int stpgb_generator_erode(stpgb_generator* gen, float* const* heightfield,
+	uint16_t* const* heightfield_fixed);
+
+/* erode() with explicit HOST droplet starts (`count` xy pairs in merged-map
+ * coordinates); `residual_sediment` (host, may be NULL) receives the mass
+ * that left with dying droplets. */
+STPGB_API int stpgb_generator_erode_starts(stpgb_generator* gen, float* const* heightfield,
+	uint16_t* const* heightfield_fixed, const float* starts_xy, uint32_t count,
+	double* residual_sediment);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STPGB_H_ */

@@ -1,0 +1,168 @@
+"""ctypes front end of the oracle (test infrastructure only).
+
+Only the tests, the smoke check and bench.py's CPU-baseline leg use this
+module; it is the checker, never the product.  `Oracle` wraps the CPU
+restatement (oracle/liboracle.so), `Reference` wraps the reference's own
+compiled host sources (oracle/_ref/libstpref.so) where they could be built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
+RAINDROP_FIELDS = [
+    ("Seed", C.c_uint64), ("RainDropCount", C.c_uint32), ("Inertia", C.c_float),
+    ("SedimentCapacityFactor", C.c_float), ("minSedimentCapacity", C.c_float),
+    ("initWaterVolume", C.c_float), ("minWaterVolume", C.c_float), ("Friction", C.c_float),
+    ("initSpeed", C.c_float), ("ErodeSpeed", C.c_float), ("DepositSpeed", C.c_float),
+    ("EvaporateSpeed", C.c_float), ("Gravity", C.c_float), ("ErosionBrushRadius", C.c_uint32),
+]
+BIOME_DTYPE = np.dtype([("Scale", "<f4"), ("Octave", "<u4"), ("Persistence", "<f4"),
+                        ("Lacunarity", "<f4"), ("Depth", "<f4"), ("Variation", "<f4")])
+
+
+class OrcRaindrop(C.Structure):
+    _fields_ = RAINDROP_FIELDS
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    def __init__(self):
+        self.lib = C.CDLL(_build.build())
+        L = self.lib
+        vp, u32, u64, f32, f64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_double, C.c_int
+        L.orc_permutation.argtypes = [u64, u32, f64, vp, vp]
+        L.orc_permutation.restype = i32
+        L.orc_shf.argtypes = [vp, u32, u32, u32, u32, u32, vp, vp, u64, C.POINTER(u64)]
+        L.orc_shf.restype = i32
+        L.orc_simplex2d.argtypes = [vp, vp, u32, f32, f32]
+        L.orc_simplex2d.restype = f32
+        L.orc_fractal.argtypes = [vp, vp, u32, f32, f32, f32, f32, u32, f32, f32, f32, f32, f32]
+        L.orc_fractal.restype = f32
+        L.orc_multibiome.argtypes = [vp, vp, vp, vp, vp, vp, u32, u32, u32, f32, f32, i32]
+        L.orc_multibiome.restype = None
+        L.orc_brush.argtypes = [u32, u32, vp, vp]
+        L.orc_brush.restype = u32
+        for name in ("orc_erode_f64", "orc_erode_f32"):
+            fn = getattr(L, name)
+            fn.argtypes = [vp, u32, u32, C.POINTER(OrcRaindrop), vp, u32, vp, vp, u32, C.POINTER(u64)]
+            fn.restype = f64
+        L.orc_format.argtypes = [vp, vp, u64]
+        L.orc_format.restype = None
+        L.orc_droplet_starts.argtypes = [vp, u32, u64, u64, u32, u32, u32, u32]
+        L.orc_droplet_starts.restype = None
+        L.orc_voronoi.argtypes = [vp, u32, u32, u32, C.c_int64, C.c_int64, u32, u32, u64]
+        L.orc_voronoi.restype = None
+
+    # -- permutation
+    def permutation(self, seed, distribution, offset):
+        perm = np.zeros(512, np.uint8)
+        grad = np.zeros(2 * max(distribution, 1), np.float32)
+        rc = self.lib.orc_permutation(seed, distribution, offset, _p(perm), _p(grad))
+        return rc, perm, grad
+
+    # -- single histogram filter
+    def shf(self, samplemap, map_size, nn, radius, capacity=None):
+        mx, my = map_size
+        samplemap = np.ascontiguousarray(samplemap, np.uint16)
+        assert samplemap.size == mx * nn[0] * my * nn[1]
+        offsets = np.zeros(mx * my + 1, np.uint32)
+        cap = capacity if capacity is not None else mx * my * min(64, (2 * radius + 1) ** 2)
+        bins = np.zeros(cap, BIN_DTYPE)
+        n = C.c_uint64(0)
+        rc = self.lib.orc_shf(_p(samplemap), mx, my, nn[0], nn[1], radius, _p(offsets), _p(bins), cap, C.byref(n))
+        if rc == 5:
+            return self.shf(samplemap, map_size, nn, radius, capacity=n.value)
+        return rc, offsets, bins[: n.value]
+
+    # -- noise
+    def multibiome(self, offsets, bins, table, perm, grad, map_size, offset, threads=1):
+        mx, my = map_size
+        out = np.zeros(mx * my, np.float32)
+        bins = np.ascontiguousarray(bins, BIN_DTYPE)
+        table = np.ascontiguousarray(table, BIOME_DTYPE)
+        self.lib.orc_multibiome(_p(out), _p(np.ascontiguousarray(offsets, np.uint32)), _p(bins), _p(table),
+                                _p(perm), _p(grad), len(grad) // 2, mx, my, offset[0], offset[1], threads)
+        return out.reshape(my, mx)
+
+    # -- brush
+    def brush(self, dim_x, radius):
+        cap = (2 * radius + 1) ** 2
+        idx = np.zeros(cap, np.int32)
+        w = np.zeros(cap, np.float32)
+        n = self.lib.orc_brush(dim_x, radius, _p(idx), _p(w))
+        return idx[:n], w[:n]
+
+    # -- erosion
+    def erode(self, heightmap, setting, starts, brush_index, brush_weight, fp64=True):
+        """Serial droplets; returns (map, residual sediment, realised steps)."""
+        dim_y, dim_x = heightmap.shape
+        s = OrcRaindrop(**setting)
+        starts = np.ascontiguousarray(starts, np.float32)
+        steps = C.c_uint64(0)
+        if fp64:
+            m = np.ascontiguousarray(heightmap, np.float64).copy()
+            fn = self.lib.orc_erode_f64
+        else:
+            m = np.ascontiguousarray(heightmap, np.float32).copy()
+            fn = self.lib.orc_erode_f32
+        res = fn(_p(m), dim_x, dim_y, C.byref(s), _p(starts), len(starts) // 2,
+                 _p(np.ascontiguousarray(brush_index, np.int32)), _p(np.ascontiguousarray(brush_weight, np.float32)),
+                 len(brush_index), C.byref(steps))
+        return m, res, steps.value
+
+    def format(self, heightmap):
+        h = np.ascontiguousarray(heightmap, np.float32)
+        out = np.zeros(h.shape, np.uint16)
+        self.lib.orc_format(_p(h), _p(out), h.size)
+        return out
+
+    def droplet_starts(self, count, seed, counter_base, map_size, nn):
+        xy = np.zeros(2 * count, np.float32)
+        self.lib.orc_droplet_starts(_p(xy), count, seed, counter_base, map_size[0], map_size[1], nn[0], nn[1])
+        return xy
+
+    def voronoi(self, width, height, origin, cell, biome_count, seed):
+        out = np.zeros((height, width), np.uint16)
+        self.lib.orc_voronoi(_p(out), width, width, height, origin[0], origin[1], cell, biome_count, seed)
+        return out
+
+
+class Reference:
+    """The reference's own STPSingleHistogramFilter / STPPermutationGenerator, compiled from its sources."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_ref()
+        if not path or not os.path.exists(path):
+            raise FileNotFoundError("reference build unavailable")
+        self.lib = C.CDLL(path)
+        vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
+        self.lib.ref_shf.argtypes = [vp, u32, u32, u32, u32, u32, C.c_int, vp, vp, u64, C.POINTER(u64)]
+        self.lib.ref_shf.restype = C.c_int
+        self.lib.ref_permutation.argtypes = [u64, u32, C.c_double, vp, vp]
+        self.lib.ref_permutation.restype = C.c_int
+
+    def shf(self, samplemap, map_size, nn, radius, parallel=False, capacity=None):
+        mx, my = map_size
+        samplemap = np.ascontiguousarray(samplemap, np.uint16)
+        offsets = np.zeros(mx * my + 1, np.uint32)
+        cap = capacity if capacity is not None else mx * my * min(64, (2 * radius + 1) ** 2)
+        bins = np.zeros(max(cap, 1), BIN_DTYPE)
+        n = C.c_uint64(0)
+        rc = self.lib.ref_shf(_p(samplemap), mx, my, nn[0], nn[1], radius, int(parallel), _p(offsets), _p(bins),
+                              cap, C.byref(n))
+        if rc == 5:
+            return self.shf(samplemap, map_size, nn, radius, parallel, capacity=n.value)
+        return rc, offsets, bins[: n.value]
+
+    def permutation(self, seed, distribution, offset):
+        perm = np.zeros(512, np.uint8)
+        grad = np.zeros(2 * max(distribution, 1), np.float32)
+        rc = self.lib.ref_permutation(seed, distribution, offset, _p(perm), _p(grad))
+        return rc, perm, grad

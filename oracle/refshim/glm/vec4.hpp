@@ -1,0 +1,2 @@
+#pragma once
+#include "detail_vec.hpp"

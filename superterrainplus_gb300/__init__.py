@@ -1,0 +1,229 @@
+"""GB300-native SuperTerrain+ heightfield pipeline.
+
+Host-side mirror of the reference interface for the heightfield path, over
+the C ABI of libstpgb.so (include/stpgb.h):
+
+* STPPermutationGenerator.generate        (SuperAlgorithm+Host/STPPermutationGenerator.h:50)
+* STPSingleHistogramFilter / STPFilterBuffer (SuperAlgorithm+Host/STPSingleHistogramFilter.h:36-190)
+* STPHeightfieldGenerator.generate / erode (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:145,159)
+* kernel-level calls on device buffers (shf_filter, multibiome_heightmap,
+  hydraulic_erosion, format_heightmap, droplet_starts, voronoi_biomemap)
+
+Device buffers are torch CUDA tensors (PyTorch is only the allocator and the
+stream provider here); the compute runs in the CUDA kernels of libstpgb.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._capi import (BiomeProperty, ChunkSetting, NNInfo, Permutation, RaindropSetting, SimplexSetting,
+                    STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
+                    STPNumericDomainError, STPTimeout, check, lib)
+
+__all__ = [
+    "BiomeProperty", "ChunkSetting", "NNInfo", "Permutation", "RaindropSetting", "SimplexSetting",
+    "STPCapacityError", "STPCUDAError", "STPException", "STPInsufficientMemory", "STPInvalidEnvironment",
+    "STPNumericDomainError", "STPTimeout", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
+    "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
+    "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps",
+]
+
+BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
+BIOME_DTYPE = np.dtype([("Scale", "<f4"), ("Octave", "<u4"), ("Persistence", "<f4"),
+                        ("Lacunarity", "<f4"), ("Depth", "<f4"), ("Variation", "<f4")])
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ------------------------------------------------------------ host tables
+
+
+def permutation_generate(seed, distribution, offset):
+    """STPPermutationGenerator::generate, host half: (perm u8[512], grad f32[2N])."""
+    s = SimplexSetting(seed, distribution, offset)
+    perm = np.zeros(512, np.uint8)
+    grad = np.zeros(2 * max(distribution, 1), np.float32)
+    check(lib().stpgb_permutation_generate(C.byref(s), _p(perm), _p(grad), grad.size), env_error=True)
+    return perm, grad
+
+
+def erosion_brush(dimension_x, radius):
+    """generateErosionBrush: (index i32[n], weight f32[n])."""
+    n = C.c_uint32(0)
+    rc = lib().stpgb_erosion_brush_generate(dimension_x, radius, None, None, 0, C.byref(n))
+    if rc not in (0, 5):
+        check(rc)
+    idx = np.zeros(n.value, np.int32)
+    w = np.zeros(n.value, np.float32)
+    check(lib().stpgb_erosion_brush_generate(dimension_x, radius, _p(idx), _p(w), n.value, C.byref(n)))
+    return idx, w
+
+
+def lifetime_min_water_volume(init_water_volume, evaporate_speed, lifetime):
+    return float(lib().stpgb_lifetime_min_water_volume(init_water_volume, evaporate_speed, lifetime))
+
+
+# ------------------------------------------------- single histogram filter
+
+
+class STPFilterBuffer:
+    """STPSingleHistogramFilter::STPFilterBuffer (STPSingleHistogramFilter.h:43-123).
+
+    Holds the last filter output (host arrays).  The execution type is kept
+    for API parity; both types run the same GPU filter and give identical
+    results, as the reference's serial and parallel filters do."""
+
+    Serial, Parallel = 0, 1
+
+    def __init__(self, execution_type=Serial):
+        if execution_type not in (self.Serial, self.Parallel):
+            raise STPException(f"invalid STPExecutionType {execution_type}")
+        self._type = execution_type
+        self.offsets = np.zeros(0, np.uint32)
+        self.bins = np.zeros(0, BIN_DTYPE)
+
+    def type(self):
+        return self._type
+
+    def size(self):
+        """(bin count, offset count), as STPFilterBuffer::size."""
+        return len(self.bins), len(self.offsets)
+
+    def readHistogram(self):
+        return self.bins, self.offsets
+
+
+class STPSingleHistogramFilter:
+    """STPSingleHistogramFilter::operator() on the GPU (host arrays in and out)."""
+
+    def __call__(self, samplemap, nn_info, filter_buffer, radius):
+        sm = np.ascontiguousarray(samplemap, np.uint16)
+        mx, my = nn_info.MapSize
+        npix = mx * my
+        offsets = np.zeros(npix + 1, np.uint32)
+        cap = npix * min(256, (2 * radius + 1) ** 2) if radius else 0
+        bins = np.zeros(max(cap, 1), BIN_DTYPE)
+        n = C.c_uint64(0)
+        rc = lib().stpgb_shf_filter_host(_p(sm), C.byref(nn_info), radius, _p(offsets), _p(bins), cap, C.byref(n))
+        check(rc)
+        filter_buffer.offsets = offsets
+        filter_buffer.bins = bins[: n.value].copy()
+        return filter_buffer.readHistogram()
+
+
+# ------------------------------------------------------ plain generator
+
+
+class STPHeightfieldGenerator:
+    """STPHeightfieldGenerator + the multi-biome diversity plugin, over host arrays."""
+
+    def __init__(self, chunk_setting, raindrop_setting, simplex_setting, biome_table, interpolation_radius):
+        table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
+        h = C.c_void_p()
+        rc = lib().stpgb_generator_create(C.byref(chunk_setting), C.byref(raindrop_setting), C.byref(simplex_setting),
+                                          _p(table), len(table), interpolation_radius, C.byref(h))
+        check(rc, env_error=True)
+        self._h = h
+        self.chunk = chunk_setting
+        self.raindrop = raindrop_setting
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().stpgb_generator_destroy(h)
+            self._h = None
+
+    def generate(self, heightfield, biomemap, offset):
+        """heightfield: float32[MapSize] (written); biomemap: list of uint16 chunk arrays."""
+        arrs = [np.ascontiguousarray(b, np.uint16) for b in biomemap]
+        ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        assert heightfield.dtype == np.float32 and heightfield.flags.c_contiguous
+        check(lib().stpgb_generator_generate(self._h, _p(heightfield), ptrs, offset[0], offset[1]))
+
+    def erode(self, heightfield, heightfield_fixed, starts=None):
+        """heightfield: list of float32 chunks (in/out); heightfield_fixed: list of uint16 chunks (out).
+        With `starts` (float32 xy pairs, merged coordinates) returns the residual sediment."""
+        for a in heightfield:
+            assert a.dtype == np.float32 and a.flags.c_contiguous
+        for a in heightfield_fixed:
+            assert a.dtype == np.uint16 and a.flags.c_contiguous
+        hp = (C.c_void_p * len(heightfield))(*[a.ctypes.data for a in heightfield])
+        fp = (C.c_void_p * len(heightfield_fixed))(*[a.ctypes.data for a in heightfield_fixed])
+        if starts is None:
+            check(lib().stpgb_generator_erode(self._h, hp, fp))
+            return None
+        st = np.ascontiguousarray(starts, np.float32)
+        res = C.c_double(0.0)
+        check(lib().stpgb_generator_erode_starts(self._h, hp, fp, _p(st), st.size // 2, C.byref(res)))
+        return res.value
+
+
+# --------------------------------------------- kernel-level device calls
+
+
+class DeviceOps:
+    """Kernel-level calls on torch CUDA tensors (device pointers), enqueued on
+    the current torch stream."""
+
+    def __init__(self):
+        import torch  # plumbing only: device memory and streams
+        self.torch = torch
+
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def empty(self, shape, dtype):
+        return self.torch.empty(shape, dtype=dtype, device="cuda")
+
+    def shf_filter(self, samplemap, map_size, nn, radius, max_items=0, bins_capacity=None, workspace=None):
+        """samplemap: int16/uint16 tensor of TotalMapSize; returns (offsets i32, bins i64-view, status)."""
+        t = self.torch
+        info = NNInfo.make(map_size, nn)
+        ws = C.c_size_t(0)
+        check(lib().stpgb_shf_workspace_size(C.byref(info), radius, max_items, C.byref(ws)))
+        if workspace is None or workspace.numel() < ws.value:
+            workspace = self.empty(max(ws.value, 1), t.uint8)
+        npix = map_size[0] * map_size[1]
+        cap = bins_capacity if bins_capacity is not None else npix * min(max_items or 256, (2 * radius + 1) ** 2)
+        offsets = self.empty(npix + 1, t.int32)
+        bins = self.empty(max(cap, 1), t.int64)
+        status = self.empty(1, t.int32)
+        check(lib().stpgb_shf_filter(C.c_void_p(samplemap.data_ptr()), C.byref(info), radius, max_items,
+                                     C.c_void_p(workspace.data_ptr()), ws.value, C.c_void_p(offsets.data_ptr()),
+                                     C.c_void_p(bins.data_ptr()), cap, C.c_void_p(status.data_ptr()), self._stream()))
+        return offsets, bins, status
+
+    def status_check(self, status):
+        check(lib().stpgb_status_check(C.c_void_p(status.data_ptr()), self._stream()))
+
+    def multibiome_heightmap(self, out, pitch, offsets, bins, map_size, offset, perm_dev, grad_dev, table_dev):
+        p = Permutation(perm_dev.data_ptr(), grad_dev.data_ptr(), grad_dev.numel() // 2)
+        check(lib().stpgb_multibiome_heightmap(C.c_void_p(out.data_ptr()), pitch, C.c_void_p(offsets.data_ptr()),
+                                               C.c_void_p(bins.data_ptr()), map_size[0], map_size[1], offset[0],
+                                               offset[1], C.byref(p), C.c_void_p(table_dev.data_ptr()),
+                                               table_dev.numel() // 6, self._stream()))
+
+    def droplet_starts(self, out, count, seed, counter_base, map_size, nn):
+        info = NNInfo.make(map_size, nn)
+        check(lib().stpgb_droplet_starts(C.c_void_p(out.data_ptr()), count, seed, counter_base, C.byref(info),
+                                         self._stream()))
+
+    def hydraulic_erosion(self, heightmap, map_size, nn, setting, starts, count, brush_index, brush_weight,
+                          residual=None, status=None):
+        info = NNInfo.make(map_size, nn)
+        check(lib().stpgb_hydraulic_erosion(C.c_void_p(heightmap.data_ptr()), C.byref(info), C.byref(setting),
+                                            C.c_void_p(starts.data_ptr()), count, C.c_void_p(brush_index.data_ptr()),
+                                            C.c_void_p(brush_weight.data_ptr()), brush_index.numel(),
+                                            C.c_void_p(residual.data_ptr() if residual is not None else 0),
+                                            C.c_void_p(status.data_ptr() if status is not None else 0),
+                                            self._stream()), env_error=True)
+
+    def format_heightmap(self, src, dst, map_x, map_y):
+        check(lib().stpgb_format_heightmap(C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()), map_x, map_y,
+                                           self._stream()))
+
+    def voronoi_biomemap(self, out, pitch, width, height, origin, cell, biome_count, seed):
+        check(lib().stpgb_voronoi_biomemap(C.c_void_p(out.data_ptr()), pitch, width, height, origin[0], origin[1],
+                                           cell, biome_count, seed, self._stream()))

@@ -1,0 +1,155 @@
+"""ctypes binding of libstpgb.so (the C ABI declared in include/stpgb.h).
+
+The library must exist: importing this module without it raises, there is
+no fallback path.  Status codes are turned into the exception types the
+reference throws (STPNumericDomainError, STPInvalidEnvironment,
+STPCUDAError) plus STPTimeout / STPInsufficientMemory / STPCapacityError.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libstpgb.so")
+
+STPGB_OK, STPGB_EINVAL, STPGB_ECUDA, STPGB_ETIMEOUT, STPGB_ENOMEM, STPGB_ECAPACITY = range(6)
+
+
+class STPException(RuntimeError):
+    """Base of the error types (SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/Exception)."""
+
+
+class STPNumericDomainError(STPException):
+    pass
+
+
+class STPInvalidEnvironment(STPException):
+    pass
+
+
+class STPCUDAError(STPException):
+    pass
+
+
+class STPTimeout(STPException):
+    pass
+
+
+class STPInsufficientMemory(STPException):
+    pass
+
+
+class STPCapacityError(STPException):
+    pass
+
+
+class NNInfo(C.Structure):
+    _fields_ = [("MapSize", C.c_uint32 * 2), ("ChunkNearestNeighbour", C.c_uint32 * 2),
+                ("TotalMapSize", C.c_uint32 * 2)]
+
+    @classmethod
+    def make(cls, map_size, nn):
+        i = cls()
+        i.MapSize[:] = list(map_size)
+        i.ChunkNearestNeighbour[:] = list(nn)
+        i.TotalMapSize[:] = [map_size[0] * nn[0], map_size[1] * nn[1]]
+        return i
+
+
+class SimplexSetting(C.Structure):
+    _fields_ = [("Seed", C.c_uint64), ("Distribution", C.c_uint32), ("Offset", C.c_double)]
+
+
+class RaindropSetting(C.Structure):
+    _fields_ = [
+        ("Seed", C.c_uint64), ("RainDropCount", C.c_uint32), ("Inertia", C.c_float),
+        ("SedimentCapacityFactor", C.c_float), ("minSedimentCapacity", C.c_float),
+        ("initWaterVolume", C.c_float), ("minWaterVolume", C.c_float), ("Friction", C.c_float),
+        ("initSpeed", C.c_float), ("ErodeSpeed", C.c_float), ("DepositSpeed", C.c_float),
+        ("EvaporateSpeed", C.c_float), ("Gravity", C.c_float), ("ErosionBrushRadius", C.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class BiomeProperty(C.Structure):
+    _fields_ = [("Scale", C.c_float), ("Octave", C.c_uint32), ("Persistence", C.c_float),
+                ("Lacunarity", C.c_float), ("Depth", C.c_float), ("Variation", C.c_float)]
+
+
+class Permutation(C.Structure):
+    _fields_ = [("Permutation", C.c_void_p), ("Gradient2D", C.c_void_p), ("Gradient2DSize", C.c_uint32)]
+
+
+class ChunkSetting(C.Structure):
+    _fields_ = [("MapSize", C.c_uint32 * 2), ("DiversityNearestNeighbour", C.c_uint32 * 2),
+                ("ErosionNearestNeighbour", C.c_uint32 * 2)]
+
+
+vp, u16, u32, u64, i32, i64, f32, f64, sz = (C.c_void_p, C.c_uint16, C.c_uint32, C.c_uint64, C.c_int32,
+                                             C.c_int64, C.c_float, C.c_double, C.c_size_t)
+
+# name -> (restype, argtypes); the single source of the binding
+PROTOTYPES = {
+    "stpgb_last_error": (C.c_char_p, []),
+    "stpgb_version": (C.c_char_p, []),
+    "stpgb_simplex_setting_validate": (C.c_int, [C.POINTER(SimplexSetting)]),
+    "stpgb_raindrop_setting_validate": (C.c_int, [C.POINTER(RaindropSetting)]),
+    "stpgb_permutation_generate": (C.c_int, [C.POINTER(SimplexSetting), vp, vp, u32]),
+    "stpgb_erosion_brush_generate": (C.c_int, [u32, u32, vp, vp, u32, C.POINTER(u32)]),
+    "stpgb_lifetime_min_water_volume": (f32, [f32, f32, u32]),
+    "stpgb_shf_workspace_size": (C.c_int, [C.POINTER(NNInfo), u32, u32, C.POINTER(sz)]),
+    "stpgb_shf_filter": (C.c_int, [vp, C.POINTER(NNInfo), u32, u32, vp, sz, vp, vp, u64, vp, vp]),
+    "stpgb_shf_filter_host": (C.c_int, [vp, C.POINTER(NNInfo), u32, vp, vp, u64, C.POINTER(u64)]),
+    "stpgb_status_check": (C.c_int, [vp, vp]),
+    "stpgb_multibiome_heightmap": (C.c_int, [vp, u32, vp, vp, u32, u32, f32, f32, C.POINTER(Permutation), vp,
+                                             u32, vp]),
+    "stpgb_droplet_starts": (C.c_int, [vp, u32, u64, u64, C.POINTER(NNInfo), vp]),
+    "stpgb_hydraulic_erosion": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp, u32,
+                                          vp, vp, vp]),
+    "stpgb_format_heightmap": (C.c_int, [vp, vp, u32, u32, vp]),
+    "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
+    "stpgb_generator_create": (C.c_int, [C.POINTER(ChunkSetting), C.POINTER(RaindropSetting),
+                                         C.POINTER(SimplexSetting), vp, u32, u32, C.POINTER(vp)]),
+    "stpgb_generator_destroy": (C.c_int, [vp]),
+    "stpgb_generator_generate": (C.c_int, [vp, vp, vp, f32, f32]),
+    "stpgb_generator_erode": (C.c_int, [vp, vp, vp]),
+    "stpgb_generator_erode_starts": (C.c_int, [vp, vp, vp, vp, u32, C.POINTER(f64)]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if libstpgb.so has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                              "(the CUDA extension is required; there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+_ERRORS = {
+    STPGB_EINVAL: STPNumericDomainError,
+    STPGB_ECUDA: STPCUDAError,
+    STPGB_ETIMEOUT: STPTimeout,
+    STPGB_ENOMEM: STPInsufficientMemory,
+    STPGB_ECAPACITY: STPCapacityError,
+}
+
+
+def check(rc, env_error=False):
+    """Raise the reference-style exception for a non-zero status."""
+    if rc == STPGB_OK:
+        return
+    msg = (lib().stpgb_last_error() or b"").decode(errors="replace")
+    if rc == STPGB_EINVAL and (env_error or msg.startswith("STP") and "Setting" in msg):
+        raise STPInvalidEnvironment(msg)
+    raise _ERRORS.get(rc, STPException)(f"status {rc}: {msg}")

@@ -1,0 +1,270 @@
+// Free-slip particle hydraulic erosion and height formatting on sm_103a.
+//
+// One thread per droplet, following STPRainDrop::operator()
+// (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPRainDrop.cu:53-165) step for
+// step: bilinear height/gradient at the current cell (:23-51), inertia
+// steering, unit move, death within BrushRadius of the merged-map border,
+// deposit over the 4 corners of the OLD cell or erosion over the brush
+// centred on the OLD cell, speed and volume update.  Like the reference the
+// map is shared by all droplets and updated with float atomics (release
+// build, :133-137,154); reads go through L2 (ld.global.cg) so a droplet sees
+// the other droplets' completed updates.  Two additions:
+//  * the sediment a droplet still carries when it dies (evaporated or left
+//    the map) is summed into a double, which closes the mass balance
+//    sum(h_before) - sum(h_after) = residual;
+//  * the loop has a hard step cap (the reference loops while
+//    Volume >= minWaterVolume); reaching it sets STATUS_TIMEOUT.
+#include "erosion.cuh"
+
+#include <cmath>
+
+namespace stpgb {
+
+namespace {
+
+constexpr uint32_t kErodeBlock = 128u;
+
+struct HG {
+	float h, gx, gy;
+};
+
+// STPRainDrop.cu:23-51
+__device__ __forceinline__ HG height_gradient(const float* __restrict__ map, const uint64_t pitch, const float px,
+	const float py) {
+	const uint32_t rx = static_cast<uint32_t>(px), ry = static_cast<uint32_t>(py);
+	const float cx = px - static_cast<float>(rx), cy = py - static_cast<float>(ry);
+	const float* const base = map + static_cast<uint64_t>(ry) * pitch + rx;
+	const float h00 = __ldcg(base), h10 = __ldcg(base + 1), h01 = __ldcg(base + pitch), h11 = __ldcg(base + pitch + 1);
+	HG r;
+	r.h = h00 * (1.0f - cx) * (1.0f - cy) + h10 * cx * (1.0f - cy) + h01 * (1.0f - cx) * cy + h11 * cx * cy;
+	// glm::mix(a, b, t) = a * (1 - t) + b * t
+	r.gx = (h10 - h00) * (1.0f - cy) + (h11 - h01) * cy;
+	r.gy = (h01 - h00) * (1.0f - cx) + (h11 - h10) * cx;
+	return r;
+}
+
+__global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* __restrict__ jobs,
+	const ErosionJob single) {
+	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
+	extern __shared__ unsigned char esm[];
+	int32_t* const bidx = reinterpret_cast<int32_t*>(esm);
+	float* const bw = reinterpret_cast<float*>(esm) + J.brush_size;
+	for (uint32_t k = threadIdx.x; k < J.brush_size; k += kErodeBlock) {
+		bidx[k] = J.brush_index[k];
+		bw[k] = J.brush_weight[k];
+	}
+	__syncthreads();
+
+	const RainParams& P = J.p;
+	const uint32_t d = blockIdx.x * kErodeBlock + threadIdx.x;
+	double residual = 0.0;
+	bool capped = false;
+	if (d < J.count) {
+		float* const map = J.map;
+		const uint64_t pitch = J.pitch;
+		float px = J.starts[2u * d], py = J.starts[2u * d + 1u];
+		float dirx = 0.0f, diry = 0.0f;
+		float speed = P.initSpeed, vol = P.initWaterVolume, sed = 0.0f;
+		const float lo = static_cast<float>(P.BrushRadius);
+		const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
+		uint32_t step = 0u;
+		// A start whose 2x2 bilinear footprint is not inside the map (or is not
+		// a number) dies before its first step, so no access leaves the map.
+		if (!(px >= 0.0f && px < J.dim_x - 1.0f && py >= 0.0f && py < J.dim_y - 1.0f)) {
+			vol = 0.0f;
+		}
+		while (vol >= P.minWaterVolume) {
+			if (step++ >= P.MaxSteps) {
+				capped = true;
+				break;
+			}
+			const uint64_t mi = static_cast<uint64_t>(static_cast<uint32_t>(py)) * pitch + static_cast<uint32_t>(px);
+			const float ox = px - static_cast<float>(static_cast<int>(px)), oy = py - static_cast<float>(static_cast<int>(py));
+			const HG hg = height_gradient(map, pitch, px, py);
+			dirx = (-hg.gx) * (1.0f - P.Inertia) + dirx * P.Inertia;
+			diry = (-hg.gy) * (1.0f - P.Inertia) + diry * P.Inertia;
+			const float len = sqrtf(dirx * dirx + diry * diry);
+			if (len != 0.0f) {
+				dirx /= len;
+				diry /= len;
+			}
+			px += dirx;
+			py += diry;
+			// the reference's border test, written so that a NaN position also dies
+			if ((dirx == 0.0f && diry == 0.0f) || !(px >= lo && px < hi_x && py >= lo && py < hi_y)) {
+				vol = 0.0f;
+				break; // the carried sediment leaves with the droplet
+			}
+			const float dh = height_gradient(map, pitch, px, py).h - hg.h;
+			const float cap = fmaxf(-dh * speed * vol * P.SedimentCapacityFactor, P.minSedimentCapacity);
+			if (sed > cap || dh > 0.0f) {
+				const float dep = (dh > 0.0f) ? fminf(dh, sed) : (sed - cap) * P.DepositSpeed;
+				sed -= dep;
+				atomicAdd(map + mi, dep * (1.0f - ox) * (1.0f - oy));
+				atomicAdd(map + mi + 1, dep * ox * (1.0f - oy));
+				atomicAdd(map + mi + pitch, dep * (1.0f - ox) * oy);
+				atomicAdd(map + mi + pitch + 1, dep * ox * oy);
+			} else {
+				const float ero = fminf((cap - sed) * P.ErodeSpeed, -dh);
+				for (uint32_t b = 0u; b < J.brush_size; b++) {
+					float* const cell = map + static_cast<int64_t>(mi) + bidx[b];
+					const float we = ero * bw[b];
+					const float cur = __ldcg(cell);
+					const float ds = (cur < we) ? cur : we;
+					atomicAdd(cell, -ds);
+					sed += ds;
+				}
+			}
+			speed = sqrtf(fmaxf(0.0f, speed * speed + dh * P.Gravity));
+			speed *= 1.0f - P.Friction;
+			vol *= 1.0f - P.EvaporateSpeed;
+		}
+		residual = static_cast<double>(sed);
+	}
+	if (J.residual) {
+		for (int o = 16; o > 0; o >>= 1) {
+			residual += __shfl_xor_sync(0xFFFFFFFFu, residual, o);
+		}
+		if ((threadIdx.x & 31u) == 0u && residual != 0.0) {
+			atomicAdd(J.residual, residual);
+		}
+	}
+	if (capped && J.status) {
+		atomicOr(J.status, STATUS_TIMEOUT);
+	}
+}
+
+// STPHeightfieldKernel.cu:112-122, eight pixels per thread where rows allow.
+__device__ __forceinline__ uint32_t fmt1(const float h) {
+	return static_cast<uint32_t>(rintf(__saturatef(h) * 65535.0f));
+}
+
+__global__ void format_kernel(const float* __restrict__ in, const uint64_t in_pitch, uint16_t* __restrict__ out,
+	const uint64_t out_pitch, const uint32_t W, const uint32_t H) {
+	const uint32_t groups = (W + 7u) / 8u;
+	const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (t >= static_cast<uint64_t>(groups) * H) {
+		return;
+	}
+	const uint32_t y = static_cast<uint32_t>(t / groups), x0 = static_cast<uint32_t>(t % groups) * 8u;
+	const float* const src = in + y * in_pitch + x0;
+	uint16_t* const dst = out + y * out_pitch + x0;
+	const bool vec = x0 + 8u <= W && (reinterpret_cast<uintptr_t>(src) & 15u) == 0u
+		&& (reinterpret_cast<uintptr_t>(dst) & 15u) == 0u;
+	if (vec) {
+		const float4 a = __ldcs(reinterpret_cast<const float4*>(src));
+		const float4 b = __ldcs(reinterpret_cast<const float4*>(src) + 1);
+		uint4 o;
+		o.x = fmt1(a.x) | (fmt1(a.y) << 16);
+		o.y = fmt1(a.z) | (fmt1(a.w) << 16);
+		o.z = fmt1(b.x) | (fmt1(b.y) << 16);
+		o.w = fmt1(b.z) | (fmt1(b.w) << 16);
+		__stcs(reinterpret_cast<uint4*>(dst), o);
+	} else {
+		for (uint32_t x = x0; x < min(W, x0 + 8u); x++) {
+			out[y * out_pitch + x] = static_cast<uint16_t>(fmt1(in[y * in_pitch + x]));
+		}
+	}
+}
+
+} // namespace
+
+RainParams rain_params(const stpgb_raindrop_setting& s) {
+	RainParams p;
+	p.Inertia = s.Inertia;
+	p.SedimentCapacityFactor = s.SedimentCapacityFactor;
+	p.minSedimentCapacity = s.minSedimentCapacity;
+	p.initWaterVolume = s.initWaterVolume;
+	p.minWaterVolume = s.minWaterVolume;
+	p.Friction = s.Friction;
+	p.initSpeed = s.initSpeed;
+	p.ErodeSpeed = s.ErodeSpeed;
+	p.DepositSpeed = s.DepositSpeed;
+	p.EvaporateSpeed = s.EvaporateSpeed;
+	p.Gravity = s.Gravity;
+	p.BrushRadius = s.ErosionBrushRadius;
+	// The volume shrinks by (1 - EvaporateSpeed) per step: count the steps the
+	// loop test allows, in float exactly as the kernel does, up to 1<<20.
+	uint32_t steps = 0u;
+	float v = s.initWaterVolume;
+	const uint32_t limit = 1u << 20;
+	while (v >= s.minWaterVolume && steps < limit) {
+		v *= 1.0f - s.EvaporateSpeed;
+		steps++;
+	}
+	p.MaxSteps = steps < limit ? steps + 1u : limit;
+	return p;
+}
+
+int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
+	uint32_t max_brush, cudaStream_t stream) {
+	if (max_count == 0u || njobs == 0u) {
+		return STPGB_OK;
+	}
+	const size_t smem = static_cast<size_t>(max_brush) * (sizeof(int32_t) + sizeof(float));
+	if (smem > 48u * 1024u) {
+		STPGB_CUDA_TRY(cudaFuncSetAttribute(erosion_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			static_cast<int>(smem)));
+	}
+	const dim3 grid((max_count + kErodeBlock - 1u) / kErodeBlock, njobs);
+	erosion_kernel<<<grid, kErodeBlock, smem, stream>>>(jobs, single);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
+int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
+	cudaStream_t stream) {
+	const uint64_t threads = static_cast<uint64_t>((W + 7u) / 8u) * H;
+	if (threads == 0u) {
+		return STPGB_OK;
+	}
+	format_kernel<<<static_cast<uint32_t>((threads + 255u) / 256u), 256u, 0, stream>>>(in, in_pitch, out, out_pitch, W, H);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
+} // namespace stpgb
+
+using namespace stpgb;
+
+extern "C" {
+
+int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stpgb_raindrop_setting* setting,
+	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
+	uint32_t brush_size, double* residual_sediment, uint32_t* status, void* stream) {
+	STPGB_TRY(stpgb_raindrop_setting_validate(setting));
+	if (!heightmap || !nn || (count > 0u && !starts_xy) || !brush_index || !brush_weight || brush_size == 0u) {
+		return inval("stpgb_hydraulic_erosion: null pointer or empty brush");
+	}
+	const uint32_t dx = nn->TotalMapSize[0], dy = nn->TotalMapSize[1];
+	if (dx <= 2u * setting->ErosionBrushRadius + 1u || dy <= 2u * setting->ErosionBrushRadius + 1u) {
+		return inval("stpgb_hydraulic_erosion: map smaller than the erosion brush");
+	}
+	if (brush_size > 8192u) {
+		return inval("stpgb_hydraulic_erosion: brush larger than 8192 points");
+	}
+	ErosionJob job;
+	job.map = heightmap;
+	job.dim_x = dx;
+	job.dim_y = dy;
+	job.pitch = dx;
+	job.starts = starts_xy;
+	job.count = count;
+	job.brush_index = brush_index;
+	job.brush_weight = brush_weight;
+	job.brush_size = brush_size;
+	job.p = rain_params(*setting);
+	job.residual = residual_sediment;
+	job.status = status;
+	job.fixed = nullptr;
+	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream));
+}
+
+int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x, uint32_t map_y, void* stream) {
+	if (!in || !out) {
+		return inval("stpgb_format_heightmap: null pointer argument");
+	}
+	return format_launch(in, map_x, out, map_x, map_x, map_y, as_stream(stream));
+}
+
+} // extern "C"

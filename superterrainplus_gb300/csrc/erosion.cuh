@@ -1,0 +1,40 @@
+// Free-slip particle hydraulic erosion: job descriptor and launch.
+#pragma once
+
+#include "internal.hpp"
+
+namespace stpgb {
+
+// Droplet parameters of STPRainDropSetting that the step loop reads.
+struct RainParams {
+	float Inertia, SedimentCapacityFactor, minSedimentCapacity, initWaterVolume, minWaterVolume, Friction,
+		initSpeed, ErodeSpeed, DepositSpeed, EvaporateSpeed, Gravity;
+	uint32_t BrushRadius;
+	uint32_t MaxSteps; // hard cap on the droplet loop
+};
+
+// One merged free-slip map eroded by `count` droplets.
+struct ErosionJob {
+	float* map;
+	uint32_t dim_x, dim_y;
+	uint64_t pitch; // floats per row of `map`
+	const float* starts; // count (x, y) pairs, merged-map coordinates
+	uint32_t count;
+	const int32_t* brush_index; // relative to a row pitch of `pitch`
+	const float* brush_weight;
+	uint32_t brush_size;
+	RainParams p;
+	double* residual;
+	uint32_t* status;
+	uint16_t* fixed; // formatted output (optional, batched path)
+};
+
+RainParams rain_params(const stpgb_raindrop_setting& s);
+
+int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
+	uint32_t max_brush, cudaStream_t stream);
+
+int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
+	cudaStream_t stream);
+
+} // namespace stpgb

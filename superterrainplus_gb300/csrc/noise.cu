@@ -1,0 +1,138 @@
+// Multi-biome fractal simplex heightfield on sm_103a.
+//
+// Per pixel (x, y) of a chunk:  h = sum_bins Weight * (fractal(x, y) * Variation + Depth)
+// (SuperDemo+/Script/STPMultiHeightGenerator.cu:35-72), with the 2D simplex
+// noise and its fractal sum of SuperTerrain+/SuperAlgorithm+/Device/Private/
+// STPSimplexNoise.cu:18-110.  The kernel is FP32-pipe bound.  Two exact
+// rewrites take work out of the inner loop without changing a result:
+//  * the reference hashes a corner as perm[a] % Gradient2DSize and then reads
+//    the gradient; here a 512-entry table of the already-reduced gradient for
+//    every perm slot lives in shared memory, so a corner costs one lookup;
+//  * ((x - half) + offset) / Scale is the same for every octave (the
+//    reference multiplies it by the octave frequency afterwards), so the IEEE
+//    division is done once per bin instead of once per octave.
+#include "noise.cuh"
+
+namespace stpgb {
+
+namespace {
+
+constexpr uint32_t kNoiseBlock = 256u;
+
+// STPSimplexNoise.cu:5-7
+constexpr float kF2 = 0.3660254038f;
+constexpr float kG2 = 0.2113248654f;
+constexpr float kH2 = -1.0f + 2.0f * kG2;
+
+// STPSimplexNoise.cu:14-16: not floorf (an exact negative integer maps one lower)
+__device__ __forceinline__ int floori(const float x) {
+	return x > 0.0f ? static_cast<int>(x) : static_cast<int>(x - 1.0f);
+}
+
+__device__ __forceinline__ float corner(const float dx, const float dy, const float2 g) {
+	float w = 0.5f - dx * dx - dy * dy;
+	if (w <= 0.0f) {
+		return 0.0f;
+	}
+	w *= w;
+	return w * w * (g.x * dx + g.y * dy);
+}
+
+// STPSimplexNoise.cu:18-82
+__device__ __forceinline__ float simplex2d(const uint8_t* __restrict__ perm, const float2* __restrict__ gtab,
+	const float x, const float y) {
+	const float s = (x + y) * kF2;
+	const int i = floori(x + s), j = floori(y + s);
+	const float t = static_cast<float>(i + j) * kG2;
+	const float dx0 = x - (static_cast<float>(i) - t), dy0 = y - (static_cast<float>(j) - t);
+	const unsigned int i1 = (dx0 > dy0) ? 1u : 0u, j1 = 1u - i1;
+	const float dx1 = dx0 - static_cast<float>(i1) + kG2, dy1 = dy0 - static_cast<float>(j1) + kG2;
+	const float dx2 = dx0 + kH2, dy2 = dy0 + kH2;
+	const unsigned int ii = static_cast<unsigned int>(i) & 255u, jj = static_cast<unsigned int>(j) & 255u;
+	const float2 g0 = gtab[ii + perm[jj]];
+	const float2 g1 = gtab[ii + i1 + perm[jj + j1]];
+	const float2 g2 = gtab[ii + 1u + perm[jj + 1u]];
+	return 70.0f * (corner(dx0, dy0, g0) + corner(dx1, dy1, g1) + corner(dx2, dy2, g2));
+}
+
+__global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob* __restrict__ jobs,
+	const NoiseJob single, const stpgb_permutation perm, const stpgb_biome_property* __restrict__ table,
+	const uint32_t biome_count) {
+	__shared__ uint8_t sperm[512];
+	__shared__ float2 gtab[512];
+	for (uint32_t k = threadIdx.x; k < 512u; k += kNoiseBlock) {
+		const uint32_t p = perm.Permutation[k];
+		sperm[k] = static_cast<uint8_t>(p);
+		const uint32_t g = p % perm.Gradient2DSize;
+		gtab[k] = make_float2(perm.Gradient2D[2u * g], perm.Gradient2D[2u * g + 1u]);
+	}
+	__syncthreads();
+
+	const NoiseJob& J = jobs ? jobs[blockIdx.y] : single;
+	const uint64_t npix = static_cast<uint64_t>(J.W) * J.H;
+	const uint64_t idx = static_cast<uint64_t>(blockIdx.x) * kNoiseBlock + threadIdx.x;
+	if (idx >= npix) {
+		return;
+	}
+	const uint32_t x = static_cast<uint32_t>(idx % J.W), y = static_cast<uint32_t>(idx / J.W);
+	// HalfDimension = vec2(MapSize) / 2 (SuperDemo+/World/Biomes/STPCommonCompiler.cpp:236)
+	const float half_x = static_cast<float>(J.W) / 2.0f, half_y = static_cast<float>(J.H) / 2.0f;
+	const float fx = (1.0f * x - half_x) + J.off_x, fy = (1.0f * y - half_y) + J.off_y;
+
+	float height = 0.0f;
+	const uint32_t b0 = J.offsets[idx], b1 = J.offsets[idx + 1u];
+	for (uint32_t b = b0; b < b1; b++) {
+		const uint2 raw = __ldg(reinterpret_cast<const uint2*>(J.bins) + b);
+		const uint32_t id = raw.x & 0xFFFFu;
+		const float weight = __uint_as_float(raw.y);
+		if (id >= biome_count) {
+			continue;
+		}
+		const stpgb_biome_property p = table[id];
+		const float ux = fx / p.Scale, uy = fy / p.Scale;
+		float fractal = 0.0f, amplitude = 1.0f, frequency = 1.0f, range = 0.0f;
+		for (uint32_t o = 0u; o < p.Octave; o++) {
+			fractal += simplex2d(sperm, gtab, ux * frequency, uy * frequency) * amplitude;
+			range += amplitude;
+			amplitude *= p.Persistence;
+			frequency *= p.Lacunarity;
+		}
+		const float f = __saturatef((fractal + range) / (2.0f * range));
+		height += weight * (f * p.Variation + p.Depth);
+	}
+	J.out[static_cast<uint64_t>(y) * J.pitch + x] = height;
+}
+
+} // namespace
+
+int noise_launch(const NoiseJob* jobs, const NoiseJob& single, uint32_t njobs, uint64_t max_pixels,
+	const stpgb_permutation& perm, const stpgb_biome_property* table, uint32_t biome_count, cudaStream_t stream) {
+	const dim3 grid(static_cast<uint32_t>((max_pixels + kNoiseBlock - 1u) / kNoiseBlock), njobs);
+	multibiome_kernel<<<grid, kNoiseBlock, 0, stream>>>(jobs, single, perm, table, biome_count);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
+} // namespace stpgb
+
+using namespace stpgb;
+
+extern "C" int stpgb_multibiome_heightmap(float* heightmap, uint32_t pitch, const uint32_t* offsets,
+	const stpgb_bin* bins, uint32_t map_x, uint32_t map_y, float offset_x, float offset_y,
+	const stpgb_permutation* perm, const stpgb_biome_property* biome_table, uint32_t biome_count, void* stream) {
+	if (!heightmap || !offsets || !perm || !perm->Permutation || !perm->Gradient2D || !biome_table) {
+		return inval("stpgb_multibiome_heightmap: null pointer argument");
+	}
+	if (perm->Gradient2DSize == 0u) {
+		return inval("stpgb_multibiome_heightmap: empty gradient table");
+	}
+	if (pitch < map_x) {
+		return inval("stpgb_multibiome_heightmap: pitch below map width");
+	}
+	if (map_x == 0u || map_y == 0u) {
+		return STPGB_OK;
+	}
+	NoiseJob job { heightmap, pitch, offsets, bins, map_x, map_y, offset_x, offset_y };
+	return noise_launch(nullptr, job, 1u, static_cast<uint64_t>(map_x) * map_y, *perm, biome_table, biome_count,
+		as_stream(stream));
+}

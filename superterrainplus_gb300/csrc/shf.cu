@@ -1,0 +1,454 @@
+// Single histogram filter on sm_103a.
+//
+// Replaces the CPU filter of
+// SuperTerrain+/SuperAlgorithm+/Host/Private/STPSingleHistogramFilter.cpp.
+// The output must be bit-identical to the reference, including the order of
+// the bins inside every histogram.  That order is the insertion order of the
+// reference's accumulator (:400-450): a new item is appended, an item whose
+// count drops to zero is erased and the rest close up.  It depends on the
+// whole history of a sliding window, so each pass keeps the reference's
+// sequential slide per column (vertical pass) and per row (horizontal pass),
+// one thread per column / row, with the accumulator in shared memory; the
+// parallelism comes from the many columns and rows of many chunks at once.
+//
+//   shf_vertical   thread per column k in [0, W+2r): window of rows
+//                  [y-r, y+r] of column sx-r+k, slid down the H rows of the
+//                  central chunk (reference :522-563).  Output: ordered
+//                  (item, count) lists per (k, y) in the workspace.
+//   shf_horizontal thread per row y: window of vertical histograms of
+//                  columns [x, x+2r], slid across the W columns
+//                  (reference :608-679).  COUNT mode sums the bins of the row,
+//                  WRITE mode writes offsets and normalised bins.
+//   shf_rowscan    exclusive prefix over the row totals -> row base offsets.
+//
+// Every pixel's counts sum to (2r+1)^2, so the reference's normalisation
+// factor 1.0f / float(sum) (:495-497) is the same for every pixel.
+#include "shf.cuh"
+
+#include <algorithm>
+
+namespace stpgb {
+
+namespace {
+
+constexpr uint32_t kVBlock = 64u;
+constexpr uint32_t kHBlock = 32u;
+constexpr uint32_t kScanBlock = 256u;
+
+size_t align256(size_t v) {
+	return (v + 255u) & ~static_cast<size_t>(255u);
+}
+
+__device__ __forceinline__ const ShfJob& pick(const ShfJob* jobs, const ShfJob& single) {
+	return jobs ? jobs[blockIdx.y] : single;
+}
+
+__global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict__ jobs, const ShfJob single,
+	const uint32_t kcap) {
+	const ShfJob& J = pick(jobs, single);
+	const uint32_t ncols = J.W + 2u * J.r;
+	const uint32_t k = blockIdx.x * kVBlock + threadIdx.x;
+	if (k >= ncols) {
+		return;
+	}
+	extern __shared__ uint32_t vsm[];
+	uint32_t* const acc = vsm + threadIdx.x; // entry j at acc[j * kVBlock]
+	uint32_t n = 0u;
+	bool overflow = false;
+
+	auto inc = [&](const uint32_t v) {
+		for (uint32_t j = 0u; j < n; j++) {
+			const uint32_t e = acc[j * kVBlock];
+			if ((e >> 16) == v) {
+				acc[j * kVBlock] = e + 1u;
+				return;
+			}
+		}
+		if (n < kcap) {
+			acc[n * kVBlock] = (v << 16) | 1u;
+			n++;
+		} else {
+			overflow = true;
+		}
+	};
+	auto dec = [&](const uint32_t v) {
+		for (uint32_t j = 0u; j < n; j++) {
+			const uint32_t e = acc[j * kVBlock];
+			if ((e >> 16) == v) {
+				if ((e & 0xFFFFu) <= 1u) {
+					for (uint32_t m = j; m + 1u < n; m++) {
+						acc[m * kVBlock] = acc[(m + 1u) * kVBlock];
+					}
+					n--;
+				} else {
+					acc[j * kVBlock] = e - 1u;
+				}
+				return;
+			}
+		}
+	};
+	const uint16_t* const col = J.samplemap + (J.sx - J.r + k);
+	const uint64_t pitch = J.pitch;
+	auto emit = [&](const uint32_t y) {
+		J.vn[static_cast<size_t>(y) * ncols + k] = static_cast<uint16_t>(n);
+		uint32_t* const out = J.vbuf + static_cast<size_t>(y) * kcap * ncols + k;
+		for (uint32_t j = 0u; j < n; j++) {
+			out[static_cast<size_t>(j) * ncols] = acc[j * kVBlock];
+		}
+	};
+
+	for (uint32_t row = J.sy - J.r; row <= J.sy + J.r; row++) {
+		inc(__ldg(col + row * pitch));
+	}
+	emit(0u);
+	for (uint32_t y = 1u; y < J.H; y++) {
+		inc(__ldg(col + static_cast<uint64_t>(J.sy + y + J.r) * pitch));
+		dec(__ldg(col + static_cast<uint64_t>(J.sy + y - 1u - J.r) * pitch));
+		emit(y);
+	}
+	if (overflow) {
+		atomicOr(J.status, STATUS_CAPACITY);
+	}
+}
+
+template<bool Write>
+__global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restrict__ jobs, const ShfJob single,
+	const uint32_t kcap_v, const uint32_t kcap) {
+	const ShfJob& J = pick(jobs, single);
+	const uint32_t y = blockIdx.x * kHBlock + threadIdx.x;
+	if (y >= J.H) {
+		return;
+	}
+	extern __shared__ uint32_t hsm[];
+	uint32_t* const cnt = hsm + threadIdx.x;                                           // [kcap][kHBlock]
+	uint16_t* const item = reinterpret_cast<uint16_t*>(hsm + kcap * kHBlock) + threadIdx.x; // [kcap][kHBlock]
+	uint32_t n = 0u;
+	bool overflow = false;
+
+	auto inc = [&](const uint32_t v, const uint32_t c) {
+		for (uint32_t j = 0u; j < n; j++) {
+			if (item[j * kHBlock] == v) {
+				cnt[j * kHBlock] += c;
+				return;
+			}
+		}
+		if (n < kcap) {
+			item[n * kHBlock] = static_cast<uint16_t>(v);
+			cnt[n * kHBlock] = c;
+			n++;
+		} else {
+			overflow = true;
+		}
+	};
+	auto dec = [&](const uint32_t v, const uint32_t c) {
+		for (uint32_t j = 0u; j < n; j++) {
+			if (item[j * kHBlock] == v) {
+				if (cnt[j * kHBlock] <= c) {
+					for (uint32_t m = j; m + 1u < n; m++) {
+						item[m * kHBlock] = item[(m + 1u) * kHBlock];
+						cnt[m * kHBlock] = cnt[(m + 1u) * kHBlock];
+					}
+					n--;
+				} else {
+					cnt[j * kHBlock] -= c;
+				}
+				return;
+			}
+		}
+	};
+	const uint32_t ncols = J.W + 2u * J.r;
+	const uint16_t* const vn = J.vn + static_cast<size_t>(y) * ncols;
+	const uint32_t* const vrow = J.vbuf + static_cast<size_t>(y) * kcap_v * ncols;
+	auto add_col = [&](const uint32_t kc) {
+		const uint32_t nv = vn[kc];
+		for (uint32_t j = 0u; j < nv; j++) {
+			const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+			inc(e >> 16, e & 0xFFFFu);
+		}
+	};
+	auto sub_col = [&](const uint32_t kc) {
+		const uint32_t nv = vn[kc];
+		for (uint32_t j = 0u; j < nv; j++) {
+			const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+			dec(e >> 16, e & 0xFFFFu);
+		}
+	};
+
+	const uint32_t side = 2u * J.r + 1u;
+	const float norm = 1.0f / static_cast<float>(side * side);
+	uint64_t running = Write ? J.rows[y] : 0u;
+	uint32_t* const off_row = J.offsets + static_cast<size_t>(y) * J.W;
+	uint2* const bins = reinterpret_cast<uint2*>(J.bins);
+	auto emit = [&](const uint32_t x) {
+		if constexpr (Write) {
+			off_row[x] = static_cast<uint32_t>(running);
+			for (uint32_t j = 0u; j < n; j++) {
+				const uint64_t o = running + j;
+				if (o < J.bins_capacity) {
+					const float w = __fmul_rn(__uint2float_rn(cnt[j * kHBlock]), norm);
+					bins[o] = make_uint2(item[j * kHBlock], __float_as_uint(w));
+				}
+			}
+		}
+		running += n;
+	};
+
+	for (uint32_t kc = 0u; kc < side; kc++) {
+		add_col(kc);
+	}
+	emit(0u);
+	for (uint32_t x = 1u; x < J.W; x++) {
+		add_col(x + 2u * J.r);
+		sub_col(x - 1u);
+		emit(x);
+	}
+	if constexpr (!Write) {
+		J.rows[y] = static_cast<uint32_t>(min(running, static_cast<uint64_t>(0xFFFFFFFFu)));
+	}
+	if (overflow) {
+		atomicOr(J.status, STATUS_CAPACITY);
+	}
+}
+
+// One block per job: rows[0..H) -> exclusive prefix, rows[H] = total;
+// offsets[W*H] = total.
+__global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restrict__ jobs, const ShfJob single) {
+	const ShfJob& J = pick(jobs, single);
+	__shared__ uint64_t warp_sum[kScanBlock / 32u];
+	__shared__ uint64_t carry_s;
+	if (threadIdx.x == 0u) {
+		carry_s = 0u;
+	}
+	__syncthreads();
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	for (uint32_t base = 0u; base < J.H; base += kScanBlock) {
+		const uint32_t i = base + threadIdx.x;
+		const uint64_t v = i < J.H ? J.rows[i] : 0u;
+		uint64_t s = v;
+#pragma unroll
+		for (uint32_t d = 1u; d < 32u; d <<= 1) {
+			const uint64_t t = __shfl_up_sync(0xFFFFFFFFu, s, d);
+			if (lane >= d) {
+				s += t;
+			}
+		}
+		if (lane == 31u) {
+			warp_sum[warp] = s;
+		}
+		__syncthreads();
+		uint64_t wbase = 0u;
+		for (uint32_t w = 0u; w < warp; w++) {
+			wbase += warp_sum[w];
+		}
+		const uint64_t carry = carry_s;
+		const uint64_t excl = carry + wbase + s - v;
+		if (i < J.H) {
+			J.rows[i] = static_cast<uint32_t>(min(excl, static_cast<uint64_t>(0xFFFFFFFFu)));
+		}
+		__syncthreads();
+		if (threadIdx.x == kScanBlock - 1u) {
+			carry_s = carry + wbase + s;
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0u) {
+		const uint64_t total = carry_s;
+		J.rows[J.H] = static_cast<uint32_t>(min(total, static_cast<uint64_t>(0xFFFFFFFFu)));
+		J.offsets[static_cast<size_t>(J.W) * J.H] = static_cast<uint32_t>(min(total, static_cast<uint64_t>(0xFFFFFFFFu)));
+		if (total > J.bins_capacity || total > 0xFFFFFFFFull) {
+			atomicOr(J.status, STATUS_CAPACITY);
+		}
+	}
+}
+
+bool g_attr_set = false;
+
+} // namespace
+
+uint32_t shf_kcap_v(uint32_t r, uint32_t max_items) {
+	return std::min<uint32_t>(2u * r + 1u, max_items);
+}
+
+uint32_t shf_kcap_h(uint32_t r, uint32_t max_items) {
+	const uint64_t side = 2ull * r + 1ull;
+	return static_cast<uint32_t>(std::min<uint64_t>(side * side, max_items));
+}
+
+ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
+	const size_t ncols = static_cast<size_t>(W) + 2u * r;
+	ShfLayout l;
+	l.vbuf = 0u;
+	l.vn = align256(static_cast<size_t>(H) * kcap_v * ncols * sizeof(uint32_t));
+	l.rows = l.vn + align256(static_cast<size_t>(H) * ncols * sizeof(uint16_t));
+	l.total = l.rows + align256((static_cast<size_t>(H) + 1u) * sizeof(uint32_t));
+	return l;
+}
+
+int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
+	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream) {
+	if (!g_attr_set) {
+		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_vertical, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+		g_attr_set = true;
+	}
+	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * sizeof(uint32_t);
+	const size_t hsmem = static_cast<size_t>(kcap_h) * kHBlock * (sizeof(uint32_t) + sizeof(uint16_t));
+	const dim3 vgrid((max_W + 2u * max_r + kVBlock - 1u) / kVBlock, njobs);
+	const dim3 hgrid((max_H + kHBlock - 1u) / kHBlock, njobs);
+	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	shf_horizontal<false><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	shf_rowscan<<<dim3(1u, njobs), kScanBlock, 0, stream>>>(jobs, single);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	shf_horizontal<true><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
+namespace {
+
+int check_shf_args(const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items, uint32_t& sx, uint32_t& sy) {
+	if (!nn) {
+		return inval("stpgb_shf: null neighbour information");
+	}
+	if (nn->MapSize[0] == 0u || nn->MapSize[1] == 0u || nn->ChunkNearestNeighbour[0] == 0u
+		|| nn->ChunkNearestNeighbour[1] == 0u) {
+		return inval("stpgb_shf: empty map or neighbourhood");
+	}
+	if (nn->TotalMapSize[0] != nn->MapSize[0] * nn->ChunkNearestNeighbour[0]
+		|| nn->TotalMapSize[1] != nn->MapSize[1] * nn->ChunkNearestNeighbour[1]) {
+		return inval("stpgb_shf: TotalMapSize must equal MapSize * ChunkNearestNeighbour");
+	}
+	// STPSingleHistogramFilter.cpp:874-880
+	if (!(radius > 0u && (radius & 1u) == 0u)) {
+		return inval("radius should be an positive even number");
+	}
+	sx = nn->MapSize[0] * (nn->ChunkNearestNeighbour[0] / 2u);
+	sy = nn->MapSize[1] * (nn->ChunkNearestNeighbour[1] / 2u);
+	if (radius > sx || radius > sy) {
+		return inval("radius is too large and will overflow nearest neighbour boundary");
+	}
+	if (max_items > kShfMaxItems) {
+		return inval("stpgb_shf: max_items above the library bound of 256");
+	}
+	return STPGB_OK;
+}
+
+} // namespace
+
+} // namespace stpgb
+
+using namespace stpgb;
+
+extern "C" {
+
+int stpgb_shf_workspace_size(const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items, size_t* bytes) {
+	uint32_t sx, sy;
+	STPGB_TRY(check_shf_args(nn, radius, max_items, sx, sy));
+	if (max_items == 0u) {
+		max_items = kShfMaxItems;
+	}
+	*bytes = shf_layout(nn->MapSize[0], nn->MapSize[1], radius, shf_kcap_v(radius, max_items)).total;
+	return STPGB_OK;
+}
+
+int stpgb_shf_filter(const uint16_t* samplemap, const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items,
+	void* workspace, size_t workspace_bytes, uint32_t* offsets, stpgb_bin* bins, uint64_t bins_capacity,
+	uint32_t* status, void* stream) {
+	uint32_t sx, sy;
+	STPGB_TRY(check_shf_args(nn, radius, max_items, sx, sy));
+	if (max_items == 0u) {
+		max_items = kShfMaxItems;
+	}
+	if (!samplemap || !offsets || (!bins && bins_capacity > 0u) || !status) {
+		return inval("stpgb_shf_filter: null pointer argument");
+	}
+	const uint32_t W = nn->MapSize[0], H = nn->MapSize[1];
+	const uint32_t kv = shf_kcap_v(radius, max_items), kh = shf_kcap_h(radius, max_items);
+	const ShfLayout l = shf_layout(W, H, radius, kv);
+	if (!workspace || workspace_bytes < l.total) {
+		set_error("stpgb_shf_filter: workspace smaller than stpgb_shf_workspace_size");
+		return STPGB_ECAPACITY;
+	}
+	const cudaStream_t s = as_stream(stream);
+	STPGB_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t), s));
+	unsigned char* ws = static_cast<unsigned char*>(workspace);
+	ShfJob job;
+	job.samplemap = samplemap;
+	job.pitch = nn->TotalMapSize[0];
+	job.W = W;
+	job.H = H;
+	job.sx = sx;
+	job.sy = sy;
+	job.r = radius;
+	job.kcap_v = kv;
+	job.vbuf = reinterpret_cast<uint32_t*>(ws + l.vbuf);
+	job.vn = reinterpret_cast<uint16_t*>(ws + l.vn);
+	job.rows = reinterpret_cast<uint32_t*>(ws + l.rows);
+	job.offsets = offsets;
+	job.bins = bins;
+	job.bins_capacity = bins_capacity;
+	job.status = status;
+	return shf_launch(nullptr, job, 1u, W, H, radius, kv, kh, s);
+}
+
+int stpgb_status_check(const uint32_t* status, void* stream) {
+	uint32_t h = 0u;
+	STPGB_CUDA_TRY(cudaMemcpyAsync(&h, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, as_stream(stream)));
+	STPGB_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+	if (h & STATUS_CAPACITY) {
+		set_error("device status: an output capacity or the per-window item bound was exceeded");
+		return STPGB_ECAPACITY;
+	}
+	if (h & STATUS_TIMEOUT) {
+		set_error("device status: a droplet reached the step cap");
+		return STPGB_ETIMEOUT;
+	}
+	return STPGB_OK;
+}
+
+int stpgb_shf_filter_host(const uint16_t* samplemap_host, const stpgb_nn_info* nn, uint32_t radius,
+	uint32_t* offsets_host, stpgb_bin* bins_host, uint64_t bins_capacity, uint64_t* nbins) {
+	uint32_t sx, sy;
+	STPGB_TRY(check_shf_args(nn, radius, 0u, sx, sy));
+	const uint32_t W = nn->MapSize[0], H = nn->MapSize[1];
+	const size_t in_bytes = static_cast<size_t>(nn->TotalMapSize[0]) * nn->TotalMapSize[1] * sizeof(uint16_t);
+	const size_t npix = static_cast<size_t>(W) * H;
+	size_t ws_bytes = 0u;
+	STPGB_TRY(stpgb_shf_workspace_size(nn, radius, 0u, &ws_bytes));
+	// a window holds at most min((2r+1)^2, 256) distinct values
+	const uint64_t cap = npix * shf_kcap_h(radius, kShfMaxItems);
+	struct Scoped {
+		void* p = nullptr;
+		~Scoped() {
+			if (p) {
+				cudaFree(p);
+			}
+		}
+	} d_in, d_ws, d_off, d_bins, d_status;
+	STPGB_CUDA_TRY(cudaMalloc(&d_in.p, in_bytes));
+	STPGB_CUDA_TRY(cudaMalloc(&d_ws.p, ws_bytes));
+	STPGB_CUDA_TRY(cudaMalloc(&d_off.p, (npix + 1u) * sizeof(uint32_t)));
+	STPGB_CUDA_TRY(cudaMalloc(&d_bins.p, std::max<uint64_t>(cap, 1u) * sizeof(stpgb_bin)));
+	STPGB_CUDA_TRY(cudaMalloc(&d_status.p, sizeof(uint32_t)));
+	cudaStream_t s = nullptr;
+	STPGB_CUDA_TRY(cudaMemcpy(d_in.p, samplemap_host, in_bytes, cudaMemcpyHostToDevice));
+	STPGB_TRY(stpgb_shf_filter(static_cast<uint16_t*>(d_in.p), nn, radius, 0u, d_ws.p, ws_bytes,
+		static_cast<uint32_t*>(d_off.p), static_cast<stpgb_bin*>(d_bins.p), cap, static_cast<uint32_t*>(d_status.p), s));
+	STPGB_TRY(stpgb_status_check(static_cast<uint32_t*>(d_status.p), s));
+	STPGB_CUDA_TRY(cudaMemcpy(offsets_host, d_off.p, (npix + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+	const uint64_t total = offsets_host[npix];
+	*nbins = total;
+	if (total > bins_capacity) {
+		set_error("stpgb_shf_filter_host: bins capacity too small");
+		return STPGB_ECAPACITY;
+	}
+	if (total > 0u) {
+		STPGB_CUDA_TRY(cudaMemcpy(bins_host, d_bins.p, total * sizeof(stpgb_bin), cudaMemcpyDeviceToHost));
+	}
+	return STPGB_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,33 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle.oracle import Oracle
+    return Oracle()
+
+
+@pytest.fixture(scope="session")
+def stpgb():
+    import superterrainplus_gb300 as m
+    m.lib()
+    return m
+
+
+@pytest.fixture(scope="session")
+def dev(stpgb):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return stpgb.DeviceOps()

@@ -1,0 +1,93 @@
+"""Shared helpers of the test suite: fixture loading and seeded inputs."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_shf_kat():
+    return dict(np.load(os.path.join(GOLDEN, "shf_kat.npz")))
+
+
+def shf_small_cases(oracle):
+    """Yields (name, samplemap, map_size, nn, radius, offsets, items, weights) from the reference fixtures."""
+    z = np.load(os.path.join(GOLDEN, "shf_cases.npz"))
+    for i in range(int(z["count"])):
+        mx, my, nx, ny, r, seed = (int(v) for v in z[f"c{i}_meta"])
+        kind = str(z[f"c{i}_kind"])
+        param = tuple(int(v) for v in z[f"c{i}_param"])
+        sm = sample_map(kind, mx, my, nx, ny, param, seed, oracle, stored=z.get(f"c{i}_input"))
+        yield (f"{kind}-{mx}x{my}-r{r}", sm, (mx, my), (nx, ny), r, z[f"c{i}_offsets"], z[f"c{i}_items"],
+               z[f"c{i}_weights"])
+
+
+def shf_large_cases(oracle):
+    z = np.load(os.path.join(GOLDEN, "shf_cases.npz"))
+    with open(os.path.join(GOLDEN, "shf_digests.json")) as f:
+        cases = json.load(f)
+    for j, c in enumerate(cases):
+        mx, my = c["map"]
+        nx, ny = c["nn"]
+        sm = sample_map(c["kind"], mx, my, nx, ny, tuple(c["param"]), c["seed"], oracle,
+                        stored=z.get(f"large{j}_input"))
+        yield c, sm
+
+
+def sample_map(kind, mx, my, nx, ny, param, seed, oracle, stored=None):
+    w, h = mx * nx, my * ny
+    if stored is not None:
+        return np.asarray(stored, np.uint16).reshape(h, w)
+    if kind == "constant":
+        return np.full((h, w), seed % 7, np.uint16)
+    if kind == "voronoi":
+        cell, biomes = param
+        return oracle.voronoi(w, h, (-mx * (nx // 2), -my * (ny // 2)), cell, biomes, seed)
+    raise ValueError(kind)
+
+
+def digest(offsets, items, weights):
+    import hashlib
+    m = hashlib.sha256()
+    m.update(np.ascontiguousarray(offsets, np.uint32).tobytes())
+    m.update(np.ascontiguousarray(items, np.uint16).tobytes())
+    m.update(np.ascontiguousarray(weights, np.float32).tobytes())
+    return m.hexdigest()
+
+
+def load_permutations():
+    z = np.load(os.path.join(GOLDEN, "permutation.npz"))
+    for i in range(int(z["count"])):
+        seed, n = (int(v) for v in z[f"p{i}_setting"])
+        yield seed, n, float(z[f"p{i}_offset"]), z[f"p{i}_perm"], z[f"p{i}_grad"]
+
+
+def biome_table(n, seed):
+    """Seeded multi-biome parameters (octaves 4-8, Scale log-uniform 64-512,
+    Variation 0.2-1.0, Depth 0, persistence 0.5, lacunarity 2)."""
+    from superterrainplus_gb300 import BIOME_DTYPE
+    rng = np.random.default_rng(seed)
+    t = np.zeros(n, BIOME_DTYPE)
+    t["Scale"] = np.exp(rng.uniform(np.log(64.0), np.log(512.0), n)).astype(np.float32)
+    t["Octave"] = rng.integers(4, 9, n)
+    t["Persistence"] = 0.5
+    t["Lacunarity"] = 2.0
+    t["Depth"] = 0.0
+    t["Variation"] = rng.uniform(0.2, 1.0, n).astype(np.float32)
+    return t
+
+
+def raindrop_dict(count, radius=3, lifetime=30, seed=42):
+    """Droplet settings of the small plain-method workload (inertia 0.05,
+    capacity 4, min capacity 0.01, deposit 0.3, erode 0.3, evaporate 0.01,
+    gravity 4); initWaterVolume 1, initSpeed 1, Friction 0.1 as the demo's
+    Engine.ini; the lifetime is set through minWaterVolume."""
+    evap = 0.01
+    v = np.float32(1.0)
+    for _ in range(lifetime):
+        v = np.float32(v * np.float32(1.0 - np.float32(evap)))
+    minv = float(np.nextafter(v, np.float32(np.inf)))
+    return dict(Seed=seed, RainDropCount=count, Inertia=0.05, SedimentCapacityFactor=4.0, minSedimentCapacity=0.01,
+                initWaterVolume=1.0, minWaterVolume=minv, Friction=0.1, initSpeed=1.0, ErodeSpeed=0.3,
+                DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0, ErosionBrushRadius=radius)

@@ -1,0 +1,141 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry point
+declared in include/stpgb.h, and its host-side paths (permutation table,
+erosion brush, setting validation, argument checks) match the oracle and the
+reference's error behaviour."""
+import ctypes as C
+import math
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import helpers
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            names += re.findall(r"STPGB_API\s+[\w\s\*]+?\b(stpgb_\w+)\s*\(", text)
+    return names
+
+
+def test_exports_every_declared_symbol(stpgb):
+    from superterrainplus_gb300 import _capi
+    names = declared_symbols()
+    assert len(names) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", _capi.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (stpgb_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(stpgb.lib(), n)
+    # nothing but the C ABI leaks out
+    assert all(s.startswith("stpgb_") for s in exported)
+
+
+def test_permutation_matches_oracle_and_reference(stpgb, oracle):
+    for seed, n, offset, perm, grad in helpers.load_permutations():
+        p, g = stpgb.permutation_generate(seed, n, offset)
+        assert np.array_equal(p, perm)
+        assert np.array_equal(g.view(np.uint32), grad.view(np.uint32))
+    p, g = stpgb.permutation_generate(6666, 10, math.radians(6.5))
+    _, po, go = oracle.permutation(6666, 10, math.radians(6.5))
+    assert np.array_equal(p, po) and np.array_equal(g, go)
+
+
+def test_permutation_invalid(stpgb):
+    with pytest.raises(stpgb.STPInvalidEnvironment):
+        stpgb.permutation_generate(1, 0, 0.0)
+    with pytest.raises(stpgb.STPInvalidEnvironment):
+        stpgb.permutation_generate(1, 8, 7.0)
+
+
+def test_permutation_overflowing_distribution(stpgb, oracle):
+    """Distributions whose angle loop runs once more in the reference still give N entries, no overrun."""
+    for n in (6, 11, 13):
+        p, g = stpgb.permutation_generate(5, n, 0.5)
+        rc, po, go = oracle.permutation(5, n, 0.5)
+        assert rc == 2
+        assert np.array_equal(g, go)
+
+
+@pytest.mark.parametrize("radius", [1, 2, 3, 4, 5, 8])
+def test_brush_matches_oracle(stpgb, oracle, radius):
+    for dim in (64, 1536, 3072):
+        i1, w1 = stpgb.erosion_brush(dim, radius)
+        i2, w2 = oracle.brush(dim, radius)
+        assert np.array_equal(i1, i2)
+        assert np.array_equal(w1.view(np.uint32), w2.view(np.uint32))
+
+
+def test_brush_invalid(stpgb):
+    with pytest.raises(stpgb.STPNumericDomainError):
+        stpgb.erosion_brush(64, 0)
+    with pytest.raises(stpgb.STPNumericDomainError):
+        stpgb.erosion_brush(0, 3)
+
+
+def test_raindrop_validation(stpgb):
+    L = stpgb.lib()
+    good = stpgb.RaindropSetting(**helpers.raindrop_dict(100))
+    assert L.stpgb_raindrop_setting_validate(C.byref(good)) == 0
+    for field, bad in (("RainDropCount", 0), ("Inertia", 1.5), ("SedimentCapacityFactor", 0.0), ("Gravity", 0.0),
+                       ("ErosionBrushRadius", 0), ("EvaporateSpeed", -0.1), ("Friction", 2.0)):
+        s = stpgb.RaindropSetting(**helpers.raindrop_dict(100))
+        setattr(s, field, bad)
+        assert L.stpgb_raindrop_setting_validate(C.byref(s)) == 1, field
+
+
+def test_lifetime_helper(stpgb):
+    for life in (1, 30, 50, 64):
+        v = stpgb.lifetime_min_water_volume(1.0, 0.01, life)
+        vol, steps = np.float32(1.0), 0
+        while vol >= np.float32(v):
+            vol = np.float32(vol * np.float32(1.0 - np.float32(0.01)))
+            steps += 1
+        assert steps == life
+
+
+def test_shf_argument_errors_without_gpu(stpgb):
+    """Radius checks of STPSingleHistogramFilter.cpp:874-880 fire before any device work."""
+    kat = helpers.load_shf_kat()
+    f = stpgb.STPSingleHistogramFilter()
+    buf = stpgb.STPFilterBuffer(stpgb.STPFilterBuffer.Serial)
+    info = stpgb.NNInfo.make((4, 4), (3, 3))
+    for r in (0, 3, 128):
+        with pytest.raises(stpgb.STPNumericDomainError):
+            f(kat["texture"], info, buf, r)
+    with pytest.raises(stpgb.STPException):
+        stpgb.STPFilterBuffer(7)
+
+
+def test_generator_invalid_settings_without_gpu(stpgb):
+    cs = stpgb.ChunkSetting()
+    cs.MapSize[:] = [64, 64]
+    cs.DiversityNearestNeighbour[:] = [3, 3]
+    cs.ErosionNearestNeighbour[:] = [2, 3]  # must be odd
+    rd = stpgb.RaindropSetting(**helpers.raindrop_dict(100))
+    sx = stpgb.SimplexSetting(1, 8, 0.2)
+    table = helpers.biome_table(2, 0)
+    with pytest.raises(stpgb.STPInvalidEnvironment):
+        stpgb.STPHeightfieldGenerator(cs, rd, sx, table, 8)
+    cs.ErosionNearestNeighbour[:] = [3, 3]
+    rd.Inertia = 2.0
+    with pytest.raises(stpgb.STPInvalidEnvironment):
+        stpgb.STPHeightfieldGenerator(cs, rd, sx, table, 8)
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    from superterrainplus_gb300 import _capi
+    monkeypatch.setattr(_capi, "LIB_PATH", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(_capi, "_lib", None)
+    with pytest.raises(ImportError):
+        _capi.lib()
