@@ -284,6 +284,78 @@ STPGB_API int stpgb_generator_erode_starts(stpgb_generator* gen, float* const* h
 	uint16_t* const* heightfield_fixed, const float* starts_xy, uint32_t count,
 	double* residual_sediment);
 
+/* ------------------------------------------------------ batched pipeline -- */
+
+/* No counterpart in the reference, which generates one chunk per call: many
+ * eroded-chunk requests, each a 3x3 free-slip neighbourhood of MapSize^2
+ * chunks around world chunk (ChunkX, ChunkY), filtered, generated and eroded
+ * together by one fixed sequence of batched launches (every launch covers
+ * every chunk of every request), optionally captured in a CUDA graph. */
+typedef struct stpgb_batch stpgb_batch;
+
+typedef struct stpgb_batch_request {
+	uint32_t MapSize;             /* chunk side, a positive multiple of 8 */
+	int32_t ChunkX, ChunkY;       /* world chunk coordinate of the centre chunk */
+	uint32_t InterpolationRadius; /* filter radius (even, <= MapSize) */
+	uint32_t DropletCount;
+	uint32_t BrushRadius;
+	uint32_t Lifetime;            /* droplet steps; 0 keeps the base minWaterVolume */
+} stpgb_batch_request;
+
+enum { STPGB_BATCH_GRAPH = 1 };
+
+/* Lays out and allocates every buffer of the batch on the current device in
+ * one allocation (STPGB_ENOMEM if it exceeds `hbm_budget` bytes; 0 = no
+ * budget), builds the job tables and, with STPGB_BATCH_GRAPH, captures the
+ * launch sequence into a CUDA graph.  `base` supplies the droplet settings
+ * a request does not override; `biome_table` is indexed by biome ID. */
+STPGB_API int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count,
+	const stpgb_raindrop_setting* base, const stpgb_simplex_setting* simplex,
+	const stpgb_biome_property* biome_table, uint32_t biome_count, uint64_t hbm_budget,
+	uint32_t flags, stpgb_batch** out);
+STPGB_API int stpgb_batch_destroy(stpgb_batch* batch);
+STPGB_API uint64_t stpgb_batch_device_bytes(const stpgb_batch* batch);
+
+/* Device buffers of one request: the 5x5-chunk biome region (uint16,
+ * (5*MapSize)^2 row-major, the diversity neighbourhoods of all nine chunks),
+ * the merged 3x3 float heightmap and its uint16 format ((3*MapSize)^2), and
+ * the droplet start array (2*DropletCount floats).  Any may be NULL. */
+STPGB_API int stpgb_batch_buffers(stpgb_batch* batch, uint32_t request, uint16_t** biome_region,
+	float** heightmap, uint16_t** heightmap_fixed, float** starts_xy);
+
+/* Fills every request's biome region with the seeded Voronoi map (global
+ * coordinates, so neighbouring requests agree) and its starts with the
+ * Philox stream of the base Seed. Asynchronous. */
+STPGB_API int stpgb_batch_synthesize_inputs(stpgb_batch* batch, uint32_t voronoi_cell, uint64_t seed,
+	void* stream);
+
+/* Runs the whole batch (graph launch when captured). Asynchronous. */
+STPGB_API int stpgb_batch_run(stpgb_batch* batch, void* stream);
+
+/* Runs the same work as the plain per-chunk call sequence (one chunk's
+ * filter + noise per call, one erosion per request, a stream synchronise
+ * after every call).  Synchronous; the baseline the batched path is
+ * compared with. */
+STPGB_API int stpgb_batch_run_plain(stpgb_batch* batch, void* stream);
+
+/* HOST <-> device copies of the inputs and results, enqueued on `stream`. */
+STPGB_API int stpgb_batch_upload(stpgb_batch* batch, const uint16_t* const* biome_regions,
+	const float* const* starts_xy, void* stream);
+STPGB_API int stpgb_batch_download(stpgb_batch* batch, float* const* heightmaps,
+	uint16_t* const* heightmaps_fixed, double* residual_sediment, void* stream);
+
+/* Synchronises `stream` and decodes the batch's device status word. */
+STPGB_API int stpgb_batch_status(stpgb_batch* batch, void* stream);
+
+/* One stage of the batch on its own (0 filter, 1 noise, 2 erosion,
+ * 3 format), for per-kernel timing. Asynchronous. */
+STPGB_API int stpgb_batch_run_stage(stpgb_batch* batch, uint32_t stage, void* stream);
+
+/* Realised droplet steps and brush-erosion steps summed over the runs since
+ * the last reset (synchronises the device). */
+STPGB_API int stpgb_batch_counters(stpgb_batch* batch, uint64_t* realised_steps, uint64_t* erode_steps,
+	int reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -160,6 +160,81 @@ class STPHeightfieldGenerator:
         return res.value
 
 
+# ------------------------------------------------------- batched pipeline
+
+
+class Batch:
+    """Many eroded-chunk requests through one batched launch sequence (stpgb_batch_*).
+
+    `requests`: iterable of dicts with MapSize, ChunkX, ChunkY, InterpolationRadius,
+    DropletCount, BrushRadius, Lifetime.  `stream` arguments are raw
+    cudaStream_t values (int) or None for the legacy default stream."""
+
+    def __init__(self, requests, base_setting, simplex_setting, biome_table, hbm_budget=0, graph=True):
+        from ._capi import STPGB_BATCH_GRAPH, BatchRequest
+        reqs = list(requests)
+        arr = (BatchRequest * len(reqs))(*[BatchRequest(**r) for r in reqs])
+        table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
+        h = C.c_void_p()
+        rc = lib().stpgb_batch_create(arr, len(reqs), C.byref(base_setting), C.byref(simplex_setting), _p(table),
+                                      len(table), hbm_budget, STPGB_BATCH_GRAPH if graph else 0, C.byref(h))
+        check(rc)
+        self._h = h
+        self.requests = reqs
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().stpgb_batch_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _s(stream):
+        return C.c_void_p(stream or 0)
+
+    @property
+    def device_bytes(self):
+        return int(lib().stpgb_batch_device_bytes(self._h))
+
+    def buffers(self, i):
+        b, hgt, fx, st = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(lib().stpgb_batch_buffers(self._h, i, C.byref(b), C.byref(hgt), C.byref(fx), C.byref(st)))
+        return b.value, hgt.value, fx.value, st.value
+
+    def synthesize(self, voronoi_cell, seed, stream=None):
+        check(lib().stpgb_batch_synthesize_inputs(self._h, voronoi_cell, seed, self._s(stream)))
+
+    def run(self, stream=None):
+        check(lib().stpgb_batch_run(self._h, self._s(stream)))
+
+    def run_plain(self, stream=None):
+        check(lib().stpgb_batch_run_plain(self._h, self._s(stream)))
+
+    def run_stage(self, stage, stream=None):
+        check(lib().stpgb_batch_run_stage(self._h, stage, self._s(stream)))
+
+    def upload(self, biome_regions, starts=None, stream=None):
+        n = len(self.requests)
+        bp = (C.c_void_p * n)(*[a.ctypes.data for a in biome_regions])
+        sp = (C.c_void_p * n)(*[a.ctypes.data for a in starts]) if starts is not None else None
+        check(lib().stpgb_batch_upload(self._h, bp, sp, self._s(stream)))
+
+    def download(self, heights=None, fixed=None, residual=None, stream=None):
+        n = len(self.requests)
+        hp = (C.c_void_p * n)(*[a.ctypes.data for a in heights]) if heights is not None else None
+        fp = (C.c_void_p * n)(*[a.ctypes.data for a in fixed]) if fixed is not None else None
+        rp = residual.ctypes.data_as(C.c_void_p) if residual is not None else None
+        check(lib().stpgb_batch_download(self._h, hp, fp, rp, self._s(stream)))
+
+    def status(self, stream=None):
+        check(lib().stpgb_batch_status(self._h, self._s(stream)))
+
+    def counters(self, reset=True):
+        a, b = C.c_uint64(0), C.c_uint64(0)
+        check(lib().stpgb_batch_counters(self._h, C.byref(a), C.byref(b), int(reset)))
+        return a.value, b.value
+
+
 # --------------------------------------------- kernel-level device calls
 
 

@@ -89,6 +89,14 @@ class ChunkSetting(C.Structure):
 vp, u16, u32, u64, i32, i64, f32, f64, sz = (C.c_void_p, C.c_uint16, C.c_uint32, C.c_uint64, C.c_int32,
                                              C.c_int64, C.c_float, C.c_double, C.c_size_t)
 
+class BatchRequest(C.Structure):
+    _fields_ = [("MapSize", C.c_uint32), ("ChunkX", C.c_int32), ("ChunkY", C.c_int32),
+                ("InterpolationRadius", C.c_uint32), ("DropletCount", C.c_uint32), ("BrushRadius", C.c_uint32),
+                ("Lifetime", C.c_uint32)]
+
+
+STPGB_BATCH_GRAPH = 1
+
 # name -> (restype, argtypes); the single source of the binding
 PROTOTYPES = {
     "stpgb_last_error": (C.c_char_p, []),
@@ -115,6 +123,19 @@ PROTOTYPES = {
     "stpgb_generator_generate": (C.c_int, [vp, vp, vp, f32, f32]),
     "stpgb_generator_erode": (C.c_int, [vp, vp, vp]),
     "stpgb_generator_erode_starts": (C.c_int, [vp, vp, vp, vp, u32, C.POINTER(f64)]),
+    "stpgb_batch_create": (C.c_int, [C.POINTER(BatchRequest), u32, C.POINTER(RaindropSetting),
+                                     C.POINTER(SimplexSetting), vp, u32, u64, u32, C.POINTER(vp)]),
+    "stpgb_batch_destroy": (C.c_int, [vp]),
+    "stpgb_batch_device_bytes": (u64, [vp]),
+    "stpgb_batch_buffers": (C.c_int, [vp, u32, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "stpgb_batch_synthesize_inputs": (C.c_int, [vp, u32, u64, vp]),
+    "stpgb_batch_run": (C.c_int, [vp, vp]),
+    "stpgb_batch_run_plain": (C.c_int, [vp, vp]),
+    "stpgb_batch_upload": (C.c_int, [vp, vp, vp, vp]),
+    "stpgb_batch_download": (C.c_int, [vp, vp, vp, vp, vp]),
+    "stpgb_batch_status": (C.c_int, [vp, vp]),
+    "stpgb_batch_run_stage": (C.c_int, [vp, u32, vp]),
+    "stpgb_batch_counters": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64), C.c_int]),
 }
 
 _lib = None

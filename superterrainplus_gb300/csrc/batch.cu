@@ -1,0 +1,497 @@
+// Batched heightfield pipeline: many eroded-chunk requests (each a 3x3
+// free-slip neighbourhood, chunks of uneven side, own filter radius, droplet
+// count and brush) generated, filtered and eroded by one fixed sequence of
+// batched kernel launches -- every launch covers every chunk of every
+// request (grid.y = job) -- captured once into a CUDA graph and replayed.
+//
+// Device layout per request (side S, all buffers resident, one allocation):
+//   biome region   (5S)^2 uint16   the 3x3 diversity neighbourhoods of all
+//                                   nine chunks overlap inside a 5x5 region
+//   merged height  (3S)^2 float    noise writes each chunk straight into its
+//                                   place, erosion runs on it in place
+//   fixed height   (3S)^2 uint16   formatted output
+//   per chunk      filter workspace, offsets (S^2+1), bins
+//   starts, brush, residual sediment
+// No merge/unmerge copies are needed: a chunk's filter input is a window of
+// the biome region and its heightmap a window of the merged map.
+#include "erosion.cuh"
+#include "noise.cuh"
+#include "shf.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+namespace stpgb {
+int starts_launch(float* xy, uint32_t count, uint64_t seed, uint64_t base, uint32_t map_x, uint32_t map_y,
+	uint32_t nn_x, uint32_t nn_y, cudaStream_t stream);
+int voronoi_launch(uint16_t* out, uint32_t pitch, uint32_t width, uint32_t height, int64_t ox, int64_t oy,
+	uint32_t cell, uint32_t biomes, uint64_t seed, cudaStream_t stream);
+} // namespace stpgb
+
+using namespace stpgb;
+
+namespace {
+
+size_t al(size_t v) {
+	return (v + 255u) & ~static_cast<size_t>(255u);
+}
+
+struct RequestLayout {
+	size_t biome, height, fixed, starts, brush_idx, brush_w;
+	size_t shf_ws[9], offsets[9], bins[9];
+	uint64_t bins_cap;
+	size_t end;
+};
+
+} // namespace
+
+struct stpgb_batch {
+	std::vector<stpgb_batch_request> req;
+	stpgb_raindrop_setting base {};
+	uint32_t biome_count = 0u, max_items = 0u;
+	unsigned char* mem = nullptr;
+	size_t bytes = 0u;
+	std::vector<RequestLayout> layout;
+	// device tables
+	uint8_t* perm = nullptr;
+	float* grad = nullptr;
+	stpgb_permutation permutation {};
+	stpgb_biome_property* table = nullptr;
+	double* residual = nullptr;
+	uint32_t* status = nullptr;
+	unsigned long long* counters = nullptr; // realised droplet steps, brush-erosion steps
+	// job arrays (device) and launch bounds
+	ShfJob* shf_jobs = nullptr;
+	NoiseJob* noise_jobs = nullptr;
+	ErosionJob* ero_jobs = nullptr;
+	FormatJob* fmt_jobs = nullptr;
+	std::vector<ShfJob> shf_h;
+	std::vector<NoiseJob> noise_h;
+	std::vector<ErosionJob> ero_h;
+	std::vector<FormatJob> fmt_h;
+	uint32_t max_S = 0u, max_r = 0u, max_count = 0u, max_brush = 0u, kcap_v = 0u, kcap_h = 0u;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+
+	~stpgb_batch() {
+		if (exec) {
+			cudaGraphExecDestroy(exec);
+		}
+		if (graph) {
+			cudaGraphDestroy(graph);
+		}
+		for (void* p : { static_cast<void*>(mem), static_cast<void*>(perm), static_cast<void*>(grad),
+				 static_cast<void*>(table), static_cast<void*>(residual), static_cast<void*>(status),
+				 static_cast<void*>(counters),
+				 static_cast<void*>(shf_jobs), static_cast<void*>(noise_jobs), static_cast<void*>(ero_jobs),
+				 static_cast<void*>(fmt_jobs) }) {
+			if (p) {
+				cudaFree(p);
+			}
+		}
+	}
+
+	// the whole pipeline as a fixed launch sequence
+	int enqueue(cudaStream_t s) {
+		STPGB_CUDA_TRY(cudaMemsetAsync(residual, 0, sizeof(double) * req.size(), s));
+		STPGB_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t), s));
+		for (uint32_t st = 0u; st < 4u; st++) {
+			STPGB_TRY(stage(st, s));
+		}
+		return STPGB_OK;
+	}
+
+	// stage 0: filter, 1: noise, 2: erosion, 3: format
+	int stage(uint32_t st, cudaStream_t s) {
+		const uint32_t nchunks = static_cast<uint32_t>(shf_h.size());
+		switch (st) {
+		case 0u:
+			return shf_launch(shf_jobs, shf_h[0], nchunks, max_S, max_S, max_r, kcap_v, kcap_h, s);
+		case 1u:
+			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
+				table, biome_count, s);
+		case 2u:
+			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s);
+		case 3u:
+			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
+		default:
+			return inval("stpgb_batch_run_stage: stage must be 0..3");
+		}
+	}
+
+	// the same work as the per-chunk drop-in call sequence: one chunk's filter
+	// + noise per call, then one erosion + format per request, the stream
+	// synchronised after every call as the reference's generate()/erode() do
+	int enqueue_plain(cudaStream_t s) {
+		for (size_t n = 0; n < req.size(); n++) {
+			for (uint32_t c = 0u; c < 9u; c++) {
+				const ShfJob& j = shf_h[9u * n + c];
+				STPGB_CUDA_TRY(cudaMemsetAsync(j.status, 0, sizeof(uint32_t), s));
+				STPGB_TRY(shf_launch(nullptr, j, 1u, j.W, j.H, j.r, kcap_v, kcap_h, s));
+				const NoiseJob& nj = noise_h[9u * n + c];
+				STPGB_TRY(noise_launch(nullptr, nj, 1u, static_cast<uint64_t>(nj.W) * nj.H, permutation, table, biome_count, s));
+				STPGB_CUDA_TRY(cudaStreamSynchronize(s));
+			}
+			const ErosionJob& e = ero_h[n];
+			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s));
+			const FormatJob& f = fmt_h[n];
+			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
+			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
+		}
+		return STPGB_OK;
+	}
+};
+
+namespace {
+
+int check_request(const stpgb_batch_request& r) {
+	if (r.MapSize == 0u || (r.MapSize & 7u) != 0u) {
+		return inval("stpgb_batch: MapSize must be a positive multiple of 8");
+	}
+	if (r.InterpolationRadius == 0u || (r.InterpolationRadius & 1u) || r.InterpolationRadius > r.MapSize) {
+		return inval("stpgb_batch: radius must be positive, even and at most MapSize");
+	}
+	if (r.BrushRadius == 0u || 2u * r.BrushRadius + 2u >= 3u * r.MapSize) {
+		return inval("stpgb_batch: brush radius must be positive and fit the merged map");
+	}
+	return STPGB_OK;
+}
+
+template<typename T>
+int upload(T*& dst, const std::vector<T>& src) {
+	STPGB_CUDA_TRY(cudaMalloc(&dst, std::max<size_t>(src.size(), 1u) * sizeof(T)));
+	STPGB_CUDA_TRY(cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+	return STPGB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, const stpgb_raindrop_setting* base,
+	const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table, uint32_t biome_count,
+	uint64_t hbm_budget, uint32_t flags, stpgb_batch** out) {
+	if (!requests || count == 0u || !base || !simplex || !biome_table || biome_count == 0u || !out) {
+		return inval("stpgb_batch_create: null argument or empty batch");
+	}
+	STPGB_TRY(stpgb_simplex_setting_validate(simplex));
+	STPGB_TRY(stpgb_raindrop_setting_validate(base));
+	auto b = std::make_unique<stpgb_batch>();
+	b->req.assign(requests, requests + count);
+	b->base = *base;
+	b->biome_count = biome_count;
+	b->max_items = std::min<uint32_t>(biome_count, kShfMaxItems);
+	for (const auto& r : b->req) {
+		STPGB_TRY(check_request(r));
+		b->max_S = std::max(b->max_S, r.MapSize);
+		b->max_r = std::max(b->max_r, r.InterpolationRadius);
+		b->max_count = std::max(b->max_count, r.DropletCount);
+	}
+	b->kcap_v = shf_kcap_v(b->max_r, b->max_items);
+	b->kcap_h = shf_kcap_h(b->max_r, b->max_items);
+
+	// layout
+	size_t off = 0u;
+	std::vector<std::vector<int32_t>> brush_i(count);
+	std::vector<std::vector<float>> brush_w(count);
+	for (uint32_t n = 0u; n < count; n++) {
+		const auto& r = b->req[n];
+		const size_t S = r.MapSize;
+		RequestLayout L {};
+		L.biome = off;
+		off += al(25u * S * S * sizeof(uint16_t));
+		L.height = off;
+		off += al(9u * S * S * sizeof(float));
+		L.fixed = off;
+		off += al(9u * S * S * sizeof(uint16_t));
+		L.starts = off;
+		off += al(2u * static_cast<size_t>(r.DropletCount) * sizeof(float));
+		uint32_t bs = 0u;
+		stpgb_erosion_brush_generate(3u * r.MapSize, r.BrushRadius, nullptr, nullptr, 0u, &bs);
+		brush_i[n].resize(bs);
+		brush_w[n].resize(bs);
+		STPGB_TRY(stpgb_erosion_brush_generate(3u * r.MapSize, r.BrushRadius, brush_i[n].data(), brush_w[n].data(), bs, &bs));
+		b->max_brush = std::max(b->max_brush, bs);
+		L.brush_idx = off;
+		off += al(bs * sizeof(int32_t));
+		L.brush_w = off;
+		off += al(bs * sizeof(float));
+		const ShfLayout sl = shf_layout(r.MapSize, r.MapSize, r.InterpolationRadius, b->kcap_v);
+		L.bins_cap = S * S * std::min<uint64_t>(shf_kcap_h(r.InterpolationRadius, b->max_items),
+			(2ull * r.InterpolationRadius + 1u) * (2ull * r.InterpolationRadius + 1u));
+		for (int c = 0; c < 9; c++) {
+			L.shf_ws[c] = off;
+			off += al(sl.total);
+			L.offsets[c] = off;
+			off += al((S * S + 1u) * sizeof(uint32_t));
+			L.bins[c] = off;
+			off += al(L.bins_cap * sizeof(stpgb_bin));
+		}
+		L.end = off;
+		b->layout.push_back(L);
+	}
+	b->bytes = off;
+	if (hbm_budget != 0u && off > hbm_budget) {
+		set_error("stpgb_batch_create: the batch needs " + std::to_string(off) + " bytes, above the HBM budget");
+		return STPGB_ENOMEM;
+	}
+	{
+		const cudaError_t e = cudaMalloc(&b->mem, off);
+		if (e != cudaSuccess) {
+			cudaGetLastError();
+			set_error("stpgb_batch_create: device allocation of " + std::to_string(off) + " bytes failed");
+			return STPGB_ENOMEM;
+		}
+	}
+
+	// tables
+	std::vector<uint8_t> perm(512);
+	std::vector<float> grad(2u * simplex->Distribution);
+	STPGB_TRY(stpgb_permutation_generate(simplex, perm.data(), grad.data(), static_cast<uint32_t>(grad.size())));
+	STPGB_TRY(upload(b->perm, perm));
+	STPGB_TRY(upload(b->grad, grad));
+	b->permutation = stpgb_permutation { b->perm, b->grad, simplex->Distribution };
+	STPGB_TRY(upload(b->table, std::vector<stpgb_biome_property>(biome_table, biome_table + biome_count)));
+	STPGB_CUDA_TRY(cudaMalloc(&b->residual, sizeof(double) * count));
+	STPGB_CUDA_TRY(cudaMalloc(&b->status, sizeof(uint32_t)));
+	STPGB_CUDA_TRY(cudaMalloc(&b->counters, 2u * sizeof(unsigned long long)));
+	STPGB_CUDA_TRY(cudaMemset(b->counters, 0, 2u * sizeof(unsigned long long)));
+
+	// jobs
+	for (uint32_t n = 0u; n < count; n++) {
+		const auto& r = b->req[n];
+		const RequestLayout& L = b->layout[n];
+		const uint32_t S = r.MapSize;
+		unsigned char* const m = b->mem;
+		STPGB_CUDA_TRY(cudaMemcpy(m + L.brush_idx, brush_i[n].data(), brush_i[n].size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+		STPGB_CUDA_TRY(cudaMemcpy(m + L.brush_w, brush_w[n].data(), brush_w[n].size() * sizeof(float), cudaMemcpyHostToDevice));
+		uint16_t* const biome = reinterpret_cast<uint16_t*>(m + L.biome);
+		float* const height = reinterpret_cast<float*>(m + L.height);
+		for (uint32_t c = 0u; c < 9u; c++) {
+			const uint32_t cx = c % 3u, cy = c / 3u;
+			const ShfLayout sl = shf_layout(S, S, r.InterpolationRadius, b->kcap_v);
+			ShfJob j {};
+			j.samplemap = biome + static_cast<size_t>(cy) * S * (5u * S) + static_cast<size_t>(cx) * S;
+			j.pitch = 5u * S;
+			j.W = S;
+			j.H = S;
+			j.sx = S;
+			j.sy = S;
+			j.r = r.InterpolationRadius;
+			j.kcap_v = b->kcap_v;
+			j.vbuf = reinterpret_cast<uint32_t*>(m + L.shf_ws[c] + sl.vbuf);
+			j.vn = reinterpret_cast<uint16_t*>(m + L.shf_ws[c] + sl.vn);
+			j.rows = reinterpret_cast<uint32_t*>(m + L.shf_ws[c] + sl.rows);
+			j.offsets = reinterpret_cast<uint32_t*>(m + L.offsets[c]);
+			j.bins = reinterpret_cast<stpgb_bin*>(m + L.bins[c]);
+			j.bins_capacity = L.bins_cap;
+			j.status = b->status;
+			b->shf_h.push_back(j);
+			NoiseJob nj {};
+			nj.out = height + static_cast<size_t>(cy) * S * (3u * S) + static_cast<size_t>(cx) * S;
+			nj.pitch = 3u * S;
+			nj.offsets = j.offsets;
+			nj.bins = j.bins;
+			nj.W = S;
+			nj.H = S;
+			// chunk map offset of neighbour (cx-1, cy-1) around the request's centre chunk
+			// (STPChunk::calcChunkMapOffset: chunk unit * MapSize)
+			nj.off_x = static_cast<float>((static_cast<int64_t>(r.ChunkX) + cx - 1) * S);
+			nj.off_y = static_cast<float>((static_cast<int64_t>(r.ChunkY) + cy - 1) * S);
+			b->noise_h.push_back(nj);
+		}
+		stpgb_raindrop_setting rs = b->base;
+		rs.RainDropCount = r.DropletCount;
+		rs.ErosionBrushRadius = r.BrushRadius;
+		if (r.Lifetime != 0u) {
+			rs.minWaterVolume = stpgb_lifetime_min_water_volume(rs.initWaterVolume, rs.EvaporateSpeed, r.Lifetime);
+		}
+		ErosionJob e {};
+		e.map = height;
+		e.dim_x = 3u * S;
+		e.dim_y = 3u * S;
+		e.pitch = 3u * S;
+		e.starts = reinterpret_cast<float*>(m + L.starts);
+		e.count = r.DropletCount;
+		e.brush_index = reinterpret_cast<int32_t*>(m + L.brush_idx);
+		e.brush_weight = reinterpret_cast<float*>(m + L.brush_w);
+		e.brush_size = static_cast<uint32_t>(brush_i[n].size());
+		e.p = rain_params(rs);
+		e.residual = b->residual + n;
+		e.status = b->status;
+		e.counters = b->counters;
+		e.fixed = reinterpret_cast<uint16_t*>(m + L.fixed);
+		b->ero_h.push_back(e);
+		b->fmt_h.push_back(FormatJob { height, 3ull * S, e.fixed, 3ull * S, 3u * S, 3u * S });
+	}
+	STPGB_TRY(upload(b->shf_jobs, b->shf_h));
+	STPGB_TRY(upload(b->noise_jobs, b->noise_h));
+	STPGB_TRY(upload(b->ero_jobs, b->ero_h));
+	STPGB_TRY(upload(b->fmt_jobs, b->fmt_h));
+
+	if (flags & STPGB_BATCH_GRAPH) {
+		cudaStream_t cs;
+		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+		STPGB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+		const int rc = b->enqueue(cs);
+		cudaGraph_t g = nullptr;
+		const cudaError_t ce = cudaStreamEndCapture(cs, &g);
+		cudaStreamDestroy(cs);
+		STPGB_TRY(rc);
+		STPGB_CUDA_TRY(ce);
+		b->graph = g;
+		STPGB_CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
+	}
+	*out = b.release();
+	return STPGB_OK;
+}
+
+int stpgb_batch_destroy(stpgb_batch* b) {
+	delete b;
+	return STPGB_OK;
+}
+
+uint64_t stpgb_batch_device_bytes(const stpgb_batch* b) {
+	return b ? b->bytes : 0u;
+}
+
+int stpgb_batch_buffers(stpgb_batch* b, uint32_t request, uint16_t** biome_region, float** heightmap,
+	uint16_t** heightmap_fixed, float** starts_xy) {
+	if (!b || request >= b->req.size()) {
+		return inval("stpgb_batch_buffers: request out of range");
+	}
+	const RequestLayout& L = b->layout[request];
+	if (biome_region) {
+		*biome_region = reinterpret_cast<uint16_t*>(b->mem + L.biome);
+	}
+	if (heightmap) {
+		*heightmap = reinterpret_cast<float*>(b->mem + L.height);
+	}
+	if (heightmap_fixed) {
+		*heightmap_fixed = reinterpret_cast<uint16_t*>(b->mem + L.fixed);
+	}
+	if (starts_xy) {
+		*starts_xy = reinterpret_cast<float*>(b->mem + L.starts);
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_synthesize_inputs(stpgb_batch* b, uint32_t voronoi_cell, uint64_t seed, void* stream) {
+	if (!b || voronoi_cell == 0u) {
+		return inval("stpgb_batch_synthesize_inputs: invalid argument");
+	}
+	const cudaStream_t s = as_stream(stream);
+	for (size_t n = 0; n < b->req.size(); n++) {
+		const auto& r = b->req[n];
+		const RequestLayout& L = b->layout[n];
+		const uint32_t S = r.MapSize;
+		STPGB_TRY(voronoi_launch(reinterpret_cast<uint16_t*>(b->mem + L.biome), 5u * S, 5u * S, 5u * S,
+			(static_cast<int64_t>(r.ChunkX) - 2) * S, (static_cast<int64_t>(r.ChunkY) - 2) * S, voronoi_cell,
+			b->biome_count, seed, s));
+		// droplet counter space: the request's centre chunk coordinate keeps starts distinct per chunk
+		const uint64_t base = (static_cast<uint64_t>(static_cast<uint32_t>(r.ChunkX)) << 40)
+			^ (static_cast<uint64_t>(static_cast<uint32_t>(r.ChunkY)) << 20);
+		STPGB_TRY(starts_launch(reinterpret_cast<float*>(b->mem + L.starts), r.DropletCount, b->base.Seed, base, S, S,
+			3u, 3u, s));
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_run(stpgb_batch* b, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_run: null batch");
+	}
+	const cudaStream_t s = as_stream(stream);
+	if (b->exec) {
+		STPGB_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+		return STPGB_OK;
+	}
+	return b->enqueue(s);
+}
+
+int stpgb_batch_run_plain(stpgb_batch* b, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_run_plain: null batch");
+	}
+	return b->enqueue_plain(as_stream(stream));
+}
+
+int stpgb_batch_upload(stpgb_batch* b, const uint16_t* const* biome_regions, const float* const* starts_xy,
+	void* stream) {
+	if (!b || !biome_regions) {
+		return inval("stpgb_batch_upload: null argument");
+	}
+	const cudaStream_t s = as_stream(stream);
+	for (size_t n = 0; n < b->req.size(); n++) {
+		const size_t S = b->req[n].MapSize;
+		STPGB_CUDA_TRY(cudaMemcpyAsync(b->mem + b->layout[n].biome, biome_regions[n], 25u * S * S * sizeof(uint16_t),
+			cudaMemcpyHostToDevice, s));
+		if (starts_xy && starts_xy[n]) {
+			STPGB_CUDA_TRY(cudaMemcpyAsync(b->mem + b->layout[n].starts, starts_xy[n],
+				2u * sizeof(float) * b->req[n].DropletCount, cudaMemcpyHostToDevice, s));
+		}
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_download(stpgb_batch* b, float* const* heightmaps, uint16_t* const* heightmaps_fixed,
+	double* residual_sediment, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_download: null batch");
+	}
+	const cudaStream_t s = as_stream(stream);
+	for (size_t n = 0; n < b->req.size(); n++) {
+		const size_t S = b->req[n].MapSize;
+		if (heightmaps && heightmaps[n]) {
+			STPGB_CUDA_TRY(cudaMemcpyAsync(heightmaps[n], b->mem + b->layout[n].height, 9u * S * S * sizeof(float),
+				cudaMemcpyDeviceToHost, s));
+		}
+		if (heightmaps_fixed && heightmaps_fixed[n]) {
+			STPGB_CUDA_TRY(cudaMemcpyAsync(heightmaps_fixed[n], b->mem + b->layout[n].fixed,
+				9u * S * S * sizeof(uint16_t), cudaMemcpyDeviceToHost, s));
+		}
+	}
+	if (residual_sediment) {
+		STPGB_CUDA_TRY(cudaMemcpyAsync(residual_sediment, b->residual, sizeof(double) * b->req.size(),
+			cudaMemcpyDeviceToHost, s));
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_run_stage(stpgb_batch* b, uint32_t stage, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_run_stage: null batch");
+	}
+	return b->stage(stage, as_stream(stream));
+}
+
+int stpgb_batch_counters(stpgb_batch* b, uint64_t* realised_steps, uint64_t* erode_steps, int reset) {
+	if (!b) {
+		return inval("stpgb_batch_counters: null batch");
+	}
+	unsigned long long h[2] = { 0u, 0u };
+	STPGB_CUDA_TRY(cudaDeviceSynchronize());
+	STPGB_CUDA_TRY(cudaMemcpy(h, b->counters, sizeof(h), cudaMemcpyDeviceToHost));
+	if (realised_steps) {
+		*realised_steps = h[0];
+	}
+	if (erode_steps) {
+		*erode_steps = h[1];
+	}
+	if (reset) {
+		STPGB_CUDA_TRY(cudaMemset(b->counters, 0, sizeof(h)));
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_status(stpgb_batch* b, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_status: null batch");
+	}
+	return stpgb_status_check(b->status, stream);
+}
+
+} // extern "C"

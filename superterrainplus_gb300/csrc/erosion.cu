@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 	const uint32_t d = blockIdx.x * kErodeBlock + threadIdx.x;
 	double residual = 0.0;
 	bool capped = false;
+	uint32_t steps_done = 0u, erode_steps = 0u;
 	if (d < J.count) {
 		float* const map = J.map;
 		const uint64_t pitch = J.pitch;
@@ -105,6 +106,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 				atomicAdd(map + mi + pitch, dep * (1.0f - ox) * oy);
 				atomicAdd(map + mi + pitch + 1, dep * ox * oy);
 			} else {
+				erode_steps++;
 				const float ero = fminf((cap - sed) * P.ErodeSpeed, -dh);
 				for (uint32_t b = 0u; b < J.brush_size; b++) {
 					float* const cell = map + static_cast<int64_t>(mi) + bidx[b];
@@ -118,8 +120,20 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 			speed = sqrtf(fmaxf(0.0f, speed * speed + dh * P.Gravity));
 			speed *= 1.0f - P.Friction;
 			vol *= 1.0f - P.EvaporateSpeed;
+			steps_done++;
 		}
 		residual = static_cast<double>(sed);
+	}
+	if (J.counters) {
+		unsigned long long s = steps_done, e = erode_steps;
+		for (int o = 16; o > 0; o >>= 1) {
+			s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+			e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		}
+		if ((threadIdx.x & 31u) == 0u) {
+			atomicAdd(J.counters, s);
+			atomicAdd(J.counters + 1, e);
+		}
 	}
 	if (J.residual) {
 		for (int o = 16; o > 0; o >>= 1) {
@@ -139,10 +153,9 @@ __device__ __forceinline__ uint32_t fmt1(const float h) {
 	return static_cast<uint32_t>(rintf(__saturatef(h) * 65535.0f));
 }
 
-__global__ void format_kernel(const float* __restrict__ in, const uint64_t in_pitch, uint16_t* __restrict__ out,
-	const uint64_t out_pitch, const uint32_t W, const uint32_t H) {
+__device__ __forceinline__ void format_group(const float* __restrict__ in, const uint64_t in_pitch,
+	uint16_t* __restrict__ out, const uint64_t out_pitch, const uint32_t W, const uint32_t H, const uint64_t t) {
 	const uint32_t groups = (W + 7u) / 8u;
-	const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (t >= static_cast<uint64_t>(groups) * H) {
 		return;
 	}
@@ -165,6 +178,17 @@ __global__ void format_kernel(const float* __restrict__ in, const uint64_t in_pi
 			out[y * out_pitch + x] = static_cast<uint16_t>(fmt1(in[y * in_pitch + x]));
 		}
 	}
+}
+
+__global__ void format_kernel(const float* __restrict__ in, const uint64_t in_pitch, uint16_t* __restrict__ out,
+	const uint64_t out_pitch, const uint32_t W, const uint32_t H) {
+	format_group(in, in_pitch, out, out_pitch, W, H, static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+}
+
+__global__ void format_batch_kernel(const FormatJob* __restrict__ jobs) {
+	const FormatJob& J = jobs[blockIdx.y];
+	format_group(J.in, J.in_pitch, J.out, J.out_pitch, J.W, J.H,
+		static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
 } // namespace
@@ -223,6 +247,16 @@ int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t ou
 	return STPGB_OK;
 }
 
+int format_batch_launch(const FormatJob* jobs, uint32_t njobs, uint32_t max_W, uint32_t max_H, cudaStream_t stream) {
+	const uint64_t threads = static_cast<uint64_t>((max_W + 7u) / 8u) * max_H;
+	if (threads == 0u || njobs == 0u) {
+		return STPGB_OK;
+	}
+	format_batch_kernel<<<dim3(static_cast<uint32_t>((threads + 255u) / 256u), njobs), 256u, 0, stream>>>(jobs);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
 } // namespace stpgb
 
 using namespace stpgb;
@@ -257,6 +291,7 @@ int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stp
 	job.residual = residual_sediment;
 	job.status = status;
 	job.fixed = nullptr;
+	job.counters = nullptr;
 	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream));
 }
 

@@ -27,6 +27,8 @@ struct ErosionJob {
 	double* residual;
 	uint32_t* status;
 	uint16_t* fixed; // formatted output (optional, batched path)
+	// optional counters: [0] realised steps, [1] steps that eroded over the brush
+	unsigned long long* counters;
 };
 
 RainParams rain_params(const stpgb_raindrop_setting& s);
@@ -36,5 +38,16 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
 	cudaStream_t stream);
+
+// Formatting of many maps in one launch.
+struct FormatJob {
+	const float* in;
+	uint64_t in_pitch;
+	uint16_t* out;
+	uint64_t out_pitch;
+	uint32_t W, H;
+};
+
+int format_batch_launch(const FormatJob* jobs, uint32_t njobs, uint32_t max_W, uint32_t max_H, cudaStream_t stream);
 
 } // namespace stpgb

@@ -38,13 +38,17 @@ __device__ __forceinline__ float corner(const float dx, const float dy, const fl
 	return w * w * (g.x * dx + g.y * dy);
 }
 
-// STPSimplexNoise.cu:18-82
+// STPSimplexNoise.cu:18-82.  The skew and unskew (x + (x+y)*F2 and
+// i - (i+j)*G2) are written with separately rounded operations: fused into
+// one multiply-add they shift the cell origin by up to an ulp of the sample
+// coordinate, which at world offsets of 10^4-10^5 pixels is a visible error.
 __device__ __forceinline__ float simplex2d(const uint8_t* __restrict__ perm, const float2* __restrict__ gtab,
 	const float x, const float y) {
-	const float s = (x + y) * kF2;
-	const int i = floori(x + s), j = floori(y + s);
-	const float t = static_cast<float>(i + j) * kG2;
-	const float dx0 = x - (static_cast<float>(i) - t), dy0 = y - (static_cast<float>(j) - t);
+	const float s = __fmul_rn(__fadd_rn(x, y), kF2);
+	const int i = floori(__fadd_rn(x, s)), j = floori(__fadd_rn(y, s));
+	const float t = __fmul_rn(static_cast<float>(i + j), kG2);
+	const float dx0 = __fsub_rn(x, __fsub_rn(static_cast<float>(i), t));
+	const float dy0 = __fsub_rn(y, __fsub_rn(static_cast<float>(j), t));
 	const unsigned int i1 = (dx0 > dy0) ? 1u : 0u, j1 = 1u - i1;
 	const float dx1 = dx0 - static_cast<float>(i1) + kG2, dy1 = dy0 - static_cast<float>(j1) + kG2;
 	const float dx2 = dx0 + kH2, dy2 = dy0 + kH2;

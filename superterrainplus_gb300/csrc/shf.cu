@@ -265,13 +265,16 @@ bool g_attr_set = false;
 
 } // namespace
 
+// The reference adds the incoming row / column before it removes the
+// outgoing one, so an accumulator briefly holds the window plus one row
+// (vertical: 2r+2 samples) or one column (horizontal: (2r+2)(2r+1)).
 uint32_t shf_kcap_v(uint32_t r, uint32_t max_items) {
-	return std::min<uint32_t>(2u * r + 1u, max_items);
+	return std::min<uint32_t>(2u * r + 2u, max_items);
 }
 
 uint32_t shf_kcap_h(uint32_t r, uint32_t max_items) {
 	const uint64_t side = 2ull * r + 1ull;
-	return static_cast<uint32_t>(std::min<uint64_t>(side * side, max_items));
+	return static_cast<uint32_t>(std::min<uint64_t>((side + 1u) * side, max_items));
 }
 
 ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {

@@ -38,12 +38,12 @@ __global__ void starts_kernel(float* __restrict__ xy, const uint32_t count, cons
 	const uint64_t ctr = base + i;
 	uint32_t c[4] = { static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32), 0u, 0u };
 	philox4x32_10(c, static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-	float x = static_cast<float>((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
-	float y = static_cast<float>((c[1] >> 8) + 1u) * (1.0f / 16777216.0f);
-	x *= base_x;
-	y *= base_y;
-	x += range_x;
-	y += range_y;
+	const float ux = static_cast<float>((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
+	const float uy = static_cast<float>((c[1] >> 8) + 1u) * (1.0f / 16777216.0f);
+	// separately rounded multiply then add, as the reference's
+	// `initPos *= base; initPos += range;` (no fused multiply-add)
+	const float x = __fadd_rn(__fmul_rn(ux, base_x), range_x);
+	const float y = __fadd_rn(__fmul_rn(uy, base_y), range_y);
 	reinterpret_cast<float2*>(xy)[i] = make_float2(x, y);
 }
 
