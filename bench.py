@@ -228,6 +228,9 @@ def run_ours(args):
     sh = stream.cuda_stream
     batch.synthesize(VORONOI_CELL, SEED, sh)
     stream.synchronize()
+    # the autotuner times the erosion kernel on these inputs, then the graph is re-captured
+    batch.tune()
+    lanes, tune_ms = batch.tuning()
 
     def barrier():
         torch.cuda.synchronize()
@@ -356,6 +359,7 @@ def run_ours(args):
             "stage_ms": dict(zip(stage_names, stage_ms)),
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
+            "autotune": {"erosion_lanes_per_droplet": lanes, "erosion_ms_by_lanes": tune_ms},
             "gpu_launches": 7 * args.steps,
         }
         print(json.dumps(line), flush=True)

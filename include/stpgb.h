@@ -302,7 +302,10 @@ typedef struct stpgb_batch_request {
 	uint32_t Lifetime;            /* droplet steps; 0 keeps the base minWaterVolume */
 } stpgb_batch_request;
 
-enum { STPGB_BATCH_GRAPH = 1 };
+enum {
+	STPGB_BATCH_GRAPH = 1,   /* capture the launch sequence into a CUDA graph */
+	STPGB_BATCH_AUTOTUNE = 2 /* time the erosion kernel's lanes-per-droplet on the batch, keep the fastest */
+};
 
 /* Lays out and allocates every buffer of the batch on the current device in
  * one allocation (STPGB_ENOMEM if it exceeds `hbm_budget` bytes; 0 = no
@@ -344,12 +347,24 @@ STPGB_API int stpgb_batch_upload(stpgb_batch* batch, const uint16_t* const* biom
 STPGB_API int stpgb_batch_download(stpgb_batch* batch, float* const* heightmaps,
 	uint16_t* const* heightmaps_fixed, double* residual_sediment, void* stream);
 
+/* Device -> HOST copies of the current inputs (biome regions, starts). */
+STPGB_API int stpgb_batch_download_inputs(stpgb_batch* batch, uint16_t* const* biome_regions,
+	float* const* starts_xy, void* stream);
+
 /* Synchronises `stream` and decodes the batch's device status word. */
 STPGB_API int stpgb_batch_status(stpgb_batch* batch, void* stream);
 
 /* One stage of the batch on its own (0 filter, 1 noise, 2 erosion,
  * 3 format), for per-kernel timing. Asynchronous. */
 STPGB_API int stpgb_batch_run_stage(stpgb_batch* batch, uint32_t stage, void* stream);
+
+/* Runs the autotuner now, on the batch's current inputs (synchronous), and
+ * re-captures the graph of a batch created with STPGB_BATCH_GRAPH. */
+STPGB_API int stpgb_batch_tune(stpgb_batch* batch);
+
+/* Erosion lanes per droplet in use, and the autotuner's erosion time in ms
+ * for 1, 2, 4, 8, 16 and 32 lanes (6 floats; 0 where not tried). */
+STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_droplet, float* erosion_ms);
 
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */

@@ -25,7 +25,7 @@ __all__ = [
     "STPCapacityError", "STPCUDAError", "STPException", "STPInsufficientMemory", "STPInvalidEnvironment",
     "STPNumericDomainError", "STPTimeout", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
-    "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps",
+    "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch",
 ]
 
 BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
@@ -170,14 +170,17 @@ class Batch:
     DropletCount, BrushRadius, Lifetime.  `stream` arguments are raw
     cudaStream_t values (int) or None for the legacy default stream."""
 
-    def __init__(self, requests, base_setting, simplex_setting, biome_table, hbm_budget=0, graph=True):
-        from ._capi import STPGB_BATCH_GRAPH, BatchRequest
+    def __init__(self, requests, base_setting, simplex_setting, biome_table, hbm_budget=0, graph=True,
+                 autotune=False):
+        from ._capi import STPGB_BATCH_AUTOTUNE, STPGB_BATCH_GRAPH, BatchRequest
         reqs = list(requests)
         arr = (BatchRequest * len(reqs))(*[BatchRequest(**r) for r in reqs])
         table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
         h = C.c_void_p()
         rc = lib().stpgb_batch_create(arr, len(reqs), C.byref(base_setting), C.byref(simplex_setting), _p(table),
-                                      len(table), hbm_budget, STPGB_BATCH_GRAPH if graph else 0, C.byref(h))
+                                      len(table), hbm_budget,
+                                      (STPGB_BATCH_GRAPH if graph else 0) | (STPGB_BATCH_AUTOTUNE if autotune else 0),
+                                      C.byref(h))
         check(rc)
         self._h = h
         self.requests = reqs
@@ -226,8 +229,25 @@ class Batch:
         rp = residual.ctypes.data_as(C.c_void_p) if residual is not None else None
         check(lib().stpgb_batch_download(self._h, hp, fp, rp, self._s(stream)))
 
+    def download_inputs(self, biome_regions=None, starts=None, stream=None):
+        n = len(self.requests)
+        bp = (C.c_void_p * n)(*[a.ctypes.data for a in biome_regions]) if biome_regions is not None else None
+        sp = (C.c_void_p * n)(*[a.ctypes.data for a in starts]) if starts is not None else None
+        check(lib().stpgb_batch_download_inputs(self._h, bp, sp, self._s(stream)))
+
     def status(self, stream=None):
         check(lib().stpgb_batch_status(self._h, self._s(stream)))
+
+    def tune(self):
+        """Autotune on the current inputs (synchronous) and re-capture the graph."""
+        check(lib().stpgb_batch_tune(self._h))
+
+    def tuning(self):
+        """(lanes per droplet in use, {lanes: autotuner erosion ms})."""
+        lanes = C.c_uint32(0)
+        ms = (C.c_float * 6)()
+        check(lib().stpgb_batch_tuning(self._h, C.byref(lanes), ms))
+        return lanes.value, {1 << i: ms[i] for i in range(6) if ms[i] > 0}
 
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)

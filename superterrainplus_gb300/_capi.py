@@ -96,6 +96,7 @@ class BatchRequest(C.Structure):
 
 
 STPGB_BATCH_GRAPH = 1
+STPGB_BATCH_AUTOTUNE = 2
 
 # name -> (restype, argtypes); the single source of the binding
 PROTOTYPES = {
@@ -135,6 +136,9 @@ PROTOTYPES = {
     "stpgb_batch_download": (C.c_int, [vp, vp, vp, vp, vp]),
     "stpgb_batch_status": (C.c_int, [vp, vp]),
     "stpgb_batch_run_stage": (C.c_int, [vp, u32, vp]),
+    "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), vp]),
+    "stpgb_batch_tune": (C.c_int, [vp]),
+    "stpgb_batch_download_inputs": (C.c_int, [vp, vp, vp, vp]),
     "stpgb_batch_counters": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64), C.c_int]),
 }
 

@@ -72,8 +72,40 @@ struct stpgb_batch {
 	std::vector<ErosionJob> ero_h;
 	std::vector<FormatJob> fmt_h;
 	uint32_t max_S = 0u, max_r = 0u, max_count = 0u, max_brush = 0u, kcap_v = 0u, kcap_h = 0u;
+	uint32_t lanes = 8u; // lanes per droplet of the erosion kernel
+	float tune_ms[6] = { 0, 0, 0, 0, 0, 0 }; // erosion time per candidate 1..32 lanes (0 = not tried)
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
+	bool use_graph = false;
+
+	// (re)captures the launch sequence into a graph
+	int capture() {
+		if (exec) {
+			cudaGraphExecDestroy(exec);
+			exec = nullptr;
+		}
+		if (graph) {
+			cudaGraphDestroy(graph);
+			graph = nullptr;
+		}
+		cudaStream_t cs;
+		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+		STPGB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+		const int rc = enqueue(cs);
+		cudaGraph_t g = nullptr;
+		const cudaError_t ce = cudaStreamEndCapture(cs, &g);
+		cudaStreamDestroy(cs);
+		if (rc != STPGB_OK) {
+			if (g) {
+				cudaGraphDestroy(g);
+			}
+			return rc;
+		}
+		STPGB_CUDA_TRY(ce);
+		graph = g;
+		STPGB_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+		return STPGB_OK;
+	}
 
 	~stpgb_batch() {
 		if (exec) {
@@ -113,12 +145,55 @@ struct stpgb_batch {
 			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
 				table, biome_count, s);
 		case 2u:
-			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s);
+			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes);
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
 			return inval("stpgb_batch_run_stage: stage must be 0..3");
 		}
+	}
+
+	// Autotuner: times the erosion stage of this batch with every candidate
+	// lane count (noise regenerates the heights before each trial, so every
+	// trial erodes the same map) and keeps the fastest.
+	int autotune() {
+		cudaStream_t s;
+		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+		cudaEvent_t e0, e1;
+		STPGB_CUDA_TRY(cudaEventCreate(&e0));
+		STPGB_CUDA_TRY(cudaEventCreate(&e1));
+		int rc = stage(0u, s);
+		float best = 0.0f;
+		uint32_t best_lanes = lanes;
+		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
+		for (int c = 0; c < 6 && rc == STPGB_OK; c++) {
+			lanes = cands[c];
+			float t = 0.0f;
+			for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
+				rc = stage(1u, s);
+				if (rc == STPGB_OK) {
+					cudaEventRecord(e0, s);
+					rc = stage(2u, s);
+					cudaEventRecord(e1, s);
+				}
+				if (cudaStreamSynchronize(s) != cudaSuccess) {
+					rc = cuda_fail(cudaGetLastError(), "autotune");
+				}
+				float ms = 0.0f;
+				cudaEventElapsedTime(&ms, e0, e1);
+				t = rep == 0 ? ms : std::min(t, ms);
+			}
+			tune_ms[c] = t;
+			if (rc == STPGB_OK && (best == 0.0f || t < best)) {
+				best = t;
+				best_lanes = cands[c];
+			}
+		}
+		lanes = best_lanes;
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		cudaStreamDestroy(s);
+		return rc;
 	}
 
 	// the same work as the per-chunk drop-in call sequence: one chunk's filter
@@ -136,7 +211,7 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -332,21 +407,24 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 	STPGB_TRY(upload(b->ero_jobs, b->ero_h));
 	STPGB_TRY(upload(b->fmt_jobs, b->fmt_h));
 
-	if (flags & STPGB_BATCH_GRAPH) {
-		cudaStream_t cs;
-		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-		STPGB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-		const int rc = b->enqueue(cs);
-		cudaGraph_t g = nullptr;
-		const cudaError_t ce = cudaStreamEndCapture(cs, &g);
-		cudaStreamDestroy(cs);
-		STPGB_TRY(rc);
-		STPGB_CUDA_TRY(ce);
-		b->graph = g;
-		STPGB_CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
+	if (flags & STPGB_BATCH_AUTOTUNE) {
+		STPGB_TRY(b->autotune());
+	}
+	b->use_graph = (flags & STPGB_BATCH_GRAPH) != 0u;
+	if (b->use_graph) {
+		STPGB_TRY(b->capture());
 	}
 	*out = b.release();
 	return STPGB_OK;
+}
+
+int stpgb_batch_tune(stpgb_batch* b) {
+	if (!b) {
+		return inval("stpgb_batch_tune: null batch");
+	}
+	STPGB_CUDA_TRY(cudaDeviceSynchronize());
+	STPGB_TRY(b->autotune());
+	return b->use_graph ? b->capture() : STPGB_OK;
 }
 
 int stpgb_batch_destroy(stpgb_batch* b) {
@@ -461,6 +539,21 @@ int stpgb_batch_download(stpgb_batch* b, float* const* heightmaps, uint16_t* con
 	return STPGB_OK;
 }
 
+int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, float* erosion_ms) {
+	if (!b) {
+		return inval("stpgb_batch_tuning: null batch");
+	}
+	if (lanes_per_droplet) {
+		*lanes_per_droplet = b->lanes;
+	}
+	if (erosion_ms) {
+		for (int c = 0; c < 6; c++) {
+			erosion_ms[c] = b->tune_ms[c];
+		}
+	}
+	return STPGB_OK;
+}
+
 int stpgb_batch_run_stage(stpgb_batch* b, uint32_t stage, void* stream) {
 	if (!b) {
 		return inval("stpgb_batch_run_stage: null batch");
@@ -483,6 +576,26 @@ int stpgb_batch_counters(stpgb_batch* b, uint64_t* realised_steps, uint64_t* ero
 	}
 	if (reset) {
 		STPGB_CUDA_TRY(cudaMemset(b->counters, 0, sizeof(h)));
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_download_inputs(stpgb_batch* b, uint16_t* const* biome_regions, float* const* starts_xy,
+	void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_download_inputs: null batch");
+	}
+	const cudaStream_t s = as_stream(stream);
+	for (size_t n = 0; n < b->req.size(); n++) {
+		const size_t S = b->req[n].MapSize;
+		if (biome_regions && biome_regions[n]) {
+			STPGB_CUDA_TRY(cudaMemcpyAsync(biome_regions[n], b->mem + b->layout[n].biome, 25u * S * S * sizeof(uint16_t),
+				cudaMemcpyDeviceToHost, s));
+		}
+		if (starts_xy && starts_xy[n]) {
+			STPGB_CUDA_TRY(cudaMemcpyAsync(starts_xy[n], b->mem + b->layout[n].starts,
+				2u * sizeof(float) * b->req[n].DropletCount, cudaMemcpyDeviceToHost, s));
+		}
 	}
 	return STPGB_OK;
 }

@@ -23,6 +23,8 @@ namespace stpgb {
 namespace {
 
 constexpr uint32_t kErodeBlock = 128u;
+// lanes per droplet of the per-call entry point; batches choose their own
+constexpr uint32_t kDefaultLanes = 8u;
 
 struct HG {
 	float h, gx, gy;
@@ -43,6 +45,19 @@ __device__ __forceinline__ HG height_gradient(const float* __restrict__ map, con
 	return r;
 }
 
+// Brush points a lane loads before it issues its atomics.
+constexpr uint32_t kBrushBatch = 8u;
+
+// G lanes (1, 2, 4, 8, 16 or 32) carry one droplet.  Every lane of a group
+// holds the same droplet state and takes the same branches (same inputs,
+// same instructions, the corner loads are one broadcast transaction); the
+// brush points of an erosion step and the four deposit corners are split
+// across the lanes, so one droplet's scattered updates leave the warp as a
+// few coalesced requests instead of one request per point.  Each lane first
+// loads all of its points, then issues the atomics, so the loads of a step
+// overlap instead of following one another.  The eroded amounts are summed
+// over the group with a butterfly, which gives every lane the same total.
+template<uint32_t G>
 __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single) {
 	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
@@ -56,13 +71,17 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 	__syncthreads();
 
 	const RainParams& P = J.p;
-	const uint32_t d = blockIdx.x * kErodeBlock + threadIdx.x;
+	const uint32_t g = threadIdx.x % G;
+	const uint32_t d = (blockIdx.x * kErodeBlock + threadIdx.x) / G;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gmask = G == 32u ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1u)));
 	double residual = 0.0;
 	bool capped = false;
 	uint32_t steps_done = 0u, erode_steps = 0u;
 	if (d < J.count) {
 		float* const map = J.map;
 		const uint64_t pitch = J.pitch;
+		const uint32_t bsize = J.brush_size;
 		float px = J.starts[2u * d], py = J.starts[2u * d + 1u];
 		float dirx = 0.0f, diry = 0.0f;
 		float speed = P.initSpeed, vol = P.initWaterVolume, sed = 0.0f;
@@ -101,21 +120,39 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 			if (sed > cap || dh > 0.0f) {
 				const float dep = (dh > 0.0f) ? fminf(dh, sed) : (sed - cap) * P.DepositSpeed;
 				sed -= dep;
-				atomicAdd(map + mi, dep * (1.0f - ox) * (1.0f - oy));
-				atomicAdd(map + mi + 1, dep * ox * (1.0f - oy));
-				atomicAdd(map + mi + pitch, dep * (1.0f - ox) * oy);
-				atomicAdd(map + mi + pitch + 1, dep * ox * oy);
+				for (uint32_t c = g; c < 4u; c += G) {
+					const float wx = (c & 1u) ? ox : 1.0f - ox, wy = (c & 2u) ? oy : 1.0f - oy;
+					atomicAdd(map + mi + ((c & 2u) ? pitch : 0u) + (c & 1u), dep * wx * wy);
+				}
 			} else {
 				erode_steps++;
 				const float ero = fminf((cap - sed) * P.ErodeSpeed, -dh);
-				for (uint32_t b = 0u; b < J.brush_size; b++) {
-					float* const cell = map + static_cast<int64_t>(mi) + bidx[b];
-					const float we = ero * bw[b];
-					const float cur = __ldcg(cell);
-					const float ds = (cur < we) ? cur : we;
-					atomicAdd(cell, -ds);
-					sed += ds;
+				float part = 0.0f;
+				for (uint32_t base = g; base < bsize; base += G * kBrushBatch) {
+					float cur[kBrushBatch], we[kBrushBatch];
+#pragma unroll
+					for (uint32_t k = 0u; k < kBrushBatch; k++) {
+						const uint32_t p = base + k * G;
+						if (p < bsize) {
+							we[k] = ero * bw[p];
+							cur[k] = __ldcg(map + static_cast<int64_t>(mi) + bidx[p]);
+						}
+					}
+#pragma unroll
+					for (uint32_t k = 0u; k < kBrushBatch; k++) {
+						const uint32_t p = base + k * G;
+						if (p < bsize) {
+							const float ds = (cur[k] < we[k]) ? cur[k] : we[k];
+							atomicAdd(map + static_cast<int64_t>(mi) + bidx[p], -ds);
+							part += ds;
+						}
+					}
 				}
+#pragma unroll
+				for (uint32_t o = G / 2u; o > 0u; o >>= 1) {
+					part += __shfl_xor_sync(gmask, part, o);
+				}
+				sed += part;
 			}
 			speed = sqrtf(fmaxf(0.0f, speed * speed + dh * P.Gravity));
 			speed *= 1.0f - P.Friction;
@@ -124,13 +161,20 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 		}
 		residual = static_cast<double>(sed);
 	}
+	if (g != 0u) {
+		// one lane per droplet reports
+		residual = 0.0;
+		steps_done = 0u;
+		erode_steps = 0u;
+		capped = false;
+	}
 	if (J.counters) {
 		unsigned long long s = steps_done, e = erode_steps;
 		for (int o = 16; o > 0; o >>= 1) {
 			s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
 			e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
 		}
-		if ((threadIdx.x & 31u) == 0u) {
+		if (lane == 0u) {
 			atomicAdd(J.counters, s);
 			atomicAdd(J.counters + 1, e);
 		}
@@ -139,7 +183,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 		for (int o = 16; o > 0; o >>= 1) {
 			residual += __shfl_xor_sync(0xFFFFFFFFu, residual, o);
 		}
-		if ((threadIdx.x & 31u) == 0u && residual != 0.0) {
+		if (lane == 0u && residual != 0.0) {
 			atomicAdd(J.residual, residual);
 		}
 	}
@@ -221,19 +265,40 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 }
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream) {
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
 	const size_t smem = static_cast<size_t>(max_brush) * (sizeof(int32_t) + sizeof(float));
-	if (smem > 48u * 1024u) {
-		STPGB_CUDA_TRY(cudaFuncSetAttribute(erosion_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			static_cast<int>(smem)));
+	const uint64_t threads = static_cast<uint64_t>(max_count) * lanes_per_droplet;
+	if (threads > 0xFFFFFFFFull - kErodeBlock) {
+		return inval("erosion: too many droplets for one launch");
 	}
-	const dim3 grid((max_count + kErodeBlock - 1u) / kErodeBlock, njobs);
-	erosion_kernel<<<grid, kErodeBlock, smem, stream>>>(jobs, single);
-	STPGB_CUDA_TRY(cudaGetLastError());
-	return STPGB_OK;
+	const dim3 grid(static_cast<uint32_t>((threads + kErodeBlock - 1u) / kErodeBlock), njobs);
+	auto go = [&](auto kernel) -> int {
+		if (smem > 48u * 1024u) {
+			STPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+		}
+		kernel<<<grid, kErodeBlock, smem, stream>>>(jobs, single);
+		STPGB_CUDA_TRY(cudaGetLastError());
+		return STPGB_OK;
+	};
+	switch (lanes_per_droplet) {
+	case 1u:
+		return go(erosion_kernel<1u>);
+	case 2u:
+		return go(erosion_kernel<2u>);
+	case 4u:
+		return go(erosion_kernel<4u>);
+	case 8u:
+		return go(erosion_kernel<8u>);
+	case 16u:
+		return go(erosion_kernel<16u>);
+	case 32u:
+		return go(erosion_kernel<32u>);
+	default:
+		return inval("erosion: lanes per droplet must be 1, 2, 4, 8, 16 or 32");
+	}
 }
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
@@ -292,7 +357,7 @@ int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stp
 	job.status = status;
 	job.fixed = nullptr;
 	job.counters = nullptr;
-	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream));
+	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), kDefaultLanes);
 }
 
 int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x, uint32_t map_y, void* stream) {

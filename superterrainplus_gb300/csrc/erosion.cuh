@@ -33,8 +33,9 @@ struct ErosionJob {
 
 RainParams rain_params(const stpgb_raindrop_setting& s);
 
+// lanes_per_droplet: 1, 2, 4, 8, 16 or 32 lanes carry one droplet
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream);
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet);
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
 	cudaStream_t stream);

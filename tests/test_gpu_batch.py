@@ -1,0 +1,103 @@
+"""The batched pipeline (uneven requests in one launch sequence / CUDA graph)
+against the oracle: filter + noise stage within 2e-6 of the oracle heights,
+synthesized inputs bit-exact, per-request mass balance within 1e-5, the
+formatted output bit-exact, and the tuner's choice still correct."""
+import numpy as np
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+REQS = [
+    dict(MapSize=64, ChunkX=0, ChunkY=0, InterpolationRadius=16, DropletCount=9000, BrushRadius=3, Lifetime=30),
+    dict(MapSize=96, ChunkX=7, ChunkY=-2, InterpolationRadius=8, DropletCount=20000, BrushRadius=5, Lifetime=64),
+    dict(MapSize=32, ChunkX=-5, ChunkY=11, InterpolationRadius=20, DropletCount=2300, BrushRadius=2, Lifetime=40),
+    dict(MapSize=128, ChunkX=3, ChunkY=3, InterpolationRadius=32, DropletCount=37000, BrushRadius=4, Lifetime=50),
+]
+NB = 6
+CELL = 40
+
+
+def make_batch(stpgb, graph=True):
+    base = stpgb.RaindropSetting(**helpers.raindrop_dict(1000, radius=3, lifetime=30, seed=5))
+    simplex = stpgb.SimplexSetting(5, 8, 0.2181661565)
+    table = helpers.biome_table(NB, 5)
+    b = stpgb.Batch(REQS, base, simplex, table, graph=graph)
+    b.synthesize(CELL, 17)
+    return b, table
+
+
+def heights(b):
+    out = [np.zeros((3 * r["MapSize"], 3 * r["MapSize"]), np.float32) for r in REQS]
+    fixed = [np.zeros((3 * r["MapSize"], 3 * r["MapSize"]), np.uint16) for r in REQS]
+    res = np.zeros(len(REQS), np.float64)
+    b.download(out, fixed, res)
+    b.status()
+    return out, fixed, res
+
+
+def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle):
+    b, table = make_batch(stpgb)
+    regions = [np.zeros((5 * r["MapSize"], 5 * r["MapSize"]), np.uint16) for r in REQS]
+    starts = [np.zeros(2 * r["DropletCount"], np.float32) for r in REQS]
+    b.download_inputs(regions, starts)
+    b.run_stage(0)
+    b.run_stage(1)
+    h, _, _ = heights(b)
+    perm, grad = stpgb.permutation_generate(5, 8, 0.2181661565)
+    for n, r in enumerate(REQS):
+        S = r["MapSize"]
+        ref_region = oracle.voronoi(5 * S, 5 * S, ((r["ChunkX"] - 2) * S, (r["ChunkY"] - 2) * S), CELL, NB, 17)
+        assert np.array_equal(regions[n], ref_region)
+        x, y = starts[n][0::2], starts[n][1::2]
+        assert x.min() > S and x.max() <= 2 * S - 1 and y.min() > S and y.max() <= 2 * S - 1
+        for c in range(9):
+            cx, cy = c % 3, c // 3
+            sub = np.ascontiguousarray(ref_region[cy * S:cy * S + 3 * S, cx * S:cx * S + 3 * S])
+            rc, off, bins = oracle.shf(sub, (S, S), (3, 3), r["InterpolationRadius"])
+            assert rc == 0
+            off_xy = (float((r["ChunkX"] + cx - 1) * S), float((r["ChunkY"] + cy - 1) * S))
+            ref = oracle.multibiome(off, bins, table, perm, grad, (S, S), off_xy)
+            got = h[n][cy * S:(cy + 1) * S, cx * S:(cx + 1) * S]
+            assert np.abs(got - ref).max() <= 2e-6, (n, c)
+
+
+@pytest.mark.parametrize("tune", [False, True])
+def test_batch_erosion_mass_balance_and_format(stpgb, dev, oracle, tune):
+    b, _ = make_batch(stpgb)
+    if tune:
+        b.tune()
+        lanes, ms = b.tuning()
+        assert lanes in (1, 2, 4, 8, 16, 32) and len(ms) == 6
+    b.run_stage(0)
+    b.run_stage(1)
+    before, _, _ = heights(b)
+    b.run()
+    after, fixed, res = heights(b)
+    for n in range(len(REQS)):
+        t0 = before[n].astype(np.float64).sum()
+        bal = (t0 - after[n].astype(np.float64).sum()) - res[n]
+        assert abs(bal) <= 1e-5 * t0, (n, bal)
+        assert not np.array_equal(before[n], after[n])
+        assert np.array_equal(fixed[n], oracle.format(after[n]))
+
+
+def test_batch_plain_sequence_same_noise(stpgb, dev):
+    """The plain per-chunk sequence and the graph produce the same heights before erosion."""
+    b, _ = make_batch(stpgb)
+    b.run_stage(0)
+    b.run_stage(1)
+    ref, _, _ = heights(b)
+    b.run_plain()
+    plain, _, res = heights(b)
+    for n in range(len(REQS)):
+        t0 = ref[n].astype(np.float64).sum()
+        assert abs((t0 - plain[n].astype(np.float64).sum()) - res[n]) <= 1e-5 * t0
+
+
+def test_batch_budget_refusal(stpgb):
+    base = stpgb.RaindropSetting(**helpers.raindrop_dict(1000))
+    simplex = stpgb.SimplexSetting(5, 8, 0.2181661565)
+    with pytest.raises(stpgb.STPInsufficientMemory):
+        stpgb.Batch(REQS, base, simplex, helpers.biome_table(NB, 5), hbm_budget=1 << 20)
