@@ -242,11 +242,13 @@ def run_ours(args):
     barrier()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clocks:
+        torch.cuda.nvtx.range_push("timed_region")
         evs[0].record(stream)
         for k in range(args.steps):
             batch.run(sh)
             evs[k + 1].record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     batch.status(sh)
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1000.0

@@ -1,6 +1,6 @@
 // Free-slip particle hydraulic erosion and height formatting on sm_103a.
 //
-// One thread per droplet, following STPRainDrop::operator()
+// A group of 1-32 lanes per droplet, following STPRainDrop::operator()
 // (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPRainDrop.cu:53-165) step for
 // step: bilinear height/gradient at the current cell (:23-51), inertia
 // steering, unit move, death within BrushRadius of the merged-map border,
@@ -30,13 +30,36 @@ struct HG {
 	float h, gx, gy;
 };
 
+// The four corner heights of a cell, identical in every lane of the group:
+// the map changes under concurrent droplets, so the lanes must not read it
+// separately.  With G >= 4 lane c of the group reads corner c, with G == 2
+// each lane reads one row, and the values are broadcast over the group.
+template<uint32_t G>
+__device__ __forceinline__ float4 cell_corners(const float* __restrict__ base, const uint64_t pitch, const uint32_t g,
+	const uint32_t gmask, const uint32_t glead) {
+	if constexpr (G == 1u) {
+		return make_float4(__ldcg(base), __ldcg(base + 1), __ldcg(base + pitch), __ldcg(base + pitch + 1));
+	} else if constexpr (G == 2u) {
+		const float* const row = base + (g ? pitch : 0u);
+		const float a = __ldcg(row), b = __ldcg(row + 1);
+		return make_float4(__shfl_sync(gmask, a, glead), __shfl_sync(gmask, b, glead), __shfl_sync(gmask, a, glead + 1),
+			__shfl_sync(gmask, b, glead + 1));
+	} else {
+		const uint32_t c = g & 3u;
+		const float v = __ldcg(base + ((c & 2u) ? pitch : 0u) + (c & 1u));
+		return make_float4(__shfl_sync(gmask, v, glead), __shfl_sync(gmask, v, glead + 1),
+			__shfl_sync(gmask, v, glead + 2), __shfl_sync(gmask, v, glead + 3));
+	}
+}
+
 // STPRainDrop.cu:23-51
+template<uint32_t G>
 __device__ __forceinline__ HG height_gradient(const float* __restrict__ map, const uint64_t pitch, const float px,
-	const float py) {
+	const float py, const uint32_t g, const uint32_t gmask, const uint32_t glead) {
 	const uint32_t rx = static_cast<uint32_t>(px), ry = static_cast<uint32_t>(py);
 	const float cx = px - static_cast<float>(rx), cy = py - static_cast<float>(ry);
-	const float* const base = map + static_cast<uint64_t>(ry) * pitch + rx;
-	const float h00 = __ldcg(base), h10 = __ldcg(base + 1), h01 = __ldcg(base + pitch), h11 = __ldcg(base + pitch + 1);
+	const float4 q = cell_corners<G>(map + static_cast<uint64_t>(ry) * pitch + rx, pitch, g, gmask, glead);
+	const float h00 = q.x, h10 = q.y, h01 = q.z, h11 = q.w;
 	HG r;
 	r.h = h00 * (1.0f - cx) * (1.0f - cy) + h10 * cx * (1.0f - cy) + h01 * (1.0f - cx) * cy + h11 * cx * cy;
 	// glm::mix(a, b, t) = a * (1 - t) + b * t
@@ -75,6 +98,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 	const uint32_t d = (blockIdx.x * kErodeBlock + threadIdx.x) / G;
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t gmask = G == 32u ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1u)));
+	const uint32_t glead = lane & ~(G - 1u);
 	double residual = 0.0;
 	bool capped = false;
 	uint32_t steps_done = 0u, erode_steps = 0u;
@@ -100,7 +124,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 			}
 			const uint64_t mi = static_cast<uint64_t>(static_cast<uint32_t>(py)) * pitch + static_cast<uint32_t>(px);
 			const float ox = px - static_cast<float>(static_cast<int>(px)), oy = py - static_cast<float>(static_cast<int>(py));
-			const HG hg = height_gradient(map, pitch, px, py);
+			const HG hg = height_gradient<G>(map, pitch, px, py, g, gmask, glead);
 			dirx = (-hg.gx) * (1.0f - P.Inertia) + dirx * P.Inertia;
 			diry = (-hg.gy) * (1.0f - P.Inertia) + diry * P.Inertia;
 			const float len = sqrtf(dirx * dirx + diry * diry);
@@ -115,7 +139,7 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 				vol = 0.0f;
 				break; // the carried sediment leaves with the droplet
 			}
-			const float dh = height_gradient(map, pitch, px, py).h - hg.h;
+			const float dh = height_gradient<G>(map, pitch, px, py, g, gmask, glead).h - hg.h;
 			const float cap = fmaxf(-dh * speed * vol * P.SedimentCapacityFactor, P.minSedimentCapacity);
 			if (sed > cap || dh > 0.0f) {
 				const float dep = (dh > 0.0f) ? fminf(dh, sed) : (sed - cap) * P.DepositSpeed;
@@ -158,6 +182,9 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 			speed *= 1.0f - P.Friction;
 			vol *= 1.0f - P.EvaporateSpeed;
 			steps_done++;
+			// the group leaves every step together (the deposit loop above runs
+			// on some of its lanes only)
+			__syncwarp(gmask);
 		}
 		residual = static_cast<double>(sed);
 	}
