@@ -231,6 +231,23 @@ STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
 	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,
 	double* residual_sediment, uint32_t* status, void* stream);
 
+/* stpgb_hydraulic_erosion with an explicit number of lanes carrying one
+ * droplet (1, 2, 4, 8, 16 or 32) and flags.  Each lane erodes its share of
+ * the brush in the reference's order (STPRainDrop.cu:146-157): read a cell,
+ * subtract min(cell, w), next point; one lane per droplet is the reference
+ * kernel itself.  The plain entry point uses the largest power of two up to
+ * 8 that leaves each lane at least four brush points (below that, densely
+ * packed droplets read a step's cells nearly together and the map can run
+ * away).  STPGB_EROSION_EXACT_CLAMP erodes each point by compare-and-swap
+ * instead, so racing droplets never remove more than a cell holds (closer to
+ * the serial algorithm, slower).  No counterpart in the reference. */
+enum { STPGB_EROSION_EXACT_CLAMP = 1 };
+STPGB_API int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn,
+	const stpgb_raindrop_setting* setting, const float* starts_xy, uint32_t count,
+	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,
+	double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet, uint32_t flags,
+	void* stream);
+
 /* Replaces STPHeightfieldKernel::formatHeightmap
  * (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPHeightfieldKernel.cu:51-57,112-122):
  * out[i] = uint16(rint(saturate(in[i]) * 65535)). Device buffers. */

@@ -306,14 +306,14 @@ class DeviceOps:
                                          self._stream()))
 
     def hydraulic_erosion(self, heightmap, map_size, nn, setting, starts, count, brush_index, brush_weight,
-                          residual=None, status=None):
+                          residual=None, status=None, lanes=0, exact_clamp=False):
         info = NNInfo.make(map_size, nn)
-        check(lib().stpgb_hydraulic_erosion(C.c_void_p(heightmap.data_ptr()), C.byref(info), C.byref(setting),
-                                            C.c_void_p(starts.data_ptr()), count, C.c_void_p(brush_index.data_ptr()),
-                                            C.c_void_p(brush_weight.data_ptr()), brush_index.numel(),
-                                            C.c_void_p(residual.data_ptr() if residual is not None else 0),
-                                            C.c_void_p(status.data_ptr() if status is not None else 0),
-                                            self._stream()), env_error=True)
+        check(lib().stpgb_hydraulic_erosion_ex(
+            C.c_void_p(heightmap.data_ptr()), C.byref(info), C.byref(setting), C.c_void_p(starts.data_ptr()), count,
+            C.c_void_p(brush_index.data_ptr()), C.c_void_p(brush_weight.data_ptr()), brush_index.numel(),
+            C.c_void_p(residual.data_ptr() if residual is not None else 0),
+            C.c_void_p(status.data_ptr() if status is not None else 0), lanes, int(exact_clamp),
+            self._stream()), env_error=True)
 
     def format_heightmap(self, src, dst, map_x, map_y):
         check(lib().stpgb_format_heightmap(C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()), map_x, map_y,

@@ -116,6 +116,8 @@ PROTOTYPES = {
     "stpgb_droplet_starts": (C.c_int, [vp, u32, u64, u64, C.POINTER(NNInfo), vp]),
     "stpgb_hydraulic_erosion": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp, u32,
                                           vp, vp, vp]),
+    "stpgb_hydraulic_erosion_ex": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp,
+                                             u32, vp, vp, u32, u32, vp]),
     "stpgb_format_heightmap": (C.c_int, [vp, vp, u32, u32, vp]),
     "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
     "stpgb_generator_create": (C.c_int, [C.POINTER(ChunkSetting), C.POINTER(RaindropSetting),

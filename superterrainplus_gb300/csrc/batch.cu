@@ -72,7 +72,8 @@ struct stpgb_batch {
 	std::vector<ErosionJob> ero_h;
 	std::vector<FormatJob> fmt_h;
 	uint32_t max_S = 0u, max_r = 0u, max_count = 0u, max_brush = 0u, kcap_v = 0u, kcap_h = 0u;
-	uint32_t lanes = 8u; // lanes per droplet of the erosion kernel
+	uint32_t lanes = 8u;       // lanes per droplet of the erosion kernel
+	uint32_t lane_limit = 32u; // max_lanes() of the smallest brush in the batch
 	float tune_ms[6] = { 0, 0, 0, 0, 0, 0 }; // erosion time per candidate 1..32 lanes (0 = not tried)
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
@@ -166,7 +167,7 @@ struct stpgb_batch {
 		float best = 0.0f;
 		uint32_t best_lanes = lanes;
 		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
-		for (int c = 0; c < 6 && rc == STPGB_OK; c++) {
+		for (int c = 0; c < 6 && rc == STPGB_OK && cands[c] <= lane_limit; c++) {
 			lanes = cands[c];
 			float t = 0.0f;
 			for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
@@ -290,6 +291,8 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		brush_w[n].resize(bs);
 		STPGB_TRY(stpgb_erosion_brush_generate(3u * r.MapSize, r.BrushRadius, brush_i[n].data(), brush_w[n].data(), bs, &bs));
 		b->max_brush = std::max(b->max_brush, bs);
+		b->lane_limit = std::min(b->lane_limit, max_lanes(bs));
+		b->lanes = std::min(8u, b->lane_limit);
 		L.brush_idx = off;
 		off += al(bs * sizeof(int32_t));
 		L.brush_w = off;

@@ -17,14 +17,13 @@
 #include "erosion.cuh"
 
 #include <cmath>
+#include <type_traits>
 
 namespace stpgb {
 
 namespace {
 
 constexpr uint32_t kErodeBlock = 128u;
-// lanes per droplet of the per-call entry point; batches choose their own
-constexpr uint32_t kDefaultLanes = 8u;
 
 struct HG {
 	float h, gx, gy;
@@ -68,19 +67,21 @@ __device__ __forceinline__ HG height_gradient(const float* __restrict__ map, con
 	return r;
 }
 
-// Brush points a lane loads before it issues its atomics.
+// Brush points a lane has in flight at once (compare-and-swap mode), and
+// the bound on failed swaps per batch before the plain subtraction.
 constexpr uint32_t kBrushBatch = 8u;
+constexpr uint32_t kCasRetries = 16u;
 
 // G lanes (1, 2, 4, 8, 16 or 32) carry one droplet.  Every lane of a group
-// holds the same droplet state and takes the same branches (same inputs,
-// same instructions, the corner loads are one broadcast transaction); the
-// brush points of an erosion step and the four deposit corners are split
-// across the lanes, so one droplet's scattered updates leave the warp as a
-// few coalesced requests instead of one request per point.  Each lane first
-// loads all of its points, then issues the atomics, so the loads of a step
-// overlap instead of following one another.  The eroded amounts are summed
-// over the group with a butterfly, which gives every lane the same total.
-template<uint32_t G>
+// holds the same droplet state and takes the same branches: the corner
+// heights are read once and broadcast, so no lane sees a different racy
+// value.  The brush points of an erosion step and the four deposit corners
+// are split across the lanes, so one droplet's scattered updates leave the
+// warp as a few coalesced requests instead of one request per point, and a
+// step costs ceil(points / G) read-update round trips instead of one per
+// point.  The eroded amounts are summed over the group with a butterfly,
+// which gives every lane the same total.
+template<uint32_t G, bool ExactClamp>
 __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single) {
 	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
@@ -152,23 +153,72 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 				erode_steps++;
 				const float ero = fminf((cap - sed) * P.ErodeSpeed, -dh);
 				float part = 0.0f;
-				for (uint32_t base = g; base < bsize; base += G * kBrushBatch) {
-					float cur[kBrushBatch], we[kBrushBatch];
-#pragma unroll
-					for (uint32_t k = 0u; k < kBrushBatch; k++) {
-						const uint32_t p = base + k * G;
-						if (p < bsize) {
-							we[k] = ero * bw[p];
-							cur[k] = __ldcg(map + static_cast<int64_t>(mi) + bidx[p]);
-						}
+				if constexpr (!ExactClamp) {
+					// The reference's order (STPRainDrop.cu:146-157): read the
+					// cell, subtract min(cell, w), then the next point; the next
+					// read stays behind the previous atomic.
+#pragma unroll 1
+					for (uint32_t p = g; p < bsize; p += G) {
+						float* const cell = map + static_cast<int64_t>(mi) + bidx[p];
+						const float we = ero * bw[p];
+						const float cur = __ldcg(cell);
+						const float ds = (cur < we) ? cur : we;
+						atomicAdd(cell, -ds);
+						part += ds;
+						asm volatile("" ::: "memory");
 					}
+				} else {
+					// The reference's min(cell, w) as one compare-and-swap per
+					// point: read all of the lane's cells, then replace each
+					// value v by v - clamp(v, 0, w) only if the cell still holds
+					// v, retrying with the value found otherwise.  All of a
+					// step's points are in flight at once, yet racing droplets
+					// can never remove more than a cell holds -- reading every
+					// cell first and subtracting later (or subtracting first and
+					// giving back) lets densely packed droplets all remove the
+					// same stale height, which drives the map unstable.  After
+					// kCasRetries failed swaps the lane falls back to the
+					// reference's unconditional subtraction of its last read.
+					for (uint32_t base = g; base < bsize; base += G * kBrushBatch) {
+						float cur[kBrushBatch], we[kBrushBatch];
+						bool done[kBrushBatch];
 #pragma unroll
-					for (uint32_t k = 0u; k < kBrushBatch; k++) {
-						const uint32_t p = base + k * G;
-						if (p < bsize) {
-							const float ds = (cur[k] < we[k]) ? cur[k] : we[k];
-							atomicAdd(map + static_cast<int64_t>(mi) + bidx[p], -ds);
-							part += ds;
+						for (uint32_t k = 0u; k < kBrushBatch; k++) {
+							const uint32_t p = base + k * G;
+							done[k] = p >= bsize;
+							if (!done[k]) {
+								we[k] = ero * bw[p];
+								cur[k] = __ldcg(map + static_cast<int64_t>(mi) + bidx[p]);
+							}
+						}
+						for (uint32_t attempt = 0u; attempt < kCasRetries; attempt++) {
+							bool pending = false;
+#pragma unroll
+							for (uint32_t k = 0u; k < kBrushBatch; k++) {
+								if (!done[k]) {
+									int* const cell = reinterpret_cast<int*>(map + static_cast<int64_t>(mi) + bidx[base + k * G]);
+									const float ds = fminf(fmaxf(cur[k], 0.0f), we[k]);
+									const int seen = atomicCAS(cell, __float_as_int(cur[k]), __float_as_int(cur[k] - ds));
+									if (seen == __float_as_int(cur[k])) {
+										part += ds;
+										done[k] = true;
+									} else {
+										cur[k] = __int_as_float(seen);
+										pending = true;
+									}
+								}
+							}
+							if (!pending) {
+								break;
+							}
+						}
+#pragma unroll
+						for (uint32_t k = 0u; k < kBrushBatch; k++) {
+							if (!done[k]) {
+								const float ds = fminf(fmaxf(cur[k], 0.0f), we[k]);
+								atomicAdd(map + static_cast<int64_t>(mi) + bidx[base + k * G], -ds);
+								part += ds;
+							}
 						}
 					}
 				}
@@ -264,6 +314,25 @@ __global__ void format_batch_kernel(const FormatJob* __restrict__ jobs) {
 
 } // namespace
 
+// Each lane of a group walks ceil(points / G) brush points one after another.
+// Below four points per lane the reads of a step happen nearly together again,
+// and on densely packed droplets (a 64^2 chunk with 9,000 droplets, brush 3)
+// the map then runs away, as it does when all reads precede the updates; at
+// four or more the grouped kernel stays within the one-lane kernel's
+// run-to-run spread.  max_lanes() is the largest power of two that keeps four
+// points per lane; the per-call entry point uses min(8, max_lanes()).
+uint32_t max_lanes(uint32_t brush_size) {
+	uint32_t g = 1u;
+	while (g < 32u && 2u * g * 4u <= brush_size) {
+		g *= 2u;
+	}
+	return g;
+}
+
+uint32_t default_lanes(uint32_t brush_size) {
+	return std::min(8u, max_lanes(brush_size));
+}
+
 RainParams rain_params(const stpgb_raindrop_setting& s) {
 	RainParams p;
 	p.Inertia = s.Inertia;
@@ -292,7 +361,7 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 }
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet) {
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
@@ -310,22 +379,26 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 		STPGB_CUDA_TRY(cudaGetLastError());
 		return STPGB_OK;
 	};
-	switch (lanes_per_droplet) {
-	case 1u:
-		return go(erosion_kernel<1u>);
-	case 2u:
-		return go(erosion_kernel<2u>);
-	case 4u:
-		return go(erosion_kernel<4u>);
-	case 8u:
-		return go(erosion_kernel<8u>);
-	case 16u:
-		return go(erosion_kernel<16u>);
-	case 32u:
-		return go(erosion_kernel<32u>);
-	default:
-		return inval("erosion: lanes per droplet must be 1, 2, 4, 8, 16 or 32");
-	}
+	auto pick = [&](auto ref_order) -> int {
+		constexpr bool R = decltype(ref_order)::value;
+		switch (lanes_per_droplet) {
+		case 1u:
+			return go(erosion_kernel<1u, R>);
+		case 2u:
+			return go(erosion_kernel<2u, R>);
+		case 4u:
+			return go(erosion_kernel<4u, R>);
+		case 8u:
+			return go(erosion_kernel<8u, R>);
+		case 16u:
+			return go(erosion_kernel<16u, R>);
+		case 32u:
+			return go(erosion_kernel<32u, R>);
+		default:
+			return inval("erosion: lanes per droplet must be 1, 2, 4, 8, 16 or 32");
+		}
+	};
+	return exact_clamp ? pick(std::true_type {}) : pick(std::false_type {});
 }
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
@@ -358,6 +431,14 @@ extern "C" {
 int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stpgb_raindrop_setting* setting,
 	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
 	uint32_t brush_size, double* residual_sediment, uint32_t* status, void* stream) {
+	return stpgb_hydraulic_erosion_ex(heightmap, nn, setting, starts_xy, count, brush_index, brush_weight,
+		brush_size, residual_sediment, status, default_lanes(brush_size), 0u, stream);
+}
+
+int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const stpgb_raindrop_setting* setting,
+	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
+	uint32_t brush_size, double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet, uint32_t flags,
+	void* stream) {
 	STPGB_TRY(stpgb_raindrop_setting_validate(setting));
 	if (!heightmap || !nn || (count > 0u && !starts_xy) || !brush_index || !brush_weight || brush_size == 0u) {
 		return inval("stpgb_hydraulic_erosion: null pointer or empty brush");
@@ -384,7 +465,9 @@ int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stp
 	job.status = status;
 	job.fixed = nullptr;
 	job.counters = nullptr;
-	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), kDefaultLanes);
+	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream),
+		lanes_per_droplet == 0u ? default_lanes(brush_size) : lanes_per_droplet,
+		(flags & STPGB_EROSION_EXACT_CLAMP) != 0u);
 }
 
 int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x, uint32_t map_y, void* stream) {

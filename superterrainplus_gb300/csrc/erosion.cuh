@@ -33,9 +33,16 @@ struct ErosionJob {
 
 RainParams rain_params(const stpgb_raindrop_setting& s);
 
-// lanes_per_droplet: 1, 2, 4, 8, 16 or 32 lanes carry one droplet
+// lanes_per_droplet: 1, 2, 4, 8, 16 or 32 lanes carry one droplet;
+// exact_clamp: brush updates by compare-and-swap (never more than a cell
+// holds) instead of the reference's read-then-subtract order
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet);
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false);
+
+// Largest lanes-per-droplet that keeps at least four brush points per lane,
+// and the per-call default, min(8, max_lanes).
+uint32_t max_lanes(uint32_t brush_size);
+uint32_t default_lanes(uint32_t brush_size);
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
 	cudaStream_t stream);
