@@ -69,7 +69,8 @@ def test_batch_erosion_mass_balance_and_format(stpgb, dev, oracle, tune):
     if tune:
         b.tune()
         lanes, ms = b.tuning()
-        assert lanes in (1, 2, 4, 8, 16, 32) and len(ms) == 6
+        # the smallest brush (radius 2, 9 points) allows at most 2 lanes per droplet
+        assert set(ms) == {1, 2} and lanes in ms
     b.run_stage(0)
     b.run_stage(1)
     before, _, _ = heights(b)
