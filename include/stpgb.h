@@ -177,6 +177,20 @@ STPGB_API int stpgb_shf_filter(const uint16_t* samplemap, const stpgb_nn_info* n
 	uint32_t* offsets, stpgb_bin* bins, uint64_t bins_capacity, uint32_t* status,
 	void* stream);
 
+/* No counterpart in the reference.  stpgb_shf_filter for callers that may not
+ * allocate device memory (a frame loop where cudaFree would stall on the whole
+ * device, an engine whose own allocator owns every byte of its budget): the
+ * filter's scratch comes from a fixed 16 MiB array inside the library, held
+ * by every GPU that loads it until the process exits, instead of a caller
+ * workspace.  Inputs and outputs are the caller's, as in stpgb_shf_filter.
+ * Returns STPGB_ECAPACITY if stpgb_shf_workspace_size exceeds 16 MiB.  The
+ * first call on a device looks up the array's address; make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Allocates nothing. */
+STPGB_API int stpgb_shf_filter_noalloc(const uint16_t* samplemap, const stpgb_nn_info* nn,
+	uint32_t radius, uint32_t max_items, uint32_t* offsets, stpgb_bin* bins,
+	uint64_t bins_capacity, uint32_t* status, void* stream);
+
 /* Synchronous convenience: runs the filter into library-owned device memory
  * and copies offsets (W*H+1) and bins to HOST memory.  `*nbins` receives the
  * bin count; if `bins_capacity` is too small nothing is copied to `bins`
