@@ -361,7 +361,8 @@ def run_ours(args):
             "stage_ms": dict(zip(stage_names, stage_ms)),
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
-            "autotune": {"erosion_lanes_per_droplet": lanes, "erosion_ms_by_lanes": tune_ms},
+            "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
+                         "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}": v for (a, b), v in tune_ms.items()}},
             "gpu_launches": 7 * args.steps,
         }
         print(json.dumps(line), flush=True)

@@ -246,7 +246,9 @@ STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
 	double* residual_sediment, uint32_t* status, void* stream);
 
 /* stpgb_hydraulic_erosion with an explicit number of lanes carrying one
- * droplet (1, 2, 4, 8, 16 or 32) and flags.  Each lane erodes its share of
+ * droplet (1, 2, 4, 8, 16 or 32; 0 = default), droplets per lane group (1, or
+ * 2 / 4 with 4, 8 or 16 lanes: the group advances its droplets together so
+ * their memory round trips overlap) and flags.  Each lane erodes its share of
  * the brush in the reference's order (STPRainDrop.cu:146-157): read a cell,
  * subtract min(cell, w), next point; one lane per droplet is the reference
  * kernel itself.  The plain entry point uses the largest power of two up to
@@ -259,8 +261,8 @@ enum { STPGB_EROSION_EXACT_CLAMP = 1 };
 STPGB_API int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn,
 	const stpgb_raindrop_setting* setting, const float* starts_xy, uint32_t count,
 	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,
-	double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet, uint32_t flags,
-	void* stream);
+	double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet,
+	uint32_t droplets_per_group, uint32_t flags, void* stream);
 
 /* Replaces STPHeightfieldKernel::formatHeightmap
  * (SuperTerrain+/SuperTerrain+/Private/GPGPU/STPHeightfieldKernel.cu:51-57,112-122):
@@ -393,9 +395,11 @@ STPGB_API int stpgb_batch_run_stage(stpgb_batch* batch, uint32_t stage, void* st
  * re-captures the graph of a batch created with STPGB_BATCH_GRAPH. */
 STPGB_API int stpgb_batch_tune(stpgb_batch* batch);
 
-/* Erosion lanes per droplet in use, and the autotuner's erosion time in ms
- * for 1, 2, 4, 8, 16 and 32 lanes (6 floats; 0 where not tried). */
-STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_droplet, float* erosion_ms);
+/* Erosion lanes per droplet and droplets per lane group in use, and the
+ * autotuner's erosion time in ms per candidate: 18 floats, index
+ * 3*log2(lanes) + {0, 1, 2} for 1, 2, 4 droplets per group (0 = not tried). */
+STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_droplet,
+	uint32_t* droplets_per_group, float* erosion_ms);
 
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */

@@ -118,7 +118,7 @@ PROTOTYPES = {
     "stpgb_hydraulic_erosion": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp, u32,
                                           vp, vp, vp]),
     "stpgb_hydraulic_erosion_ex": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp,
-                                             u32, vp, vp, u32, u32, vp]),
+                                             u32, vp, vp, u32, u32, u32, vp]),
     "stpgb_format_heightmap": (C.c_int, [vp, vp, u32, u32, vp]),
     "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
     "stpgb_generator_create": (C.c_int, [C.POINTER(ChunkSetting), C.POINTER(RaindropSetting),
@@ -139,7 +139,7 @@ PROTOTYPES = {
     "stpgb_batch_download": (C.c_int, [vp, vp, vp, vp, vp]),
     "stpgb_batch_status": (C.c_int, [vp, vp]),
     "stpgb_batch_run_stage": (C.c_int, [vp, u32, vp]),
-    "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), vp]),
+    "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), vp]),
     "stpgb_batch_tune": (C.c_int, [vp]),
     "stpgb_batch_download_inputs": (C.c_int, [vp, vp, vp, vp]),
     "stpgb_batch_counters": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64), C.c_int]),

@@ -74,7 +74,9 @@ struct stpgb_batch {
 	uint32_t max_S = 0u, max_r = 0u, max_count = 0u, max_brush = 0u, kcap_v = 0u, kcap_h = 0u;
 	uint32_t lanes = 8u;       // lanes per droplet of the erosion kernel
 	uint32_t lane_limit = 32u; // max_lanes() of the smallest brush in the batch
-	float tune_ms[6] = { 0, 0, 0, 0, 0, 0 }; // erosion time per candidate 1..32 lanes (0 = not tried)
+	uint32_t dpg = 1u;         // droplets per lane group
+	// autotuner's erosion time per candidate, [lanes 1..32][droplets 1, 2, 4] (0 = not tried)
+	float tune_ms[18] = {};
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	bool use_graph = false;
@@ -146,7 +148,8 @@ struct stpgb_batch {
 			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
 				table, biome_count, s);
 		case 2u:
-			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes);
+			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
+				false, dpg);
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -165,10 +168,18 @@ struct stpgb_batch {
 		STPGB_CUDA_TRY(cudaEventCreate(&e1));
 		int rc = stage(0u, s);
 		float best = 0.0f;
-		uint32_t best_lanes = lanes;
+		uint32_t best_lanes = lanes, best_dpg = dpg;
 		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
-		for (int c = 0; c < 6 && rc == STPGB_OK && cands[c] <= lane_limit; c++) {
-			lanes = cands[c];
+		const uint32_t dcands[3] = { 1u, 2u, 4u };
+		for (int c = 0; c < 18 && rc == STPGB_OK; c++) {
+			const uint32_t cl = cands[c / 3], cd = dcands[c % 3];
+			// lane counts above the brush limit, and several droplets per group
+			// below four lanes or above sixteen, are not candidates
+			if (cl > lane_limit || (cd > 1u && (cl < 4u || cl > 16u))) {
+				continue;
+			}
+			lanes = cl;
+			dpg = cd;
 			float t = 0.0f;
 			for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
 				rc = stage(1u, s);
@@ -187,10 +198,12 @@ struct stpgb_batch {
 			tune_ms[c] = t;
 			if (rc == STPGB_OK && (best == 0.0f || t < best)) {
 				best = t;
-				best_lanes = cands[c];
+				best_lanes = cl;
+				best_dpg = cd;
 			}
 		}
 		lanes = best_lanes;
+		dpg = best_dpg;
 		cudaEventDestroy(e0);
 		cudaEventDestroy(e1);
 		cudaStreamDestroy(s);
@@ -212,7 +225,7 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -542,15 +555,19 @@ int stpgb_batch_download(stpgb_batch* b, float* const* heightmaps, uint16_t* con
 	return STPGB_OK;
 }
 
-int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, float* erosion_ms) {
+int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32_t* droplets_per_group,
+	float* erosion_ms) {
 	if (!b) {
 		return inval("stpgb_batch_tuning: null batch");
 	}
 	if (lanes_per_droplet) {
 		*lanes_per_droplet = b->lanes;
 	}
+	if (droplets_per_group) {
+		*droplets_per_group = b->dpg;
+	}
 	if (erosion_ms) {
-		for (int c = 0; c < 6; c++) {
+		for (int c = 0; c < 18; c++) {
 			erosion_ms[c] = b->tune_ms[c];
 		}
 	}

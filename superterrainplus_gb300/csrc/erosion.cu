@@ -269,6 +269,230 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 	}
 }
 
+// K droplets per group of G >= 4 lanes (reference order only).  The erosion
+// kernel is bound by the latency of each lane's chain of brush reads; a
+// droplet's chain cannot be shortened without changing how racing droplets
+// see each other, so instead each group carries K independent droplets and
+// advances them through every phase of a step together: the K corner reads,
+// and the K reads of each brush position, are in flight at the same time.
+// Each droplet still reads and updates its own brush points in order.
+template<uint32_t G, uint32_t K>
+__global__ void __launch_bounds__(kErodeBlock) erosion_multi_kernel(const ErosionJob* __restrict__ jobs,
+	const ErosionJob single) {
+	static_assert(G >= 4u && K >= 2u, "one corner per lane needs four lanes");
+	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
+	extern __shared__ unsigned char esm[];
+	int32_t* const bidx = reinterpret_cast<int32_t*>(esm);
+	float* const bw = reinterpret_cast<float*>(esm) + J.brush_size;
+	for (uint32_t k = threadIdx.x; k < J.brush_size; k += kErodeBlock) {
+		bidx[k] = J.brush_index[k];
+		bw[k] = J.brush_weight[k];
+	}
+	__syncthreads();
+
+	const RainParams& P = J.p;
+	const uint32_t g = threadIdx.x % G;
+	const uint32_t group = (blockIdx.x * kErodeBlock + threadIdx.x) / G;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gmask = G == 32u ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1u)));
+	const uint32_t glead = lane & ~(G - 1u);
+	const uint32_t corner = g & 3u;
+	float* const map = J.map;
+	const uint64_t pitch = J.pitch;
+	const uint64_t corner_off = ((corner & 2u) ? pitch : 0u) + (corner & 1u);
+	const uint32_t bsize = J.brush_size;
+	const float lo = static_cast<float>(P.BrushRadius);
+	const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
+
+	float px[K], py[K], dirx[K], diry[K], speed[K], vol[K], sed[K];
+	uint32_t step[K];
+	bool alive[K];
+	double residual = 0.0;
+	bool capped = false;
+	uint32_t steps_done = 0u, erode_steps = 0u;
+#pragma unroll
+	for (uint32_t k = 0u; k < K; k++) {
+		const uint32_t d = group * K + k;
+		alive[k] = d < J.count;
+		px[k] = alive[k] ? J.starts[2u * d] : 0.0f;
+		py[k] = alive[k] ? J.starts[2u * d + 1u] : 0.0f;
+		// a start whose 2x2 bilinear footprint is not inside the map dies at once
+		alive[k] = alive[k] && px[k] >= 0.0f && px[k] < J.dim_x - 1.0f && py[k] >= 0.0f && py[k] < J.dim_y - 1.0f;
+		dirx[k] = diry[k] = 0.0f;
+		speed[k] = P.initSpeed;
+		vol[k] = P.initWaterVolume;
+		sed[k] = 0.0f;
+		step[k] = 0u;
+	}
+	auto bilinear = [](const float v, const uint32_t gm, const uint32_t gl, const float cx, const float cy) {
+		const float h00 = __shfl_sync(gm, v, gl), h10 = __shfl_sync(gm, v, gl + 1), h01 = __shfl_sync(gm, v, gl + 2),
+			h11 = __shfl_sync(gm, v, gl + 3);
+		HG r;
+		r.h = h00 * (1.0f - cx) * (1.0f - cy) + h10 * cx * (1.0f - cy) + h01 * (1.0f - cx) * cy + h11 * cx * cy;
+		r.gx = (h10 - h00) * (1.0f - cy) + (h11 - h01) * cy;
+		r.gy = (h01 - h00) * (1.0f - cx) + (h11 - h10) * cx;
+		return r;
+	};
+
+	while (true) {
+		bool any = false;
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k] && !(vol[k] >= P.minWaterVolume)) {
+				alive[k] = false;
+				residual += sed[k];
+			} else if (alive[k] && step[k]++ >= P.MaxSteps) {
+				alive[k] = false;
+				capped = true;
+				residual += sed[k];
+			}
+			any = any || alive[k];
+		}
+		if (!any) {
+			break;
+		}
+		// phase 1: corners of the current cell of every droplet
+		uint64_t mi[K];
+		float ox[K], oy[K], v[K];
+		HG hg[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				mi[k] = static_cast<uint64_t>(static_cast<uint32_t>(py[k])) * pitch + static_cast<uint32_t>(px[k]);
+				ox[k] = px[k] - static_cast<float>(static_cast<int>(px[k]));
+				oy[k] = py[k] - static_cast<float>(static_cast<int>(py[k]));
+				v[k] = __ldcg(map + mi[k] + corner_off);
+			}
+		}
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				hg[k] = bilinear(v[k], gmask, glead, ox[k], oy[k]);
+				dirx[k] = (-hg[k].gx) * (1.0f - P.Inertia) + dirx[k] * P.Inertia;
+				diry[k] = (-hg[k].gy) * (1.0f - P.Inertia) + diry[k] * P.Inertia;
+				const float len = sqrtf(dirx[k] * dirx[k] + diry[k] * diry[k]);
+				if (len != 0.0f) {
+					dirx[k] /= len;
+					diry[k] /= len;
+				}
+				px[k] += dirx[k];
+				py[k] += diry[k];
+				if ((dirx[k] == 0.0f && diry[k] == 0.0f)
+					|| !(px[k] >= lo && px[k] < hi_x && py[k] >= lo && py[k] < hi_y)) {
+					alive[k] = false; // the carried sediment leaves with the droplet
+					residual += sed[k];
+				}
+			}
+		}
+		// phase 2: corners of the new cell, capacity, deposit or erode
+		float v2[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				const uint64_t ni = static_cast<uint64_t>(static_cast<uint32_t>(py[k])) * pitch + static_cast<uint32_t>(px[k]);
+				v2[k] = __ldcg(map + ni + corner_off);
+			}
+		}
+		bool erode[K];
+		float ero[K], dh[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			erode[k] = false;
+			if (alive[k]) {
+				const float cx = px[k] - static_cast<float>(static_cast<uint32_t>(px[k]));
+				const float cy = py[k] - static_cast<float>(static_cast<uint32_t>(py[k]));
+				dh[k] = bilinear(v2[k], gmask, glead, cx, cy).h - hg[k].h;
+				const float cap = fmaxf(-dh[k] * speed[k] * vol[k] * P.SedimentCapacityFactor, P.minSedimentCapacity);
+				if (sed[k] > cap || dh[k] > 0.0f) {
+					const float dep = (dh[k] > 0.0f) ? fminf(dh[k], sed[k]) : (sed[k] - cap) * P.DepositSpeed;
+					sed[k] -= dep;
+					if (g < 4u) {
+						const float wx = (corner & 1u) ? ox[k] : 1.0f - ox[k], wy = (corner & 2u) ? oy[k] : 1.0f - oy[k];
+						atomicAdd(map + mi[k] + corner_off, dep * wx * wy);
+					}
+				} else {
+					erode[k] = true;
+					erode_steps++;
+					ero[k] = fminf((cap - sed[k]) * P.ErodeSpeed, -dh[k]);
+				}
+			}
+		}
+		// phase 3: the brush chains of the eroding droplets, interleaved
+		float part[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			part[k] = 0.0f;
+		}
+#pragma unroll 1
+		for (uint32_t p = g; p < bsize; p += G) {
+			const int32_t off = bidx[p];
+			const float wp = bw[p];
+			float cur[K];
+#pragma unroll
+			for (uint32_t k = 0u; k < K; k++) {
+				if (erode[k]) {
+					cur[k] = __ldcg(map + static_cast<int64_t>(mi[k]) + off);
+				}
+			}
+#pragma unroll
+			for (uint32_t k = 0u; k < K; k++) {
+				if (erode[k]) {
+					const float we = ero[k] * wp;
+					const float ds = (cur[k] < we) ? cur[k] : we;
+					atomicAdd(map + static_cast<int64_t>(mi[k]) + off, -ds);
+					part[k] += ds;
+				}
+			}
+			asm volatile("" ::: "memory");
+		}
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (erode[k]) {
+#pragma unroll
+				for (uint32_t o = G / 2u; o > 0u; o >>= 1) {
+					part[k] += __shfl_xor_sync(gmask, part[k], o);
+				}
+				sed[k] += part[k];
+			}
+			if (alive[k]) {
+				speed[k] = sqrtf(fmaxf(0.0f, speed[k] * speed[k] + dh[k] * P.Gravity));
+				speed[k] *= 1.0f - P.Friction;
+				vol[k] *= 1.0f - P.EvaporateSpeed;
+				steps_done++;
+			}
+		}
+		__syncwarp(gmask);
+	}
+	if (g != 0u) {
+		residual = 0.0;
+		steps_done = 0u;
+		erode_steps = 0u;
+		capped = false;
+	}
+	if (J.counters) {
+		unsigned long long s = steps_done, e = erode_steps;
+		for (int o = 16; o > 0; o >>= 1) {
+			s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+			e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		}
+		if (lane == 0u) {
+			atomicAdd(J.counters, s);
+			atomicAdd(J.counters + 1, e);
+		}
+	}
+	if (J.residual) {
+		for (int o = 16; o > 0; o >>= 1) {
+			residual += __shfl_xor_sync(0xFFFFFFFFu, residual, o);
+		}
+		if (lane == 0u && residual != 0.0) {
+			atomicAdd(J.residual, residual);
+		}
+	}
+	if (capped && J.status) {
+		atomicOr(J.status, STATUS_TIMEOUT);
+	}
+}
+
 // STPHeightfieldKernel.cu:112-122, eight pixels per thread where rows allow.
 __device__ __forceinline__ uint32_t fmt1(const float h) {
 	return static_cast<uint32_t>(rintf(__saturatef(h) * 65535.0f));
@@ -361,11 +585,49 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 }
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp) {
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp,
+	uint32_t droplets_per_group) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
 	const size_t smem = static_cast<size_t>(max_brush) * (sizeof(int32_t) + sizeof(float));
+	if (droplets_per_group > 1u) {
+		if (exact_clamp || lanes_per_droplet < 4u || (droplets_per_group != 2u && droplets_per_group != 4u)) {
+			return inval("erosion: 2 or 4 droplets per group need >= 4 lanes and the reference order");
+		}
+		const uint64_t groups = (static_cast<uint64_t>(max_count) + droplets_per_group - 1u) / droplets_per_group;
+		const uint64_t mthreads = groups * lanes_per_droplet;
+		if (mthreads > 0xFFFFFFFFull - kErodeBlock) {
+			return inval("erosion: too many droplets for one launch");
+		}
+		const dim3 mgrid(static_cast<uint32_t>((mthreads + kErodeBlock - 1u) / kErodeBlock), njobs);
+		auto go = [&](auto kernel) -> int {
+			if (smem > 48u * 1024u) {
+				STPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+					static_cast<int>(smem)));
+			}
+			kernel<<<mgrid, kErodeBlock, smem, stream>>>(jobs, single);
+			STPGB_CUDA_TRY(cudaGetLastError());
+			return STPGB_OK;
+		};
+		const uint32_t key = lanes_per_droplet * 8u + droplets_per_group;
+		switch (key) {
+		case 4u * 8u + 2u:
+			return go(erosion_multi_kernel<4u, 2u>);
+		case 4u * 8u + 4u:
+			return go(erosion_multi_kernel<4u, 4u>);
+		case 8u * 8u + 2u:
+			return go(erosion_multi_kernel<8u, 2u>);
+		case 8u * 8u + 4u:
+			return go(erosion_multi_kernel<8u, 4u>);
+		case 16u * 8u + 2u:
+			return go(erosion_multi_kernel<16u, 2u>);
+		case 16u * 8u + 4u:
+			return go(erosion_multi_kernel<16u, 4u>);
+		default:
+			return inval("erosion: droplets per group supported with 4, 8 or 16 lanes");
+		}
+	}
 	const uint64_t threads = static_cast<uint64_t>(max_count) * lanes_per_droplet;
 	if (threads > 0xFFFFFFFFull - kErodeBlock) {
 		return inval("erosion: too many droplets for one launch");
@@ -432,12 +694,13 @@ int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stp
 	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
 	uint32_t brush_size, double* residual_sediment, uint32_t* status, void* stream) {
 	return stpgb_hydraulic_erosion_ex(heightmap, nn, setting, starts_xy, count, brush_index, brush_weight,
-		brush_size, residual_sediment, status, default_lanes(brush_size), 0u, stream);
+		brush_size, residual_sediment, status, default_lanes(brush_size), 1u, 0u, stream);
 }
 
 int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const stpgb_raindrop_setting* setting,
 	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
-	uint32_t brush_size, double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet, uint32_t flags,
+	uint32_t brush_size, double* residual_sediment, uint32_t* status, uint32_t lanes_per_droplet,
+	uint32_t droplets_per_group, uint32_t flags,
 	void* stream) {
 	STPGB_TRY(stpgb_raindrop_setting_validate(setting));
 	if (!heightmap || !nn || (count > 0u && !starts_xy) || !brush_index || !brush_weight || brush_size == 0u) {
@@ -467,7 +730,7 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	job.counters = nullptr;
 	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream),
 		lanes_per_droplet == 0u ? default_lanes(brush_size) : lanes_per_droplet,
-		(flags & STPGB_EROSION_EXACT_CLAMP) != 0u);
+		(flags & STPGB_EROSION_EXACT_CLAMP) != 0u, droplets_per_group == 0u ? 1u : droplets_per_group);
 }
 
 int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x, uint32_t map_y, void* stream) {

@@ -35,9 +35,12 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 
 // lanes_per_droplet: 1, 2, 4, 8, 16 or 32 lanes carry one droplet;
 // exact_clamp: brush updates by compare-and-swap (never more than a cell
-// holds) instead of the reference's read-then-subtract order
+// holds) instead of the reference's read-then-subtract order;
+// droplets_per_group: 1, or 2 / 4 droplets advanced together by a group of
+// 4, 8 or 16 lanes (reference order only)
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
-	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false);
+	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
+	uint32_t droplets_per_group = 1u);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).

@@ -139,9 +139,17 @@ EROSION_CASES = {
 }
 
 
+VARIANTS = {
+    "default": {},
+    "exact-clamp": {"exact_clamp": True},
+    "2-droplets-per-group": {"droplets_per_group": 2},
+    "4-droplets-per-group": {"droplets_per_group": 4},
+}
+
+
 @pytest.mark.parametrize("case", sorted(EROSION_CASES))
-@pytest.mark.parametrize("exact_clamp", [False, True])
-def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, exact_clamp):
+@pytest.mark.parametrize("variant", sorted(VARIANTS))
+def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, variant):
     """Per-pixel RMS against the FP64 serial oracle stays within the reference kernel's own band.
 
     The reference kernel is one thread per droplet reading and updating the brush point by point
@@ -158,9 +166,12 @@ def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, exact_cla
     ref_runs = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 5, lanes=1)
     ref_rms = [rms(r, ref) for r, _ in ref_runs]
     spread = max(rms(a, b) for i, (a, _) in enumerate(ref_runs) for b, _ in ref_runs[i + 1:])
-    prod = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 3, exact_clamp=exact_clamp)
+    kw = dict(VARIANTS[variant])
+    if kw.get("droplets_per_group", 1) > 1:
+        kw["lanes"] = 4  # several droplets per group need >= 4 lanes; every brush here allows 4
+    prod = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 3, **kw)
     prod_rms = [rms(r, ref) for r, _ in prod]
-    print(f"{case} exact_clamp={exact_clamp}: reference kernel RMS vs FP64 {min(ref_rms):.3g}..{max(ref_rms):.3g}, "
+    print(f"{case} {variant}: reference kernel RMS vs FP64 {min(ref_rms):.3g}..{max(ref_rms):.3g}, "
           f"spread {spread:.3g}; production RMS {prod_rms}")
     assert max(prod_rms) <= max(ref_rms) + spread
     total = h.astype(np.float64).sum()
