@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--batch", type=int, default=16)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--serve-requests", type=int, default=600,
+                   help="camera-walk requests replayed through the server (0 skips the serving section)")
     return p.parse_args()
 
 
@@ -338,6 +340,10 @@ def run_ours(args):
                 "note": "erosion bytes = 32 B gather per realised step + 16 B deposit or 8 B x brush per step; "
                         "the 9.4 MB merged map of each request is L2-resident"}
 
+    serving = None
+    if rank == 0 and args.serve_requests > 0:
+        serving = serve_section(m, np, torch, args.serve_requests)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cores, sample = cpu_eroded_chunk(os.cpu_count() or 1)
@@ -361,6 +367,7 @@ def run_ours(args):
             "stage_ms": dict(zip(stage_names, stage_ms)),
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
+            "serving": serving,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}": v for (a, b), v in tune_ms.items()}},
             "gpu_launches": 7 * args.steps,
@@ -368,6 +375,66 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def serve_section(m, np, torch, n):
+    """Camera walk (1 chunk/s, new heading every 5 s), Poisson arrivals at 200/s, LOD sides
+    256/512/1024 with p 0.5/0.35/0.15, 3x3 neighbourhoods, 8 biomes, radius 32, 2.3 droplets/px,
+    brush 4, lifetime 50, through the continuous-batching server on a 40 GB pool; beside it the
+    plain per-request call sequence (9 generate + 1 erode through the drop-in generator API, host
+    buffers) on a sample of the same requests."""
+    from superterrainplus_gb300.serve import Server, camera_walk
+    reqs, times = camera_walk(n, SEED, rate=200.0)
+    base = raindrop(m, 1)
+    simplex = m.SimplexSetting(*SIMPLEX)
+    table = biome_table(np, m.BIOME_DTYPE)
+    sv = Server(base, simplex, table, hbm_budget=40 << 30, max_in_flight=64, max_batch=16, streams=3,
+                voronoi_cell=VORONOI_CELL, biome_seed=SEED)
+    warm, wt = camera_walk(16, SEED + 1, rate=1e6)
+    for w in warm:  # warm-up far from the measured walk, so it leaves no resident chunk behind for it
+        w["ChunkX"] += 100000
+    sv.replay(warm, wt)
+    lat, wall = sv.replay(reqs, times)
+    stats = sv.stats()
+    sv.close()
+    px512 = sum((r["MapSize"] / 512.0) ** 2 for r in reqs)
+    out = {"requests": n, "arrival_rate_per_s": 200.0, "wall_s": wall, "chunks_per_s": n / wall,
+           "chunks_512_equivalent_per_s": px512 / wall, "p50_latency_ms": float(np.percentile(lat, 50)),
+           "p99_latency_ms": float(np.percentile(lat, 99)), "chunks_generated": stats["ChunksGenerated"],
+           "launch_sequences": stats["Launches"], "hbm_pool_gb": 40}
+    # plain per-request calls on a sample of the same requests
+    dev = m.DeviceOps()
+    gens, sample = {}, reqs[: min(12, n)]
+    plain_lat = []
+    for r in sample:
+        S = r["MapSize"]
+        if S not in gens:
+            cs = m.ChunkSetting()
+            cs.MapSize[:] = [S, S]
+            cs.DiversityNearestNeighbour[:] = [3, 3]
+            cs.ErosionNearestNeighbour[:] = [3, 3]
+            rd = raindrop(m, int(round(2.3 * S * S)))
+            gens[S] = m.STPHeightfieldGenerator(cs, rd, simplex, table, RADIUS)
+        region = torch.empty((5 * S, 5 * S), dtype=torch.int16, device="cuda")
+        cell = max(1, VORONOI_CELL * S // 512)
+        dev.voronoi_biomemap(region, 5 * S, 5 * S, 5 * S, ((r["ChunkX"] - 2) * S, (r["ChunkY"] - 2) * S), cell,
+                             BIOMES, SEED)
+        reg = region.cpu().numpy().view(np.uint16)
+        chunk = lambda bx, by: np.ascontiguousarray(reg[by * S:(by + 1) * S, bx * S:(bx + 1) * S])
+        heights = [np.zeros((S, S), np.float32) for _ in range(9)]
+        fixed = [np.zeros((S, S), np.uint16) for _ in range(9)]
+        t0 = time.perf_counter()
+        for c in range(9):
+            cx, cy = c % 3 + 1, c // 3 + 1  # in the 5x5 region
+            biomes = [chunk(cx + (k % 3) - 1, cy + (k // 3) - 1) for k in range(9)]
+            gens[S].generate(heights[c], biomes, (float((r["ChunkX"] + c % 3 - 1) * S),
+                                                  float((r["ChunkY"] + c // 3 - 1) * S)))
+        gens[S].erode(heights, fixed)
+        plain_lat.append((time.perf_counter() - t0) * 1000.0)
+    out["plain_per_request"] = {"sample": len(sample), "chunks_per_s": len(sample) / (sum(plain_lat) / 1000.0),
+                                "p50_latency_ms": float(np.percentile(plain_lat, 50)),
+                                "note": "drop-in generator API, host buffers, one request at a time, no queueing"}
+    return out
 
 
 if __name__ == "__main__":

@@ -406,6 +406,76 @@ STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_d
 STPGB_API int stpgb_batch_counters(stpgb_batch* batch, uint64_t* realised_steps, uint64_t* erode_steps,
 	int reset);
 
+/* ---------------------------------------------------------- serving ---- */
+
+/* No counterpart in the reference (its world pipeline, SuperTerrain+/
+ * SuperTerrain+/Private/World/STPWorldPipeline.cpp:411-662, runs one
+ * synchronous generate/erode call per chunk from a host thread pool).  A
+ * continuous-batching server: requests are admitted against a fixed HBM
+ * budget, batched with whatever else is admitted while earlier batches run
+ * on other streams, and served from resident generated chunks shared by
+ * overlapping neighbourhoods.  Each request erodes a private copy of its
+ * 3x3 neighbourhood, so its result does not depend on the other requests. */
+typedef struct stpgb_server stpgb_server;
+
+typedef struct stpgb_server_config {
+	uint64_t HbmBudget;    /* device bytes of the pool (results, resident chunks, scratch) */
+	uint32_t MaxInFlight;  /* requests admitted and not yet complete */
+	uint32_t MaxBatch;     /* requests per launch sequence */
+	uint32_t Streams;      /* launch sequences in flight at once */
+	uint32_t VoronoiCell;  /* synthetic biome-map cell, in pixels of a 512 chunk (scaled with the side) */
+	uint64_t BiomeSeed;
+} stpgb_server_config;
+
+typedef struct stpgb_serve_request {
+	int32_t ChunkX, ChunkY;       /* centre chunk of the 3x3 neighbourhood */
+	uint32_t MapSize;             /* chunk side (level of detail), a multiple of 8 */
+	uint32_t InterpolationRadius; /* filter radius, even, <= MapSize */
+	float DropletsPerPixel;       /* droplets = round(DropletsPerPixel * MapSize^2) */
+	uint32_t BrushRadius;
+	uint32_t Lifetime;            /* droplet steps; 0 keeps the base minWaterVolume */
+	uint64_t UserTag;
+} stpgb_serve_request;
+
+typedef struct stpgb_serve_result {
+	uint64_t Ticket, UserTag;
+	int Status;
+	uint32_t MapSize;
+	double LatencyMs;              /* submission -> result complete on the device */
+	const float* Heightmap;        /* device, eroded (3*MapSize)^2 neighbourhood */
+	const uint16_t* HeightmapFixed; /* device, its uint16 format */
+	double ResidualSediment;
+} stpgb_serve_result;
+
+typedef struct stpgb_server_stats {
+	uint64_t Submitted, Admitted, Completed, Launches, ChunksGenerated, ChunksEvicted;
+	uint64_t PoolBytesUsed, ResidentChunks;
+} stpgb_server_stats;
+
+/* Allocates the pool (STPGB_ENOMEM if the budget cannot be had) and starts
+ * the scheduler thread on the current device. */
+STPGB_API int stpgb_server_create(const stpgb_server_config* config, const stpgb_raindrop_setting* base,
+	const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table, uint32_t biome_count,
+	stpgb_server** out);
+STPGB_API int stpgb_server_destroy(stpgb_server* server);
+/* Thread-safe, non-blocking.  STPGB_ENOMEM if one request alone exceeds the budget. */
+STPGB_API int stpgb_server_submit(stpgb_server* server, const stpgb_serve_request* request, uint64_t* ticket);
+/* Up to `capacity` completed results; waits up to `wait_ms` (-1 = until one completes). */
+STPGB_API int stpgb_server_poll(stpgb_server* server, stpgb_serve_result* results, uint32_t capacity,
+	uint32_t* count, int wait_ms);
+/* Copies a completed, not yet released result to HOST memory ((3*MapSize)^2
+ * floats and uint16; either may be NULL).  Synchronous. */
+STPGB_API int stpgb_server_download(stpgb_server* server, uint64_t ticket, float* heightmap,
+	uint16_t* heightmap_fixed);
+/* Returns a completed result's device memory to the pool. */
+STPGB_API int stpgb_server_release(stpgb_server* server, uint64_t ticket);
+STPGB_API int stpgb_server_stats_get(stpgb_server* server, stpgb_server_stats* stats);
+/* Submits `requests[i]` at `arrival_s[i]` seconds after the call (ascending),
+ * releases every result as it completes, writes each request's latency and
+ * the wall time until the last completed.  Synchronous. */
+STPGB_API int stpgb_server_replay(stpgb_server* server, const stpgb_serve_request* requests,
+	const double* arrival_s, uint32_t count, double* latency_ms, double* wall_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,29 @@ class BatchRequest(C.Structure):
                 ("Lifetime", C.c_uint32)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("HbmBudget", C.c_uint64), ("MaxInFlight", C.c_uint32), ("MaxBatch", C.c_uint32),
+                ("Streams", C.c_uint32), ("VoronoiCell", C.c_uint32), ("BiomeSeed", C.c_uint64)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("ChunkX", C.c_int32), ("ChunkY", C.c_int32), ("MapSize", C.c_uint32),
+                ("InterpolationRadius", C.c_uint32), ("DropletsPerPixel", C.c_float), ("BrushRadius", C.c_uint32),
+                ("Lifetime", C.c_uint32), ("UserTag", C.c_uint64)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("Ticket", C.c_uint64), ("UserTag", C.c_uint64), ("Status", C.c_int), ("MapSize", C.c_uint32),
+                ("LatencyMs", C.c_double), ("Heightmap", C.c_void_p), ("HeightmapFixed", C.c_void_p),
+                ("ResidualSediment", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("Submitted", C.c_uint64), ("Admitted", C.c_uint64), ("Completed", C.c_uint64),
+                ("Launches", C.c_uint64), ("ChunksGenerated", C.c_uint64), ("ChunksEvicted", C.c_uint64),
+                ("PoolBytesUsed", C.c_uint64), ("ResidentChunks", C.c_uint64)]
+
+
 STPGB_BATCH_GRAPH = 1
 STPGB_BATCH_AUTOTUNE = 2
 
@@ -142,6 +165,15 @@ PROTOTYPES = {
     "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), vp]),
     "stpgb_batch_tune": (C.c_int, [vp]),
     "stpgb_batch_download_inputs": (C.c_int, [vp, vp, vp, vp]),
+    "stpgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(RaindropSetting), C.POINTER(SimplexSetting),
+                                      vp, u32, C.POINTER(vp)]),
+    "stpgb_server_destroy": (C.c_int, [vp]),
+    "stpgb_server_submit": (C.c_int, [vp, C.POINTER(ServeRequest), C.POINTER(u64)]),
+    "stpgb_server_poll": (C.c_int, [vp, C.POINTER(ServeResult), u32, C.POINTER(u32), C.c_int]),
+    "stpgb_server_release": (C.c_int, [vp, u64]),
+    "stpgb_server_download": (C.c_int, [vp, u64, vp, vp]),
+    "stpgb_server_stats_get": (C.c_int, [vp, C.POINTER(ServerStats)]),
+    "stpgb_server_replay": (C.c_int, [vp, C.POINTER(ServeRequest), vp, u32, vp, C.POINTER(f64)]),
     "stpgb_batch_counters": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64), C.c_int]),
 }
 

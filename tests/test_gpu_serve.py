@@ -1,0 +1,115 @@
+"""The continuous-batching server: generation of resident chunks against the
+oracle (through the mass balance of every eroded result), results the same
+alone and in a mix (within the erosion's run-to-run spread), admission under
+a small HBM budget, refusal of a request larger than the budget, and a short
+camera-walk replay."""
+import numpy as np
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+NB, SEED, CELL = 6, 11, 160
+REQS = [dict(ChunkX=x, ChunkY=y, MapSize=S, InterpolationRadius=16, DropletsPerPixel=2.3, BrushRadius=3,
+             Lifetime=30, UserTag=i)
+        for i, (x, y, S) in enumerate([(0, 0, 64), (1, 0, 64), (0, 1, 64), (1, 1, 64), (-1, -1, 64), (3, 0, 64),
+                                       (0, 0, 128), (1, 0, 128)])]
+
+
+def make_server(stpgb, **kw):
+    from superterrainplus_gb300.serve import Server
+    base = stpgb.RaindropSetting(**helpers.raindrop_dict(1000, radius=3, lifetime=30, seed=SEED))
+    simplex = stpgb.SimplexSetting(SEED, 8, 0.2181661565)
+    args = dict(hbm_budget=1 << 30, max_in_flight=16, max_batch=8, streams=3, voronoi_cell=CELL, biome_seed=SEED)
+    args.update(kw)
+    return Server(base, simplex, helpers.biome_table(NB, SEED), **args)
+
+
+def run_all(server, reqs):
+    tickets = {server.submit(**r): r["UserTag"] for r in reqs}
+    out = {}
+    while len(out) < len(tickets):
+        for res in server.poll(wait_ms=2000):
+            assert res.Status == 0
+            h, f = server.download(res)
+            out[res.UserTag] = (h, f, res.ResidualSediment, res.LatencyMs)
+            server.release(res.Ticket)
+    return out
+
+
+def expected_merged(oracle, stpgb, r):
+    """Pre-erosion neighbourhood of a request from the oracle (Voronoi, filter, noise)."""
+    S, rad = r["MapSize"], r["InterpolationRadius"]
+    table = helpers.biome_table(NB, SEED)
+    perm, grad = stpgb.permutation_generate(SEED, 8, 0.2181661565)
+    cell = max(1, CELL * S // 512)
+    out = np.zeros((3 * S, 3 * S), np.float32)
+    for c in range(9):
+        kx, ky = r["ChunkX"] + c % 3 - 1, r["ChunkY"] + c // 3 - 1
+        region = oracle.voronoi(3 * S, 3 * S, ((kx - 1) * S, (ky - 1) * S), cell, NB, SEED)
+        rc, off, bins = oracle.shf(region, (S, S), (3, 3), rad)
+        assert rc == 0
+        h = oracle.multibiome(off, bins, table, perm, grad, (S, S), (float(kx * S), float(ky * S)))
+        out[(c // 3) * S:(c // 3 + 1) * S, (c % 3) * S:(c % 3 + 1) * S] = h
+    return out
+
+
+def test_serve_generation_mass_balance_and_format(stpgb, dev, oracle):
+    sv = make_server(stpgb)
+    res = run_all(sv, REQS)
+    st = sv.stats()
+    # neighbourhoods overlap: far fewer chunks generated than 9 per request
+    assert st["ChunksGenerated"] < 9 * len(REQS)
+    for r in REQS:
+        h, f, residual, lat = res[r["UserTag"]]
+        pre = expected_merged(oracle, stpgb, r).astype(np.float64)
+        total = pre.sum()
+        assert abs((total - h.astype(np.float64).sum()) - residual) <= 1e-5 * total, r
+        assert np.array_equal(f, oracle.format(h))
+        assert lat > 0.0
+    sv.close()
+
+
+def test_serve_same_alone_and_in_the_mix(stpgb, dev):
+    mix = run_all(make_server(stpgb), REQS)
+    alone1, alone2 = {}, {}
+    for r in REQS:
+        alone1.update(run_all(make_server(stpgb), [r]))
+        alone2.update(run_all(make_server(stpgb), [r]))
+    spread = max(float(np.sqrt(np.mean((alone1[k][0] - alone2[k][0]).astype(np.float64) ** 2))) for k in alone1)
+    for k in alone1:
+        d = float(np.sqrt(np.mean((alone1[k][0] - mix[k][0]).astype(np.float64) ** 2)))
+        print(f"request {k}: RMS alone vs mix {d:.3g}, run-to-run spread {spread:.3g}")
+        assert d <= 2.0 * spread + 1e-6
+
+
+def test_serve_admission_under_small_budget(stpgb, dev):
+    # about two 64-side requests with their generation scratch fit at once
+    budget = 24 << 20
+    sv = make_server(stpgb, hbm_budget=budget, max_in_flight=64)
+    reqs = [dict(r, UserTag=i) for i, r in enumerate(REQS[:6])]
+    res = run_all(sv, reqs)
+    assert len(res) == 6
+    st = sv.stats()
+    assert st["Completed"] == 6 and st["PoolBytesUsed"] <= budget
+    sv.close()
+
+
+def test_serve_refuses_request_above_budget(stpgb, dev):
+    sv = make_server(stpgb, hbm_budget=8 << 20)
+    with pytest.raises(stpgb.STPInsufficientMemory):
+        sv.submit(**dict(REQS[-1], MapSize=512))
+    sv.close()
+
+
+def test_serve_camera_walk_replay(stpgb, dev):
+    from superterrainplus_gb300.serve import camera_walk
+    reqs, times = camera_walk(40, 3, rate=400.0, lods=(64, 128), probs=(0.6, 0.4), radius=16, brush=3, lifetime=30)
+    keys = {(r["MapSize"], r["ChunkX"], r["ChunkY"]) for r in reqs}
+    assert len(keys) == len(reqs)  # every request is a chunk not requested before
+    sv = make_server(stpgb)
+    lat, wall = sv.replay(reqs, times)
+    assert np.all(lat > 0.0) and wall >= times[-1]
+    assert sv.stats()["Completed"] == len(reqs)
+    sv.close()
