@@ -417,33 +417,51 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_multi_kernel(const Erosio
 				}
 			}
 		}
-		// phase 3: the brush chains of the eroding droplets, interleaved
+		// phase 3: the brush chains of the eroding droplets, interleaved.  Two
+		// droplets of the group whose brushes overlap (droplets that flowed
+		// into the same channel stay together) would read the same cells in
+		// the same instruction and both remove the same stale height, step
+		// after step; their chains then run one droplet after the other, so
+		// the second reads the first one's updates.
 		float part[K];
+		bool serial = false;
+		const int32_t reach = 2 * static_cast<int32_t>(P.BrushRadius) - 2;
 #pragma unroll
 		for (uint32_t k = 0u; k < K; k++) {
 			part[k] = 0.0f;
+#pragma unroll
+			for (uint32_t q = k + 1u; q < K; q++) {
+				if (erode[k] && erode[q]) {
+					const int32_t dx = static_cast<int32_t>(mi[k] % pitch) - static_cast<int32_t>(mi[q] % pitch);
+					const int32_t dy = static_cast<int32_t>(mi[k] / pitch) - static_cast<int32_t>(mi[q] / pitch);
+					serial = serial || (abs(dx) <= reach && abs(dy) <= reach);
+				}
+			}
 		}
 #pragma unroll 1
-		for (uint32_t p = g; p < bsize; p += G) {
-			const int32_t off = bidx[p];
-			const float wp = bw[p];
-			float cur[K];
+		for (uint32_t turn = 0u; turn < (serial ? K : 1u); turn++) {
+#pragma unroll 1
+			for (uint32_t p = g; p < bsize; p += G) {
+				const int32_t off = bidx[p];
+				const float wp = bw[p];
+				float cur[K];
 #pragma unroll
-			for (uint32_t k = 0u; k < K; k++) {
-				if (erode[k]) {
-					cur[k] = __ldcg(map + static_cast<int64_t>(mi[k]) + off);
+				for (uint32_t k = 0u; k < K; k++) {
+					if (erode[k] && (!serial || k == turn)) {
+						cur[k] = __ldcg(map + static_cast<int64_t>(mi[k]) + off);
+					}
 				}
-			}
 #pragma unroll
-			for (uint32_t k = 0u; k < K; k++) {
-				if (erode[k]) {
-					const float we = ero[k] * wp;
-					const float ds = (cur[k] < we) ? cur[k] : we;
-					atomicAdd(map + static_cast<int64_t>(mi[k]) + off, -ds);
-					part[k] += ds;
+				for (uint32_t k = 0u; k < K; k++) {
+					if (erode[k] && (!serial || k == turn)) {
+						const float we = ero[k] * wp;
+						const float ds = (cur[k] < we) ? cur[k] : we;
+						atomicAdd(map + static_cast<int64_t>(mi[k]) + off, -ds);
+						part[k] += ds;
+					}
 				}
+				asm volatile("" ::: "memory");
 			}
-			asm volatile("" ::: "memory");
 		}
 #pragma unroll
 		for (uint32_t k = 0u; k < K; k++) {

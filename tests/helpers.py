@@ -78,6 +78,21 @@ def biome_table(n, seed):
     return t
 
 
+def multibiome_terrain(oracle, stpgb, S, nbiomes, cell, seed):
+    """A 3x3 neighbourhood of S^2 chunks from the oracle pipeline (Voronoi biome map, filter
+    radius 16, multi-biome fractal noise)."""
+    table = biome_table(nbiomes, seed)
+    perm, grad = stpgb.permutation_generate(seed, 8, 0.2181661565)
+    out = np.zeros((3 * S, 3 * S), np.float32)
+    for c in range(9):
+        kx, ky = c % 3 - 1, c // 3 - 1
+        region = oracle.voronoi(3 * S, 3 * S, ((kx - 1) * S, (ky - 1) * S), cell, nbiomes, seed)
+        rc, off, bins = oracle.shf(region, (S, S), (3, 3), 16)
+        h = oracle.multibiome(off, bins, table, perm, grad, (S, S), (float(kx * S), float(ky * S)))
+        out[(c // 3) * S:(c // 3 + 1) * S, (c % 3) * S:(c % 3 + 1) * S] = h
+    return out
+
+
 def raindrop_dict(count, radius=3, lifetime=30, seed=42):
     """Droplet settings of the small plain-method workload (inertia 0.05,
     capacity 4, min capacity 0.01, deposit 0.3, erode 0.3, evaporate 0.01,

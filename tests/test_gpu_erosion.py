@@ -139,6 +139,22 @@ EROSION_CASES = {
 }
 
 
+@pytest.mark.parametrize("lanes,droplets_per_group", [(1, 1), (2, 1), (4, 1), (4, 2), (4, 4)])
+def test_erosion_stays_physical_where_droplets_channel(dev, oracle, stpgb, lanes, droplets_per_group):
+    """Multi-biome terrain with many biome borders gathers densely packed droplets (2.3 per pixel
+    of a 64^2 chunk) into shared channels; in no variant may the heights leave their range."""
+    S = 64
+    h = helpers.multibiome_terrain(oracle, stpgb, S, 6, 20, 11)
+    count = int(round(2.3 * S * S))
+    s = helpers.raindrop_dict(count, radius=3, lifetime=30, seed=11)
+    starts = oracle.droplet_starts(count, 11, 0, (S, S), (3, 3))
+    total = h.astype(np.float64).sum()
+    for out, res in erode_runs(dev, stpgb, h, (S, S), (3, 3), s, starts, 10, lanes=lanes,
+                               droplets_per_group=droplets_per_group):
+        assert np.isfinite(out).all() and out.min() >= h.min() - 1e-3 and out.max() <= h.max() + 1e-3
+        assert abs((total - out.sum()) - res) <= 1e-5 * total
+
+
 VARIANTS = {
     "default": {},
     "exact-clamp": {"exact_clamp": True},

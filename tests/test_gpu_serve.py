@@ -77,6 +77,9 @@ def test_serve_same_alone_and_in_the_mix(stpgb, dev):
     for r in REQS:
         alone1.update(run_all(make_server(stpgb), [r]))
         alone2.update(run_all(make_server(stpgb), [r]))
+    for res in (mix, alone1, alone2):
+        for h, _, _, _ in res.values():
+            assert np.isfinite(h).all() and h.min() >= 0.0 and h.max() <= 1.0  # heights stay physical
     spread = max(float(np.sqrt(np.mean((alone1[k][0] - alone2[k][0]).astype(np.float64) ** 2))) for k in alone1)
     for k in alone1:
         d = float(np.sqrt(np.mean((alone1[k][0] - mix[k][0]).astype(np.float64) ** 2)))
