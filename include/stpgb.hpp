@@ -1,0 +1,241 @@
+/*
+ * stpgb.hpp — C++ façade over the C ABI (stpgb.h) with the reference's class
+ * names, namespaces and exception types for the heightfield path, so that a
+ * C++ caller of SuperTerrain+ switches by changing includes and linking
+ * libstpgb.so.  Header-only; vector-like arguments accept any type with
+ * .x / .y members (glm::vec2, glm::uvec2, ...).
+ *
+ *   SuperTerrainPlus::STPAlgorithm::STPPermutationGenerator::generate
+ *       (SuperAlgorithm+Host/STPPermutationGenerator.h:23-50)
+ *   SuperTerrainPlus::STPAlgorithm::STPSingleHistogramFilter + STPFilterBuffer
+ *       (SuperAlgorithm+Host/STPSingleHistogramFilter.h:36-190)
+ *   SuperTerrainPlus::STPHeightfieldGenerator::generate / erode
+ *       (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,145,159)
+ *   SuperTerrainPlus::STPException::{STPNumericDomainError, STPInvalidEnvironment, STPCUDAError}
+ */
+#ifndef STPGB_HPP_
+#define STPGB_HPP_
+
+#include "stpgb.h"
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace SuperTerrainPlus {
+
+typedef uint16_t STPSample_t;
+typedef float STPHeightFloat_t;
+typedef uint16_t STPHeightFixed_t;
+typedef uint64_t STPSeed_t;
+
+namespace STPException {
+
+class STPFundamentalException : public std::runtime_error {
+public:
+	using std::runtime_error::runtime_error;
+};
+class STPNumericDomainError : public STPFundamentalException {
+public:
+	using STPFundamentalException::STPFundamentalException;
+};
+class STPInvalidEnvironment : public STPFundamentalException {
+public:
+	using STPFundamentalException::STPFundamentalException;
+};
+class STPCUDAError : public STPFundamentalException {
+public:
+	using STPFundamentalException::STPFundamentalException;
+};
+class STPInsufficientMemory : public STPFundamentalException {
+public:
+	using STPFundamentalException::STPFundamentalException;
+};
+
+} // namespace STPException
+
+namespace detail {
+
+// Throws the reference's exception type for a C ABI status; `environment`
+// selects STPInvalidEnvironment for setting validation failures.
+inline void check(int rc, bool environment = false) {
+	if (rc == STPGB_OK) {
+		return;
+	}
+	const std::string msg = stpgb_last_error();
+	switch (rc) {
+	case STPGB_EINVAL:
+		if (environment) {
+			throw STPException::STPInvalidEnvironment(msg);
+		}
+		throw STPException::STPNumericDomainError(msg);
+	case STPGB_ECUDA:
+		throw STPException::STPCUDAError(msg);
+	case STPGB_ENOMEM:
+		throw STPException::STPInsufficientMemory(msg);
+	default:
+		throw STPException::STPFundamentalException("status " + std::to_string(rc) + ": " + msg);
+	}
+}
+
+template<class V>
+stpgb_nn_info nn(const V& map, const V& neighbour) {
+	stpgb_nn_info i {};
+	i.MapSize[0] = static_cast<uint32_t>(map.x);
+	i.MapSize[1] = static_cast<uint32_t>(map.y);
+	i.ChunkNearestNeighbour[0] = static_cast<uint32_t>(neighbour.x);
+	i.ChunkNearestNeighbour[1] = static_cast<uint32_t>(neighbour.y);
+	i.TotalMapSize[0] = i.MapSize[0] * i.ChunkNearestNeighbour[0];
+	i.TotalMapSize[1] = i.MapSize[1] * i.ChunkNearestNeighbour[1];
+	return i;
+}
+
+} // namespace detail
+
+namespace STPEnvironment {
+
+struct STPSimplexNoiseSetting : stpgb_simplex_setting {
+	void validate() const {
+		detail::check(stpgb_simplex_setting_validate(this), true);
+	}
+};
+
+struct STPRainDropSetting : stpgb_raindrop_setting {
+	void validate() const {
+		detail::check(stpgb_raindrop_setting_validate(this), true);
+	}
+};
+
+} // namespace STPEnvironment
+
+namespace STPAlgorithm {
+
+/* STPSingleHistogram (SuperAlgorithm+Host/STPSingleHistogram.hpp:15-50) */
+struct STPSingleHistogram {
+	typedef stpgb_bin STPBin;
+	const STPBin* Bin;
+	const unsigned int* HistogramStartOffset;
+};
+
+class STPSingleHistogramFilter {
+public:
+	class STPFilterBuffer {
+	public:
+		enum class STPExecutionType : unsigned char { Serial = 0x00u, Parallel = 0x01u };
+		typedef std::pair<size_t, size_t> STPHistogramSize;
+
+		explicit STPFilterBuffer(STPExecutionType type) : Type(type) {}
+
+		STPSingleHistogram readHistogram() const {
+			return STPSingleHistogram { Bins.data(), Offsets.data() };
+		}
+		STPHistogramSize size() const {
+			return { Bins.size(), Offsets.size() };
+		}
+		STPExecutionType type() const noexcept {
+			return Type;
+		}
+
+	private:
+		friend class STPSingleHistogramFilter;
+		STPExecutionType Type;
+		std::vector<stpgb_bin> Bins;
+		std::vector<unsigned int> Offsets;
+	};
+
+	/* `nn_info` is any STPNearestNeighbourInformation-like value with
+	 * MapSize / ChunkNearestNeighbour members (.x, .y).  Both execution
+	 * types run the same GPU filter and give the reference's result. */
+	template<class NN>
+	STPSingleHistogram operator()(const STPSample_t* samplemap, const NN& nn_info, STPFilterBuffer& buffer,
+		unsigned int radius) {
+		const stpgb_nn_info info = detail::nn(nn_info.MapSize, nn_info.ChunkNearestNeighbour);
+		const size_t npix = static_cast<size_t>(info.MapSize[0]) * info.MapSize[1];
+		const uint64_t side = 2ull * radius + 1ull;
+		const uint64_t cap = npix * (side * side < 256u ? side * side : 256u);
+		buffer.Offsets.resize(npix + 1u);
+		buffer.Bins.resize(static_cast<size_t>(cap > 0u ? cap : 1u));
+		uint64_t n = 0u;
+		detail::check(stpgb_shf_filter_host(samplemap, &info, radius, buffer.Offsets.data(), buffer.Bins.data(), cap, &n));
+		buffer.Bins.resize(static_cast<size_t>(n));
+		return buffer.readHistogram();
+	}
+};
+
+/* STPPermutation (SuperAlgorithm+Host/STPPermutation.hpp:9-22), device pointers */
+typedef stpgb_permutation STPPermutation;
+
+namespace STPPermutationGenerator {
+
+/* Host copies of the generated tables; Permutation points at device copies
+ * made by upload() (the reference keeps only device memory). */
+class STPPermutationTable {
+public:
+	std::vector<uint8_t> HostPermutation;
+	std::vector<float> HostGradient2D;
+	STPPermutation Permutation {};
+};
+
+inline STPPermutationTable generate(const STPEnvironment::STPSimplexNoiseSetting& setting) {
+	setting.validate();
+	STPPermutationTable t;
+	t.HostPermutation.resize(512u);
+	t.HostGradient2D.resize(2u * setting.Distribution);
+	detail::check(stpgb_permutation_generate(&setting, t.HostPermutation.data(), t.HostGradient2D.data(),
+		static_cast<uint32_t>(t.HostGradient2D.size())), true);
+	t.Permutation.Gradient2DSize = setting.Distribution;
+	return t;
+}
+
+} // namespace STPPermutationGenerator
+
+} // namespace STPAlgorithm
+
+/* STPHeightfieldGenerator with the multi-biome diversity plugin
+ * (STPBiomefieldGenerator) folded in: the plugin's biome table and
+ * interpolation radius are constructor arguments. */
+class STPHeightfieldGenerator {
+public:
+	template<class V>
+	STPHeightfieldGenerator(const V& map_size, const V& diversity_nn, const V& erosion_nn,
+		const STPEnvironment::STPRainDropSetting& raindrop, const STPEnvironment::STPSimplexNoiseSetting& simplex,
+		const std::vector<stpgb_biome_property>& biome_table, unsigned int interpolation_radius) {
+		stpgb_chunk_setting c {};
+		c.MapSize[0] = static_cast<uint32_t>(map_size.x);
+		c.MapSize[1] = static_cast<uint32_t>(map_size.y);
+		c.DiversityNearestNeighbour[0] = static_cast<uint32_t>(diversity_nn.x);
+		c.DiversityNearestNeighbour[1] = static_cast<uint32_t>(diversity_nn.y);
+		c.ErosionNearestNeighbour[0] = static_cast<uint32_t>(erosion_nn.x);
+		c.ErosionNearestNeighbour[1] = static_cast<uint32_t>(erosion_nn.y);
+		stpgb_generator* g = nullptr;
+		detail::check(stpgb_generator_create(&c, &raindrop, &simplex, biome_table.data(),
+			static_cast<uint32_t>(biome_table.size()), interpolation_radius, &g), true);
+		Handle.reset(g);
+	}
+
+	/* STPHeightfieldGenerator::generate (STPHeightfieldGenerator.cpp:158-169) */
+	template<class V>
+	void generate(STPHeightFloat_t* heightfield, const STPSample_t* const* biomemap, const V& offset) {
+		detail::check(stpgb_generator_generate(Handle.get(), heightfield, biomemap, static_cast<float>(offset.x),
+			static_cast<float>(offset.y)));
+	}
+
+	/* STPHeightfieldGenerator::erode (STPHeightfieldGenerator.cpp:171-197) */
+	void erode(STPHeightFloat_t* const* heightfield, STPHeightFixed_t* const* heightfield_fixed) {
+		detail::check(stpgb_generator_erode(Handle.get(), heightfield, heightfield_fixed));
+	}
+
+private:
+	struct Deleter {
+		void operator()(stpgb_generator* g) const {
+			stpgb_generator_destroy(g);
+		}
+	};
+	std::unique_ptr<stpgb_generator, Deleter> Handle;
+};
+
+} // namespace SuperTerrainPlus
+
+#endif /* STPGB_HPP_ */

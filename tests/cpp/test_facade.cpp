@@ -1,0 +1,231 @@
+// The reference's own test scenarios for the heightfield path, written
+// against the C++ façade (include/stpgb.hpp) the way a SuperTerrain+ caller
+// would: SuperTest+/SuperAlgorithm+/STPTestHistogram.cpp (known-answer
+// histograms and error cases), STPTestPermutation.cpp (gradients,
+// repetition, seeds, invalid setting), and a generate/erode round trip.
+// `--cpu` runs the parts that fail before any device work.
+#include "stpgb.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+using namespace SuperTerrainPlus;
+using STPAlgorithm::STPSingleHistogramFilter;
+using FiltBuf = STPSingleHistogramFilter::STPFilterBuffer;
+
+namespace {
+
+int failures = 0;
+
+#define CHECK(cond)                                                            \
+	do {                                                                       \
+		if (!(cond)) {                                                         \
+			std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #cond);      \
+			failures++;                                                        \
+		}                                                                      \
+	} while (0)
+
+template<class E, class F>
+bool throws(F f) {
+	try {
+		f();
+	} catch (const E&) {
+		return true;
+	} catch (...) {
+		return false;
+	}
+	return false;
+}
+
+struct uvec2 {
+	unsigned int x, y;
+};
+struct vec2 {
+	float x, y;
+};
+struct NNInfo {
+	uvec2 MapSize, ChunkNearestNeighbour, TotalMapSize;
+};
+
+// STPTestHistogram.cpp:44-57
+const STPSample_t Texture[] = {
+	2, 0, 2, 0, 1, 1, 0, 3, 3, 2, 1, 2,
+	0, 1, 2, 1, 1, 1, 3, 2, 2, 0, 0, 1,
+	0, 1, 0, 2, 1, 3, 1, 1, 1, 2, 1, 0,
+	3, 3, 0, 1, 1, 2, 2, 2, 2, 0, 0, 3,
+	3, 2, 3, 3, 0, 3, 2, 2, 1, 0, 0, 3,
+	2, 0, 0, 1, 2, 0, 2, 2, 0, 2, 0, 3,
+	1, 2, 3, 0, 3, 2, 1, 2, 2, 3, 0, 2,
+	1, 1, 0, 3, 0, 2, 1, 0, 3, 2, 2, 1,
+	2, 2, 0, 1, 0, 2, 0, 0, 0, 0, 1, 1,
+	0, 1, 3, 3, 0, 3, 3, 3, 1, 0, 1, 1,
+	3, 1, 3, 0, 2, 1, 1, 0, 2, 2, 2, 0,
+	2, 0, 1, 1, 2, 3, 1, 2, 3, 2, 0, 1
+};
+const NNInfo Data = { { 4u, 4u }, { 3u, 3u }, { 12u, 12u } };
+
+void histogram_errors() {
+	STPSingleHistogramFilter filter;
+	FiltBuf serial(FiltBuf::STPExecutionType::Serial), parallel(FiltBuf::STPExecutionType::Parallel);
+	CHECK(throws<STPException::STPNumericDomainError>([&] { filter(Texture, Data, serial, 0u); }));
+	CHECK(throws<STPException::STPNumericDomainError>([&] { filter(Texture, Data, parallel, 128u); }));
+	CHECK(throws<STPException::STPNumericDomainError>([&] { filter(Texture, Data, serial, 3u); }));
+}
+
+void histogram_known_answer() {
+	STPSingleHistogramFilter filter;
+	for (auto type : { FiltBuf::STPExecutionType::Serial, FiltBuf::STPExecutionType::Parallel }) {
+		FiltBuf buf(type);
+		for (int again = 0; again < 2; again++) {
+			const STPAlgorithm::STPSingleHistogram h = filter(Texture, Data, buf, 2u);
+			// STPTestHistogram.cpp:77-105
+			const unsigned int trial[] = { 0u, 8u, 15u };
+			const std::pair<STPSample_t, float> expected[] = { { 0, .24f }, { 3, .24f }, { 2, .28f }, { 1, .24f },
+				{ 0, .36f }, { 3, .24f }, { 1, .16f }, { 2, .24f }, { 0, .32f }, { 3, .2f }, { 1, .12f }, { 2, .36f } };
+			for (int t = 0; t < 3; t++) {
+				const unsigned int o = trial[t];
+				int counter = 0;
+				for (unsigned int i = h.HistogramStartOffset[o]; i < h.HistogramStartOffset[o + 1u]; i++, counter++) {
+					const auto [item, weight] = expected[counter + t * 4];
+					CHECK(h.Bin[i].Item == item);
+					CHECK(std::fabs(h.Bin[i].Weight - weight) <= std::numeric_limits<float>::epsilon() * 5.0f * weight);
+				}
+				CHECK(counter == 4);
+			}
+			CHECK(buf.type() == type);
+			const auto [bins, offsets] = buf.size();
+			CHECK(offsets == 17u);
+			CHECK(bins == h.HistogramStartOffset[offsets - 1u]);
+		}
+	}
+}
+
+void permutation() {
+	STPEnvironment::STPSimplexNoiseSetting invalid {};
+	invalid.Distribution = 0u;
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] { STPAlgorithm::STPPermutationGenerator::generate(invalid); }));
+	// STPTestPermutation.cpp:37-41
+	STPEnvironment::STPSimplexNoiseSetting s {};
+	s.Seed = 6666u;
+	s.Distribution = 10u;
+	s.Offset = 6.5 * 3.14159265358979323846 / 180.0;
+	const auto t = STPAlgorithm::STPPermutationGenerator::generate(s);
+	CHECK(t.Permutation.Gradient2DSize == 10u);
+	const double degs[] = { 6.5, 114.5, 258.5 };
+	const int idx[] = { 0, 6, 14 };
+	for (int k = 0; k < 3; k++) {
+		const double a = degs[k] * 3.14159265358979323846 / 180.0;
+		CHECK(std::fabs(t.HostGradient2D[idx[k]] - std::cos(a)) <= 10.0 * std::numeric_limits<float>::epsilon() * std::fabs(std::cos(a)));
+		CHECK(std::fabs(t.HostGradient2D[idx[k] + 1] - std::sin(a)) <= 10.0 * std::numeric_limits<float>::epsilon() * std::fabs(std::sin(a)));
+	}
+	for (int i = 0; i < 256; i++) {
+		CHECK(t.HostPermutation[i] == t.HostPermutation[i + 256]);
+	}
+	const auto same = STPAlgorithm::STPPermutationGenerator::generate(s);
+	CHECK(same.HostPermutation == t.HostPermutation);
+	s.Seed = 183457092u;
+	const auto other = STPAlgorithm::STPPermutationGenerator::generate(s);
+	CHECK(other.HostPermutation != t.HostPermutation);
+}
+
+STPEnvironment::STPRainDropSetting raindrop(unsigned int count) {
+	STPEnvironment::STPRainDropSetting r {};
+	r.Seed = 42u;
+	r.RainDropCount = count;
+	r.Inertia = 0.05f;
+	r.SedimentCapacityFactor = 4.0f;
+	r.minSedimentCapacity = 0.01f;
+	r.initWaterVolume = 1.0f;
+	r.minWaterVolume = stpgb_lifetime_min_water_volume(1.0f, 0.01f, 30u);
+	r.Friction = 0.1f;
+	r.initSpeed = 1.0f;
+	r.ErodeSpeed = 0.3f;
+	r.DepositSpeed = 0.3f;
+	r.EvaporateSpeed = 0.01f;
+	r.Gravity = 4.0f;
+	r.ErosionBrushRadius = 3u;
+	return r;
+}
+
+void generator_errors() {
+	STPEnvironment::STPSimplexNoiseSetting s {};
+	s.Seed = 1u;
+	s.Distribution = 8u;
+	s.Offset = 0.2;
+	std::vector<stpgb_biome_property> table(2, stpgb_biome_property { 128.0f, 4u, 0.5f, 2.0f, 0.0f, 1.0f });
+	auto bad = raindrop(100u);
+	bad.Inertia = 2.0f;
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] {
+		STPHeightfieldGenerator g(uvec2 { 32u, 32u }, uvec2 { 3u, 3u }, uvec2 { 3u, 3u }, bad, s, table, 8u);
+	}));
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] {
+		STPHeightfieldGenerator g(uvec2 { 32u, 32u }, uvec2 { 2u, 3u }, uvec2 { 3u, 3u }, raindrop(100u), s, table, 8u);
+	}));
+}
+
+void generator_round_trip() {
+	const unsigned int S = 64u;
+	STPEnvironment::STPSimplexNoiseSetting s {};
+	s.Seed = 42u;
+	s.Distribution = 8u;
+	s.Offset = 0.2181661565;
+	std::vector<stpgb_biome_property> table = { { 128.0f, 6u, 0.5f, 2.0f, 0.0f, 1.0f }, { 64.0f, 4u, 0.5f, 2.0f, 0.1f, 0.5f } };
+	STPHeightfieldGenerator gen(uvec2 { S, S }, uvec2 { 3u, 3u }, uvec2 { 3u, 3u }, raindrop(20000u), s, table, 16u);
+	std::vector<std::vector<STPSample_t>> biomes(9, std::vector<STPSample_t>(S * S));
+	for (int c = 0; c < 9; c++) {
+		for (unsigned int i = 0; i < S * S; i++) {
+			biomes[c][i] = static_cast<STPSample_t>(((i % S) / 20u + (i / S) / 24u + c) % 2u);
+		}
+	}
+	std::vector<const STPSample_t*> biome_ptr;
+	for (auto& b : biomes) {
+		biome_ptr.push_back(b.data());
+	}
+	std::vector<std::vector<float>> heights(9, std::vector<float>(S * S));
+	std::vector<std::vector<STPHeightFixed_t>> fixed(9, std::vector<STPHeightFixed_t>(S * S));
+	std::vector<float*> hp;
+	std::vector<STPHeightFixed_t*> fp;
+	for (int c = 0; c < 9; c++) {
+		gen.generate(heights[c].data(), biome_ptr.data(), vec2 { float((c % 3) * S), float((c / 3) * S) });
+		hp.push_back(heights[c].data());
+		fp.push_back(fixed[c].data());
+	}
+	double before = 0.0;
+	for (auto& h : heights) {
+		for (float v : h) {
+			CHECK(v >= 0.0f && v <= 1.1f);
+			before += v;
+		}
+	}
+	gen.erode(hp.data(), fp.data());
+	double after = 0.0;
+	bool changed = false;
+	for (int c = 0; c < 9; c++) {
+		for (unsigned int i = 0; i < S * S; i++) {
+			after += heights[c][i];
+			const float cl = heights[c][i] < 0.0f ? 0.0f : (heights[c][i] > 1.0f ? 1.0f : heights[c][i]);
+			CHECK(fixed[c][i] == static_cast<STPHeightFixed_t>(std::rint(cl * 65535.0f)));
+			changed = changed || fixed[c][i] != 0u;
+		}
+	}
+	CHECK(changed);
+	CHECK(after <= before + 1e-3 * before); // sediment only leaves the map
+}
+
+} // namespace
+
+int main(int argc, char** argv) {
+	const bool cpu_only = argc > 1 && std::strcmp(argv[1], "--cpu") == 0;
+	histogram_errors();
+	permutation();
+	generator_errors();
+	if (!cpu_only) {
+		histogram_known_answer();
+		generator_round_trip();
+	}
+	std::printf("%s: %d failure(s)\n", cpu_only ? "cpu" : "all", failures);
+	return failures == 0 ? 0 : 1;
+}
