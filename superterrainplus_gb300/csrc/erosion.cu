@@ -277,7 +277,9 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 // and the K reads of each brush position, are in flight at the same time.
 // Each droplet still reads and updates its own brush points in order.
 template<uint32_t G, uint32_t K>
-__global__ void __launch_bounds__(kErodeBlock) erosion_multi_kernel(const ErosionJob* __restrict__ jobs,
+// 8 resident blocks of 128 threads (64 registers) for two droplets per group:
+// residency, not the few spilled registers, bounds this chain-latency kernel.
+__global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 1) erosion_multi_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single) {
 	static_assert(G >= 4u && K >= 2u, "one corner per lane needs four lanes");
 	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
