@@ -281,6 +281,67 @@ STPGB_API int stpgb_voronoi_biomemap(uint16_t* out, uint32_t pitch, uint32_t wid
 	uint32_t height, int64_t origin_x, int64_t origin_y, uint32_t cell,
 	uint32_t biome_count, uint64_t seed, void* stream);
 
+/* ------------------------------------------------ biome layer chain ----- */
+
+/* Layer kinds of a biome layer chain, the demo layers of SuperTerrain+
+ * (SuperDemo+/World/Layers/):
+ *   CONTINENT  STPContinentLayer.h   first ancestor: Plains 1 in 10, else Ocean
+ *   SCALE      STPScaleLayer.h       x2 zoom; Param STPGB_SCALE_NORMAL / _FUZZY
+ *   LAND       STPLandLayer.h        diagonal-neighbour (STPXCrossLayer) land growth
+ *   ISLAND     STPIslandLayer.h      4-neighbour (STPCrossLayer) islands in open ocean
+ *   VORONOI    STPVoronoiLayer.h     x4 jittered-cell zoom, 2-D (Param 0) */
+enum {
+	STPGB_LAYER_CONTINENT = 1,
+	STPGB_LAYER_SCALE = 2,
+	STPGB_LAYER_LAND = 3,
+	STPGB_LAYER_ISLAND = 4,
+	STPGB_LAYER_VORONOI = 5
+};
+enum { STPGB_SCALE_NORMAL = 0, STPGB_SCALE_FUZZY = 1 };
+enum { STPGB_MAX_LAYERS = 32 };
+
+/* One layer: its kind, kind parameter and salt (the STPLayer constructor's
+ * `salt`, SuperTerrain+/Public/SuperTerrain+/World/Diversity/STPLayer.h). */
+typedef struct stpgb_layer {
+	uint32_t Kind;
+	uint32_t Param;
+	uint64_t Salt;
+} stpgb_layer;
+
+/* Biome IDs the demo layers emit and test (STPBiomeRegistry: Ocean, Plains,
+ * Forest, and the five shallow oceans of STPBiomeRegistry::isShallowOcean:
+ * Ocean, FrozenOcean, WarmOcean, LukewarmOcean, ColdOcean). */
+typedef struct stpgb_layer_biomes {
+	uint16_t Ocean, Plains, Forest;
+	uint16_t ShallowOcean[5];
+} stpgb_layer_biomes;
+
+/* The demo's production line (SuperDemo+/World/Layers/STPAllLayers.cpp:59-105,
+ * the STPLayerChainBuilder pipeline), first ancestor first: 14 layers. */
+STPGB_API int stpgb_layer_chain_demo(stpgb_layer* chain, uint32_t capacity, uint32_t* count);
+
+/* The demo's biome IDs as its parameter loader sets them from Biome.ini
+ * (ocean 0, plains 1, forest 3; registry biomes it does not load keep 0). */
+STPGB_API void stpgb_layer_biomes_demo(stpgb_layer_biomes* ids);
+
+/* Biomemap of a linear layer chain (chain[0] = first ancestor, chain[count-1]
+ * = the layer sampled), the GPU replacement of
+ * STPBiomeFactory::operator()(STPSample_t* biomemap, glm::ivec2 offset)
+ * (SuperTerrain+/Private/World/Diversity/STPBiomeFactory.cpp:24-41):
+ * biomemap[z * pitch + x] = sample(x + offset_x, 0, z + offset_z) for
+ * x < width, z < height.  Device output, asynchronous on `stream`; bit-exact
+ * with the reference's layers.  Voronoi layers use seed std::hash(global_seed),
+ * the identity of libstdc++.  |offset| + size must stay below 2^30. */
+STPGB_API int stpgb_layer_biomemap(const stpgb_layer* chain, uint32_t count, uint64_t global_seed,
+	const stpgb_layer_biomes* ids, uint16_t* biomemap, uint32_t pitch, uint32_t width, uint32_t height,
+	int32_t offset_x, int32_t offset_z, void* stream);
+
+/* Same with a host output array of width x height (synchronous): the drop-in
+ * for a host STPBiomeFactory caller. */
+STPGB_API int stpgb_layer_biomemap_host(const stpgb_layer* chain, uint32_t count, uint64_t global_seed,
+	const stpgb_layer_biomes* ids, uint16_t* biomemap, uint32_t width, uint32_t height, int32_t offset_x,
+	int32_t offset_z);
+
 /* ------------------------------------- plain per-chunk drop-in generator -- */
 
 typedef struct stpgb_generator stpgb_generator;

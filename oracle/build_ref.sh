@@ -1,6 +1,6 @@
 #!/bin/sh
-# Compiles the reference's own host sources for the single histogram filter
-# and the permutation generator, where they lie in the read-only reference
+# Compiles the reference's own host sources for the single histogram filter,
+# the permutation generator and the demo's biome layer chain, where they lie in the read-only reference
 # tree, against the builder-written shims in oracle/refshim, into
 # oracle/_ref/libstpref.so.  Run in the development container only (the
 # reference tree is not present on GPU machines).  The reference's CMake
@@ -27,12 +27,16 @@ ARCHFLAGS=""
 case "$(uname -m)" in x86_64) ARCHFLAGS="-mavx2 -mfma";; esac
 g++ -std=c++20 -O3 $ARCHFLAGS -fPIC -shared -pthread \
 	-DSUPERTERRAINPLUS_EXPORTS -DSUPERALGORITHMPLUS_HOST_EXPORTS \
-	-I"$HERE/refshim" -I"$CORE/Public" -I"$ALG/Host/Public" -I"$CUDA_INC" -I"$CUDA_INC/cccl" \
+	-I"$HERE/refshim" -I"$CORE/Public" -I"$ALG/Host/Public" -I"$REF/SuperDemo+" -I"$CUDA_INC" -I"$CUDA_INC/cccl" \
 	"$OUT/src/STPSingleHistogramFilter.cpp" \
 	"$ALG/Host/Private/STPPermutationGenerator.cpp" \
 	"$ALG/Host/Private/STPAlgorithmEnvironment.cpp" \
 	"$CORE/Private/Utility/STPThreadPool.cpp" \
 	"$CORE/Private/STPException.cpp" \
+	"$CORE/Private/World/Diversity/STPLayer.cpp" \
+	"$CORE/Private/World/Diversity/STPBiomeFactory.cpp" \
+	"$REF/SuperDemo+/World/Layers/STPAllLayers.cpp" \
+	"$REF/SuperDemo+/World/Biomes/STPBiomeRegistry.cpp" \
 	"$HERE/refshim/cudart_host_shim.cpp" \
 	"$HERE/refshim/ref_api.cpp" \
 	-o "$OUT/libstpref.so"

@@ -59,6 +59,13 @@ class Oracle:
         L.orc_droplet_starts.restype = None
         L.orc_voronoi.argtypes = [vp, u32, u32, u32, C.c_int64, C.c_int64, u32, u32, u64]
         L.orc_voronoi.restype = None
+        L.orc_layer_biomemap.argtypes = [vp, u32, u64, vp, vp, u32, u32, i32, i32]
+        L.orc_layer_biomemap.restype = None
+        L.orc_mix_seed.argtypes = [u64, C.c_int64]
+        L.orc_layer_seed.argtypes = [u64, u64]
+        L.orc_local_seed.argtypes = [u64, u64, i32, i32]
+        for name in ("orc_mix_seed", "orc_layer_seed", "orc_local_seed"):
+            getattr(L, name).restype = u64
 
     # -- permutation
     def permutation(self, seed, distribution, offset):
@@ -134,6 +141,29 @@ class Oracle:
         return out
 
 
+    # -- biome layer chain
+    def layer_biomemap(self, chain, ids, seed, width, height, offset):
+        """chain: sequence of (kind, param, salt), first ancestor first; ids: (ocean, plains, forest, 5 x shallow)."""
+        desc = np.array([tuple(c) for c in chain], LAYER_DTYPE)
+        idv = np.ascontiguousarray(ids, np.uint16)
+        assert idv.size == 8
+        out = np.zeros((height, width), np.uint16)
+        self.lib.orc_layer_biomemap(_p(desc), len(desc), seed, _p(idv), _p(out), width, height, offset[0], offset[1])
+        return out
+
+    def mix_seed(self, s, fac):
+        return self.lib.orc_mix_seed(s, fac)
+
+    def layer_seed(self, global_seed, salt):
+        return self.lib.orc_layer_seed(global_seed, salt)
+
+    def local_seed(self, global_seed, salt, x, z):
+        return self.lib.orc_local_seed(global_seed, salt, x, z)
+
+
+LAYER_DTYPE = np.dtype([("Kind", "<u4"), ("Param", "<u4"), ("Salt", "<u8")])
+
+
 class Reference:
     """The reference's own STPSingleHistogramFilter / STPPermutationGenerator, compiled from its sources."""
 
@@ -147,6 +177,14 @@ class Reference:
         self.lib.ref_shf.restype = C.c_int
         self.lib.ref_permutation.argtypes = [u64, u32, C.c_double, vp, vp]
         self.lib.ref_permutation.restype = C.c_int
+        u16, i32 = C.c_uint16, C.c_int32
+        self.lib.ref_layer_biomemap.argtypes = [u64, u16, u16, u16, u16, u32, u32, i32, i32, vp]
+        self.lib.ref_layer_biomemap.restype = C.c_int
+        self.lib.ref_mix_seed.argtypes = [u64, C.c_int64]
+        self.lib.ref_layer_seed.argtypes = [u64, u64]
+        self.lib.ref_local_seed.argtypes = [u64, u64, i32, i32]
+        for name in ("ref_mix_seed", "ref_layer_seed", "ref_local_seed"):
+            getattr(self.lib, name).restype = u64
 
     def shf(self, samplemap, map_size, nn, radius, parallel=False, capacity=None):
         mx, my = map_size
@@ -166,3 +204,20 @@ class Reference:
         grad = np.zeros(2 * max(distribution, 1), np.float32)
         rc = self.lib.ref_permutation(seed, distribution, offset, _p(perm), _p(grad))
         return rc, perm, grad
+
+    def layer_biomemap(self, seed, width, height, offset, ocean=0, plains=1, desert=2, forest=3):
+        """The demo's STPLayerChainBuilder through STPBiomeFactory::operator()."""
+        out = np.zeros((height, width), np.uint16)
+        rc = self.lib.ref_layer_biomemap(seed, ocean, plains, desert, forest, width, height, offset[0], offset[1],
+                                         _p(out))
+        assert rc == 0
+        return out
+
+    def mix_seed(self, s, fac):
+        return self.lib.ref_mix_seed(s, fac)
+
+    def layer_seed(self, global_seed, salt):
+        return self.lib.ref_layer_seed(global_seed, salt)
+
+    def local_seed(self, global_seed, salt, x, z):
+        return self.lib.ref_local_seed(global_seed, salt, x, z)

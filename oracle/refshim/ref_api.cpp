@@ -1,10 +1,14 @@
 // C entry points over the reference's own compiled host classes
-// (STPSingleHistogramFilter, STPPermutationGenerator), used only to pin the
-// oracle restatement and to produce golden fixtures.
+// (STPSingleHistogramFilter, STPPermutationGenerator, STPLayer and the demo's
+// biome layer chain), used only to pin the oracle restatement and to produce
+// golden fixtures.
 #include <SuperAlgorithm+Host/STPSingleHistogramFilter.h>
 #include <SuperAlgorithm+Host/STPPermutationGenerator.h>
 #include <SuperTerrain+/Exception/STPNumericDomainError.h>
 #include <SuperTerrain+/Exception/STPInvalidEnvironment.h>
+#include <SuperTerrain+/World/Diversity/STPLayer.h>
+#include <World/Layers/STPAllLayers.h>
+#include <World/Biomes/STPBiomeRegistry.h>
 
 #include <cstdint>
 #include <cstring>
@@ -68,6 +72,58 @@ int ref_permutation(uint64_t seed, uint32_t distribution, double offset, uint8_t
 	} catch (...) {
 		return 9;
 	}
+}
+
+// The demo's biome layer chain (STPDemo::STPLayerChainBuilder, a
+// STPBiomeFactory) run through STPBiomeFactory::operator()(biomemap, offset).
+// Biome IDs are set the way the demo's parameter loader sets them
+// (SuperDemo+/Helpers/STPTerrainParaLoader.cpp:272-294); biomes it never
+// loads keep ID 0.  Returns 0 ok, 9 error.
+int ref_layer_biomemap(uint64_t seed, uint16_t ocean, uint16_t plains, uint16_t desert, uint16_t forest,
+	uint32_t width, uint32_t height, int32_t offset_x, int32_t offset_z, uint16_t* out) {
+	try {
+		namespace BR = STPDemo::STPBiomeRegistry;
+		BR::Ocean.ID = ocean;
+		BR::Plains.ID = plains;
+		BR::Desert.ID = desert;
+		BR::Forest.ID = forest;
+		STPDemo::STPLayerChainBuilder builder(glm::uvec2(width, height), seed);
+		builder(out, glm::ivec2(offset_x, offset_z));
+		return 0;
+	} catch (...) {
+		return 9;
+	}
+}
+
+// One STPLayer::mixSeed step and STPLayer::seedLayer, exposed through a
+// probe layer, for the local-RNG unit tests.
+namespace {
+class ProbeLayer : public STPDiversity::STPLayer {
+	STPSample_t sample(int, int, int) override {
+		return 0u;
+	}
+
+public:
+	ProbeLayer(uint64_t global, uint64_t salt) : STPLayer(0u, global, salt) {}
+	static uint64_t mix(uint64_t s, int64_t fac) {
+		return STPLayer::mixSeed(s, fac);
+	}
+	uint64_t local(int x, int z) const {
+		return this->seedLocal(x, z);
+	}
+};
+}
+
+uint64_t ref_mix_seed(uint64_t s, int64_t fac) {
+	return ProbeLayer::mix(s, fac);
+}
+
+uint64_t ref_layer_seed(uint64_t global, uint64_t salt) {
+	return ProbeLayer(global, salt).LayerSeed;
+}
+
+uint64_t ref_local_seed(uint64_t global, uint64_t salt, int32_t x, int32_t z) {
+	return ProbeLayer(global, salt).local(x, z);
 }
 
 }

@@ -545,3 +545,287 @@ void orc_voronoi(uint16_t* out, uint32_t pitch, uint32_t width, uint32_t height,
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------------
+ * Biome layer chain: STPBiomeFactory::operator() over a linear chain of the
+ * demo's layers, evaluated per pixel by recursion with one exact memo table
+ * per layer (the reference's per-layer hash cache is pure memoisation).
+ *   local RNG and seeding:  SuperTerrain+/Private/World/Diversity/STPLayer.cpp:96-160
+ *   factory loop:           SuperTerrain+/Private/World/Diversity/STPBiomeFactory.cpp:24-41
+ *   layers:                 SuperDemo+/World/Layers/STP{Continent,Scale,Land,Island,Voronoi}Layer.h,
+ *                           STP{Cross,XCross}Layer.h
+ * Kinds: 1 continent, 2 scale (param 0 normal, 1 fuzzy), 3 land, 4 island,
+ * 5 voronoi (2-D).  ids = {ocean, plains, forest, shallow ocean x5}.
+ * ------------------------------------------------------------------------ */
+#include <unordered_map>
+
+namespace {
+
+inline uint64_t lcg_mix(uint64_t s, uint64_t fac) {
+	// STPLayer::mixSeed: s *= s * A + B; s += fac (64-bit wrap-around)
+	return s * (s * 6364136223846793005ull + 1442695040888963407ull) + fac;
+}
+
+inline uint64_t sext(int v) {
+	return static_cast<uint64_t>(static_cast<int64_t>(v));
+}
+
+uint64_t layer_seed_of(uint64_t global, uint64_t salt) {
+	uint64_t mid = salt;
+	for (int i = 0; i < 3; i++) {
+		mid = lcg_mix(mid, mid);
+	}
+	uint64_t s = global;
+	for (int i = 0; i < 3; i++) {
+		s = lcg_mix(s, mid);
+	}
+	return s;
+}
+
+uint64_t local_seed_of(uint64_t layer_seed, int x, int z) {
+	uint64_t s = lcg_mix(layer_seed, sext(x));
+	s = lcg_mix(s, sext(z));
+	s = lcg_mix(s, sext(x));
+	return lcg_mix(s, sext(z));
+}
+
+struct LocalRng {
+	uint64_t state, layer;
+	uint16_t next(uint32_t range) {
+		const uint16_t v = static_cast<uint16_t>((state >> 24) % range);
+		state = lcg_mix(state, layer);
+		return v;
+	}
+};
+
+struct OrcLayerDesc {
+	uint32_t kind, param;
+	uint64_t salt;
+};
+
+class LayerChainOracle {
+public:
+	LayerChainOracle(const OrcLayerDesc* chain, uint32_t count, uint64_t global, const uint16_t* ids) :
+		desc(chain, chain + count), seed(count), memo(count), voronoi_seed(global) {
+		for (uint32_t i = 0; i < count; i++) {
+			seed[i] = layer_seed_of(global, chain[i].salt);
+		}
+		ocean = ids[0];
+		plains = ids[1];
+		forest = ids[2];
+		std::copy(ids + 3, ids + 8, shallow);
+	}
+
+	uint16_t get(int layer, int x, int z) {
+		if (layer + 1 == static_cast<int>(desc.size())) {
+			return eval(layer, x, z);
+		}
+		const uint64_t key = (static_cast<uint64_t>(static_cast<uint32_t>(x)) << 32) | static_cast<uint32_t>(z);
+		auto& m = memo[layer];
+		const auto it = m.find(key);
+		if (it != m.end()) {
+			return it->second;
+		}
+		const uint16_t v = eval(layer, x, z);
+		m.emplace(key, v);
+		return v;
+	}
+
+private:
+	std::vector<OrcLayerDesc> desc;
+	std::vector<uint64_t> seed;
+	std::vector<std::unordered_map<uint64_t, uint16_t>> memo;
+	uint64_t voronoi_seed;
+	uint16_t ocean, plains, forest, shallow[5];
+
+	bool so(uint16_t v) const {
+		for (uint16_t s : shallow) {
+			if (v == s) {
+				return true;
+			}
+		}
+		return false;
+	}
+
+	LocalRng rng(int layer, int x, int z) const {
+		return LocalRng { local_seed_of(seed[layer], x, z), seed[layer] };
+	}
+
+	uint16_t eval(int layer, int x, int z) {
+		const int up = layer - 1;
+		switch (desc[layer].kind) {
+		case 1: {
+			LocalRng r = rng(layer, x, z);
+			return r.next(10u) == 0u ? plains : ocean;
+		}
+		case 2: {
+			const uint16_t c = get(up, x >> 1, z >> 1);
+			LocalRng r = rng(layer, x & -2, z & -2);
+			const int odd_x = x & 1, odd_z = z & 1;
+			if (!odd_x && !odd_z) {
+				return c;
+			}
+			const uint16_t below = get(up, x >> 1, (z + 1) >> 1);
+			const uint16_t pick_z = r.next(2u) == 0u ? c : below;
+			if (!odd_x) {
+				return pick_z;
+			}
+			const uint16_t right = get(up, (x + 1) >> 1, z >> 1);
+			const uint16_t pick_x = r.next(2u) == 0u ? c : right;
+			if (!odd_z) {
+				return pick_x;
+			}
+			const uint16_t diag = get(up, (x + 1) >> 1, (z + 1) >> 1);
+			return scale_corner(c, right, below, diag, r, desc[layer].param != 0u);
+		}
+		case 3: {
+			const uint16_t c = get(up, x, z), ne = get(up, x + 1, z - 1), se = get(up, x + 1, z + 1),
+				sw = get(up, x - 1, z + 1), nw = get(up, x - 1, z - 1);
+			LocalRng r = rng(layer, x, z);
+			const bool all_so = so(sw) && so(se) && so(ne) && so(nw);
+			const bool none_so = !so(sw) && !so(se) && !so(ne) && !so(nw);
+			if (!so(c) || all_so) {
+				if (so(c) || none_so || r.next(5u) != 0u) {
+					return c;
+				}
+				const uint16_t order[4] = { nw, sw, ne, se };
+				for (uint16_t n : order) {
+					if (so(n)) {
+						return c == forest ? forest : n;
+					}
+				}
+				return c;
+			}
+			uint32_t tries = 1u;
+			uint16_t chosen = 1u;
+			const uint16_t order[4] = { nw, ne, sw, se };
+			for (int k = 0; k < 4; k++) {
+				if (!so(order[k])) {
+					const uint32_t range = tries;
+					if (k < 3) {
+						tries++;
+					}
+					if (r.next(range) == 0u) {
+						chosen = order[k];
+					}
+				}
+			}
+			if (r.next(3u) == 0u) {
+				return chosen;
+			}
+			return chosen == forest ? forest : c;
+		}
+		case 4: {
+			const uint16_t c = get(up, x, z), n = get(up, x, z - 1), e = get(up, x + 1, z), s = get(up, x, z + 1),
+				w = get(up, x - 1, z);
+			LocalRng r = rng(layer, x, z);
+			return so(c) && so(n) && so(e) && so(s) && so(w) && r.next(2u) == 0u ? plains : c;
+		}
+		case 5:
+			return voronoi(up, x, z);
+		default:
+			return 0u;
+		}
+	}
+
+	static uint16_t scale_corner(uint16_t c, uint16_t e, uint16_t s, uint16_t se, LocalRng& r, bool fuzzy) {
+		const uint32_t k = r.next(4u);
+		const uint16_t any = k == 0u ? c : k == 1u ? e : k == 2u ? s : se;
+		if (fuzzy) {
+			return any;
+		}
+		if (e == s && e == se) {
+			return e;
+		}
+		if (c == e && (c == se || s != se)) {
+			return c;
+		}
+		if (c == s && (c == se || e != se)) {
+			return c;
+		}
+		if (c == se && e != s) {
+			return c;
+		}
+		if (e == s && c != se) {
+			return e;
+		}
+		if (e == se && c != s) {
+			return e;
+		}
+		if (s == se && c != e) {
+			return s;
+		}
+		return any;
+	}
+
+	static double jitter(uint64_t h) {
+		const double u = static_cast<double>(static_cast<uint32_t>((h >> 24) % 1024u)) / 1024.0;
+		return (u - 0.5) * 0.9;
+	}
+
+	// Squared distance from the pixel to the jittered point of cell (cx,cy,cz),
+	// summed z, y, x as the reference does (STPVoronoiLayer.h sqrtDist).
+	double cell_distance(int cx, int cy, int cz, double fx, double fy, double fz) const {
+		uint64_t h = voronoi_seed;
+		const int axis[6] = { cx, cy, cz, cx, cy, cz };
+		for (int a : axis) {
+			h = lcg_mix(h, sext(a));
+		}
+		const double jx = jitter(h);
+		h = lcg_mix(h, voronoi_seed);
+		const double jy = jitter(h);
+		h = lcg_mix(h, voronoi_seed);
+		const double jz = jitter(h);
+		const double tz = fz + jz, ty = fy + jy, tx = fx + jx;
+		return tz * tz + ty * ty + tx * tx;
+	}
+
+	uint16_t voronoi(int up, int x, int z) {
+		const int bx = x - 2, by = -2, bz = z - 2;
+		const int cx = bx >> 2, cy = by >> 2, cz = bz >> 2;
+		const double fx = (bx & 3) / 4.0, fy = (by & 3) / 4.0, fz = (bz & 3) / 4.0;
+		int best = 0;
+		double best_d = 0.0;
+		for (int c = 0; c < 8; c++) {
+			const int hx = (c >> 2) & 1, hy = (c >> 1) & 1, hz = c & 1;
+			const double d = cell_distance(cx + hx, cy + hy, cz + hz, fx - hx, fy - hy, fz - hz);
+			if (c == 0 || d < best_d) {
+				best = c;
+				best_d = d;
+			}
+		}
+		return get(up, cx + ((best >> 2) & 1), cz + (best & 1));
+	}
+};
+
+} // namespace
+
+extern "C" {
+
+uint64_t orc_mix_seed(uint64_t s, int64_t fac) {
+	return lcg_mix(s, static_cast<uint64_t>(fac));
+}
+
+uint64_t orc_layer_seed(uint64_t global, uint64_t salt) {
+	return layer_seed_of(global, salt);
+}
+
+uint64_t orc_local_seed(uint64_t global, uint64_t salt, int32_t x, int32_t z) {
+	return local_seed_of(layer_seed_of(global, salt), x, z);
+}
+
+/* chain: count x {uint32 kind, uint32 param, uint64 salt}, first ancestor
+ * first; ids: ocean, plains, forest, shallow ocean x5.  Writes
+ * out[z * width + x] for the world rectangle starting at (offset_x, offset_z). */
+void orc_layer_biomemap(const void* chain, uint32_t count, uint64_t global_seed, const uint16_t* ids, uint16_t* out,
+	uint32_t width, uint32_t height, int32_t offset_x, int32_t offset_z) {
+	LayerChainOracle o(static_cast<const OrcLayerDesc*>(chain), count, global_seed, ids);
+	for (uint32_t z = 0u; z < height; z++) {
+		for (uint32_t x = 0u; x < width; x++) {
+			out[static_cast<size_t>(z) * width + x] = o.get(static_cast<int>(count) - 1,
+				static_cast<int>(x) + offset_x, static_cast<int>(z) + offset_z);
+		}
+	}
+}
+
+} // extern "C"

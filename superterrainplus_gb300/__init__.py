@@ -6,8 +6,11 @@ the C ABI of libstpgb.so (include/stpgb.h):
 * STPPermutationGenerator.generate        (SuperAlgorithm+Host/STPPermutationGenerator.h:50)
 * STPSingleHistogramFilter / STPFilterBuffer (SuperAlgorithm+Host/STPSingleHistogramFilter.h:36-190)
 * STPHeightfieldGenerator.generate / erode (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:145,159)
+* STPBiomeFactory over the demo's layer chain (STPLayerChainBuilder,
+  SuperDemo+/World/Layers/STPAllLayers.h; SuperTerrain+/World/Diversity/STPBiomeFactory.h:19-63)
 * kernel-level calls on device buffers (shf_filter, multibiome_heightmap,
-  hydraulic_erosion, format_heightmap, droplet_starts, voronoi_biomemap)
+  hydraulic_erosion, format_heightmap, droplet_starts, voronoi_biomemap,
+  layer_biomemap)
 
 Device buffers are torch CUDA tensors (PyTorch is only the allocator and the
 stream provider here); the compute runs in the CUDA kernels of libstpgb.so.
@@ -16,8 +19,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import (BiomeProperty, ChunkSetting, NNInfo, Permutation, RaindropSetting, SimplexSetting,
-                    STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
+from ._capi import (STPGB_MAX_LAYERS, BiomeProperty, ChunkSetting, Layer, LayerBiomes, NNInfo, Permutation,
+                    RaindropSetting, SimplexSetting, STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
                     STPNumericDomainError, STPTimeout, check, lib)
 
 __all__ = [
@@ -25,7 +28,8 @@ __all__ = [
     "STPCapacityError", "STPCUDAError", "STPException", "STPInsufficientMemory", "STPInvalidEnvironment",
     "STPNumericDomainError", "STPTimeout", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
-    "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch",
+    "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch", "Layer", "LayerBiomes",
+    "layer_chain_demo", "STPLayerChainBuilder",
 ]
 
 BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
@@ -66,6 +70,51 @@ def lifetime_min_water_volume(init_water_volume, evaporate_speed, lifetime):
 
 
 # ------------------------------------------------- single histogram filter
+
+
+# ------------------------------------------------------ biome layer chain
+
+
+def layer_chain_demo():
+    """The demo's production line (SuperDemo+/World/Layers/STPAllLayers.cpp:59-105), first
+    ancestor first, and the demo's biome IDs: (ctypes Layer array, LayerBiomes)."""
+    buf = (Layer * STPGB_MAX_LAYERS)()
+    n = C.c_uint32(0)
+    check(lib().stpgb_layer_chain_demo(buf, STPGB_MAX_LAYERS, C.byref(n)))
+    chain = (Layer * n.value)(*buf[:n.value])
+    ids = LayerBiomes()
+    lib().stpgb_layer_biomes_demo(C.byref(ids))
+    return chain, ids
+
+
+def _layer_array(chain):
+    if isinstance(chain, C.Array):
+        return chain
+    return (Layer * len(chain))(*[c if isinstance(c, Layer) else Layer(*c) for c in chain])
+
+
+class STPLayerChainBuilder:
+    """STPBiomeFactory with the demo's layer chain (STPDemo::STPLayerChainBuilder,
+    SuperDemo+/World/Layers/STPAllLayers.h): `factory(biomemap, offset)` fills a
+    uint16 host array of `dimension` (x, y) with the biomes of world pixels
+    offset + (x, z), as STPBiomeFactory::operator() (STPBiomeFactory.cpp:24-41).
+    The chain runs on the GPU; `chain` / `ids` replace the demo's layers and IDs."""
+
+    def __init__(self, dimension, global_seed, chain=None, ids=None):
+        if dimension[0] <= 0 or dimension[1] <= 0:
+            raise STPNumericDomainError("Biomemap should have strictly positive dimension in both vector components")
+        self.BiomeDimension = (int(dimension[0]), int(dimension[1]))
+        self.GlobalSeed = int(global_seed)
+        demo_chain, demo_ids = layer_chain_demo()
+        self.chain = _layer_array(chain) if chain is not None else demo_chain
+        self.ids = ids if ids is not None else demo_ids
+
+    def __call__(self, biomemap, offset):
+        w, h = self.BiomeDimension
+        if biomemap.dtype != np.uint16 or biomemap.size != w * h or not biomemap.flags.c_contiguous:
+            raise STPNumericDomainError("biomemap must be a contiguous uint16 array of the factory's dimension")
+        check(lib().stpgb_layer_biomemap_host(self.chain, len(self.chain), self.GlobalSeed, C.byref(self.ids),
+                                              _p(biomemap), w, h, int(offset[0]), int(offset[1])))
 
 
 class STPFilterBuffer:
@@ -318,6 +367,11 @@ class DeviceOps:
     def format_heightmap(self, src, dst, map_x, map_y):
         check(lib().stpgb_format_heightmap(C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()), map_x, map_y,
                                            self._stream()))
+
+    def layer_biomemap(self, chain, ids, global_seed, out, pitch, width, height, offset):
+        chain = _layer_array(chain)
+        check(lib().stpgb_layer_biomemap(chain, len(chain), global_seed, C.byref(ids), C.c_void_p(out.data_ptr()),
+                                         pitch, width, height, int(offset[0]), int(offset[1]), self._stream()))
 
     def voronoi_biomemap(self, out, pitch, width, height, origin, cell, biome_count, seed):
         check(lib().stpgb_voronoi_biomemap(C.c_void_p(out.data_ptr()), pitch, width, height, origin[0], origin[1],

@@ -118,6 +118,18 @@ class ServerStats(C.Structure):
                 ("PoolBytesUsed", C.c_uint64), ("ResidentChunks", C.c_uint64)]
 
 
+class Layer(C.Structure):
+    _fields_ = [("Kind", u32), ("Param", u32), ("Salt", u64)]
+
+
+class LayerBiomes(C.Structure):
+    _fields_ = [("Ocean", u16), ("Plains", u16), ("Forest", u16), ("ShallowOcean", u16 * 5)]
+
+
+STPGB_LAYER_CONTINENT, STPGB_LAYER_SCALE, STPGB_LAYER_LAND, STPGB_LAYER_ISLAND, STPGB_LAYER_VORONOI = range(1, 6)
+STPGB_SCALE_NORMAL, STPGB_SCALE_FUZZY = 0, 1
+STPGB_MAX_LAYERS = 32
+
 STPGB_BATCH_GRAPH = 1
 STPGB_BATCH_AUTOTUNE = 2
 
@@ -144,6 +156,10 @@ PROTOTYPES = {
                                              u32, vp, vp, u32, u32, u32, vp]),
     "stpgb_format_heightmap": (C.c_int, [vp, vp, u32, u32, vp]),
     "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
+    "stpgb_layer_chain_demo": (C.c_int, [vp, u32, C.POINTER(u32)]),
+    "stpgb_layer_biomes_demo": (None, [C.POINTER(LayerBiomes)]),
+    "stpgb_layer_biomemap": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, u32, i32, i32, vp]),
+    "stpgb_layer_biomemap_host": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, i32, i32]),
     "stpgb_generator_create": (C.c_int, [C.POINTER(ChunkSetting), C.POINTER(RaindropSetting),
                                          C.POINTER(SimplexSetting), vp, u32, u32, C.POINTER(vp)]),
     "stpgb_generator_destroy": (C.c_int, [vp]),

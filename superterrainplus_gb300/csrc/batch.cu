@@ -237,8 +237,8 @@ struct stpgb_batch {
 namespace {
 
 int check_request(const stpgb_batch_request& r) {
-	if (r.MapSize == 0u || (r.MapSize & 7u) != 0u) {
-		return inval("stpgb_batch: MapSize must be a positive multiple of 8");
+	if (r.MapSize == 0u || (r.MapSize & 7u) != 0u || r.MapSize > 16384u) {
+		return inval("stpgb_batch: MapSize must be a positive multiple of 8, at most 16384");
 	}
 	if (r.InterpolationRadius == 0u || (r.InterpolationRadius & 1u) || r.InterpolationRadius > r.MapSize) {
 		return inval("stpgb_batch: radius must be positive, even and at most MapSize");

@@ -434,8 +434,13 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 1) erosion_multi_ke
 #pragma unroll
 			for (uint32_t q = k + 1u; q < K; q++) {
 				if (erode[k] && erode[q]) {
-					const int32_t dx = static_cast<int32_t>(mi[k] % pitch) - static_cast<int32_t>(mi[q] % pitch);
-					const int32_t dy = static_cast<int32_t>(mi[k] / pitch) - static_cast<int32_t>(mi[q] / pitch);
+					// 32-bit division (the launch checks that a map holds
+					// fewer than 2^32 cells): a 64-bit division by a run-time
+					// divisor runs on the narrow FP64 pipe
+					const uint32_t a = static_cast<uint32_t>(mi[k]), b = static_cast<uint32_t>(mi[q]);
+					const uint32_t p32 = static_cast<uint32_t>(pitch);
+					const int32_t dx = static_cast<int32_t>(a % p32) - static_cast<int32_t>(b % p32);
+					const int32_t dy = static_cast<int32_t>(a / p32) - static_cast<int32_t>(b / p32);
 					serial = serial || (abs(dx) <= reach && abs(dy) <= reach);
 				}
 			}
@@ -732,6 +737,9 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	}
 	if (brush_size > 8192u) {
 		return inval("stpgb_hydraulic_erosion: brush larger than 8192 points");
+	}
+	if (static_cast<uint64_t>(dx) * dy >= (uint64_t(1) << 32)) {
+		return inval("stpgb_hydraulic_erosion: the map must hold fewer than 2^32 cells");
 	}
 	ErosionJob job;
 	job.map = heightmap;

@@ -705,10 +705,11 @@ int stpgb_server_submit(stpgb_server* sv, const stpgb_serve_request* req, uint64
 	if (!sv || !req) {
 		return inval("stpgb_server_submit: null argument");
 	}
-	if (req->MapSize == 0u || (req->MapSize & 7u) || req->InterpolationRadius == 0u || (req->InterpolationRadius & 1u)
-		|| req->InterpolationRadius > req->MapSize || req->BrushRadius == 0u || !(req->DropletsPerPixel >= 0.0f)) {
-		return inval("stpgb_server_submit: MapSize must be a multiple of 8, radius positive, even and <= MapSize, "
-					 "brush positive");
+	if (req->MapSize == 0u || (req->MapSize & 7u) || req->MapSize > 16384u || req->InterpolationRadius == 0u
+		|| (req->InterpolationRadius & 1u) || req->InterpolationRadius > req->MapSize || req->BrushRadius == 0u
+		|| !(req->DropletsPerPixel >= 0.0f)) {
+		return inval("stpgb_server_submit: MapSize must be a multiple of 8 and at most 16384, radius positive, even "
+					 "and <= MapSize, brush positive");
 	}
 	Request r;
 	r.req = *req;

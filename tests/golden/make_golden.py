@@ -15,6 +15,13 @@ Fixtures:
   shf_digests.json     SHA-256 of the reference output for large cases
                        (512x512 chunk, r = 32; 256x256, r = 16, ...)
   permutation.npz      reference permutation/gradient tables for several seeds
+  layer_biomemap.npz   the demo's biome layer chain (STPLayerChainBuilder through
+                       STPBiomeFactory::operator()) for several seeds, offsets and
+                       biome-ID assignments, stored in full; STPLayer seed
+                       arithmetic (mixSeed, seedLayer, seedLocal) known answers
+  layer_digests.json   SHA-256 of the layer chain's output for large maps
+
+`python tests/golden/make_golden.py layers` rewrites only the layer fixtures.
 """
 import hashlib
 import json
@@ -67,6 +74,58 @@ PERM_CASES = [(6666, 10, float(np.radians(6.5))), (42, 8, 0.2181661565), (183457
               (2**63 + 12345, 16, 6.0)]
 
 
+# (seed, width, height, offset_x, offset_z, (ocean, plains, desert, forest))
+LAYER_CASES = [
+    (42, 256, 256, 0, 0, (0, 1, 2, 3)),
+    (7, 300, 200, -5000, 3000, (0, 1, 2, 3)),
+    (2**63 + 12345, 128, 512, -70000, -90000, (0, 1, 2, 3)),
+    (123, 77, 333, -3, -7, (0, 1, 2, 3)),
+    (11, 1024, 1024, -512, -512, (0, 1, 2, 3)),
+    (99, 640, 480, 2048, -4096, (4, 7, 0, 4)),
+    (5, 600, 600, -100000, 100, (1, 0, 2, 1)),
+    (0, 512, 512, 1000000, -2000000, (0, 1, 2, 3)),
+    (3, 700, 700, -300, -300, (5, 2, 9, 1)),
+]
+LAYER_LARGE_CASES = [
+    (7, 2048, 2048, -1024, -1024, (0, 1, 2, 3)),
+    (2024, 1536, 1536, -768, 4096, (0, 1, 2, 3)),
+]
+
+
+def layer_digest(out):
+    return hashlib.sha256(np.ascontiguousarray(out, np.uint16).tobytes()).hexdigest()
+
+
+def make_layers(ref):
+    out = {}
+    for i, (seed, w, h, ox, oz, ids) in enumerate(LAYER_CASES):
+        m = ref.layer_biomemap(seed, w, h, (ox, oz), *ids)
+        out[f"l{i}_meta"] = np.array([w, h, ox, oz], np.int64)
+        out[f"l{i}_seed"] = np.array(seed, np.uint64)
+        out[f"l{i}_ids"] = np.array(ids, np.uint16)
+        out[f"l{i}_map"] = m
+    out["count"] = np.array(len(LAYER_CASES))
+    rng = np.random.default_rng(2024)
+    kat = []
+    for _ in range(64):
+        s = int(rng.integers(0, 2**64, dtype=np.uint64))
+        fac = int(rng.integers(-2**63, 2**63 - 1))
+        salt = int(rng.integers(0, 2**63))
+        x, z = (int(v) for v in rng.integers(-2**31, 2**31 - 1, 2))
+        kat.append((s, fac, salt, x, z, ref.mix_seed(s, fac), ref.layer_seed(s, salt), ref.local_seed(s, salt, x, z)))
+    out["seed_kat"] = np.array([[k[0], k[1] & (2**64 - 1), k[2], k[3] & (2**64 - 1), k[4] & (2**64 - 1), k[5], k[6],
+                                 k[7]] for k in kat], np.uint64)
+    np.savez_compressed(os.path.join(HERE, "layer_biomemap.npz"), **out)
+    digests = []
+    for seed, w, h, ox, oz, ids in LAYER_LARGE_CASES:
+        m = ref.layer_biomemap(seed, w, h, (ox, oz), *ids)
+        values, counts = np.unique(m, return_counts=True)
+        digests.append({"seed": seed, "size": [w, h], "offset": [ox, oz], "ids": list(ids), "sha256": layer_digest(m),
+                        "histogram": {int(v): int(c) for v, c in zip(values, counts)}})
+    with open(os.path.join(HERE, "layer_digests.json"), "w") as f:
+        json.dump(digests, f, indent=1)
+
+
 def make_samplemap(kind, mx, my, nx, ny, param, seed, oracle):
     w, h = mx * nx, my * ny
     if kind == "random":
@@ -87,6 +146,10 @@ def digest(offsets, bins):
 
 def main():
     orc, ref = Oracle(), Reference()
+    make_layers(ref)
+    if sys.argv[1:] == ["layers"]:
+        print("layer fixtures written to", HERE)
+        return
     rc, off, bins = ref.shf(KAT_TEXTURE, (4, 4), (3, 3), 2)
     assert rc == 0
     np.savez_compressed(os.path.join(HERE, "shf_kat.npz"), texture=KAT_TEXTURE, offsets=off,
