@@ -369,7 +369,9 @@ def run_ours(args):
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
             "serving": serving,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
-                         "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}": v for (a, b), v in tune_ms.items()}},
+                         "erosion_brush_rows": bool(lanes[2]),
+                         "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
+                                                            for (a, b, r), v in tune_ms.items()}},
             "gpu_launches": 7 * args.steps,
         }
         print(json.dumps(line), flush=True)

@@ -246,18 +246,37 @@ STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
 	double* residual_sediment, uint32_t* status, void* stream);
 
 /* stpgb_hydraulic_erosion with an explicit number of lanes carrying one
- * droplet (1, 2, 4, 8, 16 or 32; 0 = default), droplets per lane group (1, or
- * 2 / 4 with 4, 8 or 16 lanes: the group advances its droplets together so
- * their memory round trips overlap) and flags.  Each lane erodes its share of
- * the brush in the reference's order (STPRainDrop.cu:146-157): read a cell,
- * subtract min(cell, w), next point; one lane per droplet is the reference
- * kernel itself.  The plain entry point uses the largest power of two up to
- * 8 that leaves each lane at least four brush points (below that, densely
- * packed droplets read a step's cells nearly together and the map can run
- * away).  STPGB_EROSION_EXACT_CLAMP erodes each point by compare-and-swap
- * instead, so racing droplets never remove more than a cell holds (closer to
- * the serial algorithm, slower).  No counterpart in the reference. */
-enum { STPGB_EROSION_EXACT_CLAMP = 1 };
+ * droplet (1, 2, 4, 8, 16 or 32; 0 = the default, see stpgb_erosion_choice),
+ * droplets per lane group (1, or 2 / 4 with 4, 8 or 16 lanes, or 2 with 2 or
+ * 4 brush-row lanes: the group advances its droplets together so their
+ * memory round trips overlap) and flags.  Point by point, each lane erodes its
+ * share of the brush in the reference's order (STPRainDrop.cu:146-157): read
+ * a cell, subtract min(cell, w), next point; one lane per droplet is the
+ * reference kernel itself.  With 2 or 4 lanes and 1 or 2 droplets per group,
+ * on a 16-byte aligned map whose width is a multiple of four, a lane takes
+ * whole brush rows (runs of consecutive cells) and updates them in aligned
+ * 16-byte blocks instead: one vector read, then one vector reduction
+ * subtracting min(cell, w) from the row's cells (-0.0 elsewhere); a droplet's
+ * cells are distinct, so per droplet this is the same read-then-subtract,
+ * with a quarter of the memory operations.  The default keeps four points
+ * (or four 16-byte blocks) per lane: below that a step's reads happen nearly
+ * together and densely packed droplets can run the map away.
+ * STPGB_EROSION_POINTWISE keeps the point-by-point kernels.
+ * STPGB_EROSION_EXACT_CLAMP erodes each point by compare-and-swap instead, so
+ * racing droplets never remove more than a cell holds (closer to the serial
+ * algorithm, slower).  No counterpart in the reference. */
+enum { STPGB_EROSION_EXACT_CLAMP = 1, STPGB_EROSION_POINTWISE = 2 };
+
+/* The kernel variant the default (lanes_per_droplet = 0) of
+ * stpgb_hydraulic_erosion_ex takes for a brush of `brush_radius` and
+ * `droplets` over `area` pixels (the chunk the starts cover).  Racing
+ * droplets packed densely enough dig channels without bound, and the faster
+ * a droplet's brush update completes, the lower that density: up to 3
+ * droplets per pixel brush rows are taken (lanes keeping four 16-byte blocks
+ * each; point by point for brushes too small for that), beyond it one lane
+ * per droplet (the reference kernel).  No counterpart in the reference. */
+STPGB_API int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area,
+	uint32_t* lanes_per_droplet, uint32_t* vector_rows);
 STPGB_API int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn,
 	const stpgb_raindrop_setting* setting, const float* starts_xy, uint32_t count,
 	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,
@@ -456,11 +475,13 @@ STPGB_API int stpgb_batch_run_stage(stpgb_batch* batch, uint32_t stage, void* st
  * re-captures the graph of a batch created with STPGB_BATCH_GRAPH. */
 STPGB_API int stpgb_batch_tune(stpgb_batch* batch);
 
-/* Erosion lanes per droplet and droplets per lane group in use, and the
- * autotuner's erosion time in ms per candidate: 18 floats, index
- * 3*log2(lanes) + {0, 1, 2} for 1, 2, 4 droplets per group (0 = not tried). */
+/* Erosion lanes per droplet, droplets per lane group and brush update (1 =
+ * brush rows in 16-byte blocks, 0 = point by point) in use, and the
+ * autotuner's erosion time in ms per candidate: 36 floats, index
+ * 18*rows + 3*log2(lanes) + {0, 1, 2} for 1, 2, 4 droplets per group
+ * (0 = not tried).  Any output pointer may be NULL. */
 STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_droplet,
-	uint32_t* droplets_per_group, float* erosion_ms);
+	uint32_t* droplets_per_group, uint32_t* vector_rows, float* erosion_ms);
 
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */

@@ -292,11 +292,14 @@ class Batch:
         check(lib().stpgb_batch_tune(self._h))
 
     def tuning(self):
-        """((lanes per droplet, droplets per group) in use, {(lanes, droplets): autotuner erosion ms})."""
-        lanes, dpg = C.c_uint32(0), C.c_uint32(0)
-        ms = (C.c_float * 18)()
-        check(lib().stpgb_batch_tuning(self._h, C.byref(lanes), C.byref(dpg), ms))
-        return (lanes.value, dpg.value), {(1 << (i // 3), 1 << (i % 3)): ms[i] for i in range(18) if ms[i] > 0}
+        """((lanes per droplet, droplets per group, brush rows) in use,
+        {(lanes, droplets, rows): autotuner erosion ms}); rows is 1 for the
+        brush updated in 16-byte row blocks, 0 for point by point."""
+        lanes, dpg, rows = C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
+        ms = (C.c_float * 36)()
+        check(lib().stpgb_batch_tuning(self._h, C.byref(lanes), C.byref(dpg), C.byref(rows), ms))
+        return ((lanes.value, dpg.value, rows.value),
+                {(1 << ((i % 18) // 3), 1 << (i % 3), i // 18): ms[i] for i in range(36) if ms[i] > 0})
 
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)
@@ -355,14 +358,15 @@ class DeviceOps:
                                          self._stream()))
 
     def hydraulic_erosion(self, heightmap, map_size, nn, setting, starts, count, brush_index, brush_weight,
-                          residual=None, status=None, lanes=0, exact_clamp=False, droplets_per_group=1):
+                          residual=None, status=None, lanes=0, exact_clamp=False, droplets_per_group=1,
+                          pointwise=False):
         info = NNInfo.make(map_size, nn)
         check(lib().stpgb_hydraulic_erosion_ex(
             C.c_void_p(heightmap.data_ptr()), C.byref(info), C.byref(setting), C.c_void_p(starts.data_ptr()), count,
             C.c_void_p(brush_index.data_ptr()), C.c_void_p(brush_weight.data_ptr()), brush_index.numel(),
             C.c_void_p(residual.data_ptr() if residual is not None else 0),
-            C.c_void_p(status.data_ptr() if status is not None else 0), lanes, droplets_per_group, int(exact_clamp),
-            self._stream()), env_error=True)
+            C.c_void_p(status.data_ptr() if status is not None else 0), lanes, droplets_per_group,
+            int(exact_clamp) | (2 if pointwise else 0), self._stream()), env_error=True)
 
     def format_heightmap(self, src, dst, map_x, map_y):
         check(lib().stpgb_format_heightmap(C.c_void_p(src.data_ptr()), C.c_void_p(dst.data_ptr()), map_x, map_y,

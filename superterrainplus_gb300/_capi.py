@@ -155,6 +155,7 @@ PROTOTYPES = {
     "stpgb_hydraulic_erosion_ex": (C.c_int, [vp, C.POINTER(NNInfo), C.POINTER(RaindropSetting), vp, u32, vp, vp,
                                              u32, vp, vp, u32, u32, u32, vp]),
     "stpgb_format_heightmap": (C.c_int, [vp, vp, u32, u32, vp]),
+    "stpgb_erosion_choice": (C.c_int, [u32, u32, u32, C.POINTER(u32), C.POINTER(u32)]),
     "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
     "stpgb_layer_chain_demo": (C.c_int, [vp, u32, C.POINTER(u32)]),
     "stpgb_layer_biomes_demo": (None, [C.POINTER(LayerBiomes)]),
@@ -178,7 +179,7 @@ PROTOTYPES = {
     "stpgb_batch_download": (C.c_int, [vp, vp, vp, vp, vp]),
     "stpgb_batch_status": (C.c_int, [vp, vp]),
     "stpgb_batch_run_stage": (C.c_int, [vp, u32, vp]),
-    "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), vp]),
+    "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32), vp]),
     "stpgb_batch_tune": (C.c_int, [vp]),
     "stpgb_batch_download_inputs": (C.c_int, [vp, vp, vp, vp]),
     "stpgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(RaindropSetting), C.POINTER(SimplexSetting),

@@ -75,8 +75,16 @@ struct stpgb_batch {
 	uint32_t lanes = 8u;       // lanes per droplet of the erosion kernel
 	uint32_t lane_limit = 32u; // max_lanes() of the smallest brush in the batch
 	uint32_t dpg = 1u;         // droplets per lane group
-	// autotuner's erosion time per candidate, [lanes 1..32][droplets 1, 2, 4] (0 = not tried)
-	float tune_ms[18] = {};
+	// brush rows in 16-byte blocks (every merged map of a batch is 256-byte
+	// aligned with a pitch of 3 * MapSize, a multiple of 24 floats), with at
+	// most rows_limit lanes: rows_max_lanes() of the smallest brush
+	bool rows = true;
+	uint32_t rows_limit = 4u;
+	// largest droplet density (droplets per centre-chunk pixel) of the batch;
+	// the autotuner only tries the variants stable at this density
+	double density = 0.0;
+	// autotuner's erosion time per candidate, [rows 0, 1][lanes 1..32][droplets 1, 2, 4] (0 = not tried)
+	float tune_ms[36] = {};
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	bool use_graph = false;
@@ -149,7 +157,7 @@ struct stpgb_batch {
 				table, biome_count, s);
 		case 2u:
 			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
-				false, dpg);
+				false, dpg, rows);
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -169,17 +177,27 @@ struct stpgb_batch {
 		int rc = stage(0u, s);
 		float best = 0.0f;
 		uint32_t best_lanes = lanes, best_dpg = dpg;
+		bool best_rows = rows;
 		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
 		const uint32_t dcands[3] = { 1u, 2u, 4u };
-		for (int c = 0; c < 18 && rc == STPGB_OK; c++) {
-			const uint32_t cl = cands[c / 3], cd = dcands[c % 3];
+		for (int c = 0; c < 36 && rc == STPGB_OK; c++) {
+			const bool cr = c >= 18;
+			const uint32_t cl = cands[(c % 18) / 3], cd = dcands[c % 3];
 			// lane counts above the brush limit, and several droplets per group
-			// below four lanes or above sixteen, are not candidates
-			if (cl > lane_limit || (cd > 1u && (cl < 4u || cl > 16u))) {
+			// below four lanes or above sixteen, are not candidates; brush rows
+			// run with 2 or 4 lanes (up to rows_limit) and 1 or 2 droplets
+			if (!cr && (cl > lane_limit || (cd > 1u && (cl < 4u || cl > 16u)))) {
+				continue;
+			}
+			if (cr && (cl < 2u || cl > rows_limit || cd > 2u)) {
+				continue;
+			}
+			if (!erosion_variant_stable(cl, cd, cr, density)) {
 				continue;
 			}
 			lanes = cl;
 			dpg = cd;
+			rows = cr;
 			float t = 0.0f;
 			for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
 				rc = stage(1u, s);
@@ -200,10 +218,12 @@ struct stpgb_batch {
 				best = t;
 				best_lanes = cl;
 				best_dpg = cd;
+				best_rows = cr;
 			}
 		}
 		lanes = best_lanes;
 		dpg = best_dpg;
+		rows = best_rows;
 		cudaEventDestroy(e0);
 		cudaEventDestroy(e1);
 		cudaStreamDestroy(s);
@@ -225,7 +245,7 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -305,7 +325,13 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		STPGB_TRY(stpgb_erosion_brush_generate(3u * r.MapSize, r.BrushRadius, brush_i[n].data(), brush_w[n].data(), bs, &bs));
 		b->max_brush = std::max(b->max_brush, bs);
 		b->lane_limit = std::min(b->lane_limit, max_lanes(bs));
-		b->lanes = std::min(8u, b->lane_limit);
+		b->rows_limit = std::min(b->rows_limit, rows_max_lanes(r.BrushRadius));
+		b->density = std::max(b->density, static_cast<double>(r.DropletCount) / (static_cast<double>(S) * S));
+		// the default until the autotuner runs: brush rows where stable, else
+		// several lanes point by point, above kDenseRows the reference kernel
+		b->rows = b->rows_limit != 0u && b->density <= kDenseRows;
+		b->lanes = b->rows ? b->rows_limit : b->density <= kDenseRows ? std::min(8u, b->lane_limit) : 1u;
+		b->dpg = 1u;
 		L.brush_idx = off;
 		off += al(bs * sizeof(int32_t));
 		L.brush_w = off;
@@ -556,7 +582,7 @@ int stpgb_batch_download(stpgb_batch* b, float* const* heightmaps, uint16_t* con
 }
 
 int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32_t* droplets_per_group,
-	float* erosion_ms) {
+	uint32_t* vector_rows, float* erosion_ms) {
 	if (!b) {
 		return inval("stpgb_batch_tuning: null batch");
 	}
@@ -566,8 +592,11 @@ int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32
 	if (droplets_per_group) {
 		*droplets_per_group = b->dpg;
 	}
+	if (vector_rows) {
+		*vector_rows = b->rows ? 1u : 0u;
+	}
 	if (erosion_ms) {
-		for (int c = 0; c < 18; c++) {
+		for (int c = 0; c < 36; c++) {
 			erosion_ms[c] = b->tune_ms[c];
 		}
 	}

@@ -518,6 +518,327 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 1) erosion_multi_ke
 	}
 }
 
+// Brush runs: maximal sequences of brush points whose cells are consecutive
+// in memory (the rows of the reference's circular brush), found once per block.
+struct BrushRun {
+	int32_t first; // index of the run's first point
+	int32_t len;
+};
+
+__device__ __forceinline__ void red_add_v4(float4* addr, const float a, const float b, const float c, const float d) {
+	asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+		: "memory");
+}
+
+// K droplets (1 or 2) per group of G lanes (2 or 4) as erosion_multi_kernel,
+// with the erosion step done run by run in aligned 16-byte blocks: one
+// vector read of four cells, then one vector reduction that subtracts
+// min(cell, w) from the run's cells and adds -0.0 (which leaves any value,
+// -0.0 included, unchanged) to the block's other cells.  A droplet's cells
+// are distinct, so per droplet this is the reference's read-then-subtract
+// for every point; a block costs one L2 read and one L2 reduction instead
+// of one of each per point.  Needs a 16-byte aligned map whose pitch is a
+// multiple of four floats, so that no block leaves its row.
+template<uint32_t G, uint32_t K>
+__global__ void __launch_bounds__(kErodeBlock, 8) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
+	const ErosionJob single) {
+	static_assert((G == 2u || G == 4u) && (K == 1u || K == 2u), "2 or 4 lanes, 1 or 2 droplets");
+	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
+	extern __shared__ unsigned char esm[];
+	int32_t* const bidx = reinterpret_cast<int32_t*>(esm);
+	float* const bw = reinterpret_cast<float*>(esm) + J.brush_size;
+	BrushRun* const runs = reinterpret_cast<BrushRun*>(bw + J.brush_size);
+	__shared__ uint32_t nruns;
+	for (uint32_t k = threadIdx.x; k < J.brush_size; k += kErodeBlock) {
+		bidx[k] = J.brush_index[k];
+		bw[k] = J.brush_weight[k];
+	}
+	__syncthreads();
+	if (threadIdx.x == 0u) {
+		uint32_t n = 0u;
+		for (uint32_t p = 0u; p < J.brush_size; p++) {
+			if (p == 0u || bidx[p] != bidx[p - 1u] + 1) {
+				runs[n].first = static_cast<int32_t>(p);
+				runs[n].len = 0;
+				n++;
+			}
+			runs[n - 1u].len++;
+		}
+		nruns = n;
+	}
+	__syncthreads();
+
+	const RainParams& P = J.p;
+	const uint32_t g = threadIdx.x % G;
+	const uint32_t group = (blockIdx.x * kErodeBlock + threadIdx.x) / G;
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t gmask = G == 32u ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1u)));
+	const uint32_t glead = lane & ~(G - 1u);
+	float* const map = J.map;
+	const uint64_t pitch = J.pitch;
+	// bilinear corners: with four lanes lane g reads corner g (x + (g & 1),
+	// y + (g >> 1)); with two lanes lane g reads both corners of row y + g
+	const uint64_t corner_off = G == 4u ? (((g & 2u) ? pitch : 0u) + (g & 1u)) : (g ? pitch : 0u);
+	const uint32_t nrun = nruns;
+	const float lo = static_cast<float>(P.BrushRadius);
+	const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
+	// cells whose brush (reach BrushRadius - 1) and deposit corners stay inside the map
+	const uint32_t safe_lo = P.BrushRadius - 1u, safe_hx = J.dim_x - max(P.BrushRadius, 2u),
+		safe_hy = J.dim_y - max(P.BrushRadius, 2u);
+
+	float px[K], py[K], dirx[K], diry[K], speed[K], vol[K], sed[K];
+	uint32_t step[K];
+	bool alive[K];
+	double residual = 0.0;
+	bool capped = false;
+	uint32_t steps_done = 0u, erode_steps = 0u;
+#pragma unroll
+	for (uint32_t k = 0u; k < K; k++) {
+		const uint32_t d = group * K + k;
+		alive[k] = d < J.count;
+		px[k] = alive[k] ? J.starts[2u * d] : 0.0f;
+		py[k] = alive[k] ? J.starts[2u * d + 1u] : 0.0f;
+		alive[k] = alive[k] && px[k] >= 0.0f && px[k] < J.dim_x - 1.0f && py[k] >= 0.0f && py[k] < J.dim_y - 1.0f;
+		dirx[k] = diry[k] = 0.0f;
+		speed[k] = P.initSpeed;
+		vol[k] = P.initWaterVolume;
+		sed[k] = 0.0f;
+		step[k] = 0u;
+	}
+	auto corners = [&](const uint64_t cell) {
+		const float* const c = map + cell + corner_off;
+		return G == 4u ? make_float2(__ldcg(c), 0.0f) : make_float2(__ldcg(c), __ldcg(c + 1));
+	};
+	auto bilinear = [](const float2 v, const uint32_t gm, const uint32_t gl, const float cx, const float cy) {
+		float h00, h10, h01, h11;
+		if constexpr (G == 4u) {
+			h00 = __shfl_sync(gm, v.x, gl);
+			h10 = __shfl_sync(gm, v.x, gl + 1);
+			h01 = __shfl_sync(gm, v.x, gl + 2);
+			h11 = __shfl_sync(gm, v.x, gl + 3);
+		} else {
+			h00 = __shfl_sync(gm, v.x, gl);
+			h10 = __shfl_sync(gm, v.y, gl);
+			h01 = __shfl_sync(gm, v.x, gl + 1);
+			h11 = __shfl_sync(gm, v.y, gl + 1);
+		}
+		HG r;
+		r.h = h00 * (1.0f - cx) * (1.0f - cy) + h10 * cx * (1.0f - cy) + h01 * (1.0f - cx) * cy + h11 * cx * cy;
+		r.gx = (h10 - h00) * (1.0f - cy) + (h11 - h01) * cy;
+		r.gy = (h01 - h00) * (1.0f - cx) + (h11 - h10) * cx;
+		return r;
+	};
+
+	while (true) {
+		bool any = false;
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k] && !(vol[k] >= P.minWaterVolume)) {
+				alive[k] = false;
+				residual += sed[k];
+			} else if (alive[k] && step[k]++ >= P.MaxSteps) {
+				alive[k] = false;
+				capped = true;
+				residual += sed[k];
+			}
+			any = any || alive[k];
+		}
+		if (!any) {
+			break;
+		}
+		// phase 1: corners of the current cell of every droplet
+		uint64_t mi[K];
+		float ox[K], oy[K];
+		float2 v[K];
+		bool safe[K];
+		HG hg[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				const uint32_t cx = static_cast<uint32_t>(px[k]), cy = static_cast<uint32_t>(py[k]);
+				safe[k] = cx >= safe_lo && cx <= safe_hx && cy >= safe_lo && cy <= safe_hy;
+				mi[k] = static_cast<uint64_t>(cy) * pitch + cx;
+				ox[k] = px[k] - static_cast<float>(cx);
+				oy[k] = py[k] - static_cast<float>(cy);
+				v[k] = corners(mi[k]);
+			}
+		}
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				hg[k] = bilinear(v[k], gmask, glead, ox[k], oy[k]);
+				dirx[k] = (-hg[k].gx) * (1.0f - P.Inertia) + dirx[k] * P.Inertia;
+				diry[k] = (-hg[k].gy) * (1.0f - P.Inertia) + diry[k] * P.Inertia;
+				const float len = sqrtf(dirx[k] * dirx[k] + diry[k] * diry[k]);
+				if (len != 0.0f) {
+					dirx[k] /= len;
+					diry[k] /= len;
+				}
+				px[k] += dirx[k];
+				py[k] += diry[k];
+				// the reference's border test (a NaN position also dies); a unit
+				// move keeps the old cell's brush inside the map, `safe` also
+				// covers a direction that rounded above unit length
+				if ((dirx[k] == 0.0f && diry[k] == 0.0f)
+					|| !(px[k] >= lo && px[k] < hi_x && py[k] >= lo && py[k] < hi_y) || !safe[k]) {
+					alive[k] = false; // the carried sediment leaves with the droplet
+					residual += sed[k];
+				}
+			}
+		}
+		// phase 2: corners of the new cell, capacity, deposit or erode
+		float2 v2[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (alive[k]) {
+				const uint64_t ni = static_cast<uint64_t>(static_cast<uint32_t>(py[k])) * pitch + static_cast<uint32_t>(px[k]);
+				v2[k] = corners(ni);
+			}
+		}
+		bool erode[K];
+		float ero[K], dh[K];
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			erode[k] = false;
+			if (alive[k]) {
+				const float cx = px[k] - static_cast<float>(static_cast<uint32_t>(px[k]));
+				const float cy = py[k] - static_cast<float>(static_cast<uint32_t>(py[k]));
+				dh[k] = bilinear(v2[k], gmask, glead, cx, cy).h - hg[k].h;
+				const float cap = fmaxf(-dh[k] * speed[k] * vol[k] * P.SedimentCapacityFactor, P.minSedimentCapacity);
+				if (sed[k] > cap || dh[k] > 0.0f) {
+					const float dep = (dh[k] > 0.0f) ? fminf(dh[k], sed[k]) : (sed[k] - cap) * P.DepositSpeed;
+					sed[k] -= dep;
+					if constexpr (G == 4u) {
+						const float wx = (g & 1u) ? ox[k] : 1.0f - ox[k], wy = (g & 2u) ? oy[k] : 1.0f - oy[k];
+						atomicAdd(map + mi[k] + corner_off, dep * wx * wy);
+					} else {
+						const float wy = g ? oy[k] : 1.0f - oy[k];
+						atomicAdd(map + mi[k] + corner_off, dep * (1.0f - ox[k]) * wy);
+						atomicAdd(map + mi[k] + corner_off + 1u, dep * ox[k] * wy);
+					}
+				} else {
+					erode[k] = true;
+					erode_steps++;
+					ero[k] = fminf((cap - sed[k]) * P.ErodeSpeed, -dh[k]);
+				}
+			}
+		}
+		// phase 3: the brush runs of the eroding droplets, a run per lane; two
+		// droplets whose brushes overlap run one after the other
+		float part[K];
+		bool serial = false;
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			part[k] = 0.0f;
+		}
+		if constexpr (K == 2u) {
+			if (erode[0] && erode[1]) {
+				const int32_t reach = 2 * static_cast<int32_t>(P.BrushRadius) - 2;
+				const uint32_t a = static_cast<uint32_t>(mi[0]), b = static_cast<uint32_t>(mi[1]);
+				const uint32_t p32 = static_cast<uint32_t>(pitch);
+				const int32_t dx = static_cast<int32_t>(a % p32) - static_cast<int32_t>(b % p32);
+				const int32_t dy = static_cast<int32_t>(a / p32) - static_cast<int32_t>(b / p32);
+				serial = abs(dx) <= reach && abs(dy) <= reach;
+			}
+		}
+#pragma unroll 1
+		for (uint32_t turn = 0u; turn < (serial ? K : 1u); turn++) {
+#pragma unroll 1
+			for (uint32_t r = g; r < nrun; r += G) {
+				const BrushRun R = runs[r];
+				const int32_t off = bidx[R.first];
+				float4* blk[K];
+				int32_t lead[K], nb[K];
+				int32_t nmax = 0;
+#pragma unroll
+				for (uint32_t k = 0u; k < K; k++) {
+					nb[k] = 0;
+					if (erode[k] && (!serial || k == turn)) {
+						float* const first = map + static_cast<int64_t>(mi[k]) + off;
+						lead[k] = static_cast<int32_t>((reinterpret_cast<uintptr_t>(first) >> 2) & 3u);
+						blk[k] = reinterpret_cast<float4*>(first - lead[k]);
+						nb[k] = (lead[k] + R.len + 3) >> 2;
+						nmax = max(nmax, nb[k]);
+					}
+				}
+#pragma unroll 1
+				for (int32_t b = 0; b < nmax; b++) {
+					float4 cur[K];
+#pragma unroll
+					for (uint32_t k = 0u; k < K; k++) {
+						if (b < nb[k]) {
+							cur[k] = __ldcg(blk[k] + b);
+						}
+					}
+#pragma unroll
+					for (uint32_t k = 0u; k < K; k++) {
+						if (b < nb[k]) {
+							float c[4] = { cur[k].x, cur[k].y, cur[k].z, cur[k].w }, d[4];
+#pragma unroll
+							for (int i = 0; i < 4; i++) {
+								const int32_t j = 4 * b + i - lead[k];
+								d[i] = -0.0f;
+								if (j >= 0 && j < R.len) {
+									const float we = ero[k] * bw[R.first + j];
+									const float ds = (c[i] < we) ? c[i] : we;
+									d[i] = -ds;
+									part[k] += ds;
+								}
+							}
+							red_add_v4(blk[k] + b, d[0], d[1], d[2], d[3]);
+						}
+					}
+				}
+			}
+		}
+#pragma unroll
+		for (uint32_t k = 0u; k < K; k++) {
+			if (erode[k]) {
+#pragma unroll
+				for (uint32_t o = G / 2u; o > 0u; o >>= 1) {
+					part[k] += __shfl_xor_sync(gmask, part[k], o);
+				}
+				sed[k] += part[k];
+			}
+			if (alive[k]) {
+				speed[k] = sqrtf(fmaxf(0.0f, speed[k] * speed[k] + dh[k] * P.Gravity));
+				speed[k] *= 1.0f - P.Friction;
+				vol[k] *= 1.0f - P.EvaporateSpeed;
+				steps_done++;
+			}
+		}
+		__syncwarp(gmask);
+	}
+	if (g != 0u) {
+		residual = 0.0;
+		steps_done = 0u;
+		erode_steps = 0u;
+		capped = false;
+	}
+	if (J.counters) {
+		unsigned long long s = steps_done, e = erode_steps;
+		for (int o = 16; o > 0; o >>= 1) {
+			s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+			e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		}
+		if (lane == 0u) {
+			atomicAdd(J.counters, s);
+			atomicAdd(J.counters + 1, e);
+		}
+	}
+	if (J.residual) {
+		for (int o = 16; o > 0; o >>= 1) {
+			residual += __shfl_xor_sync(0xFFFFFFFFu, residual, o);
+		}
+		if (lane == 0u && residual != 0.0) {
+			atomicAdd(J.residual, residual);
+		}
+	}
+	if (capped && J.status) {
+		atomicOr(J.status, STATUS_TIMEOUT);
+	}
+}
+
 // STPHeightfieldKernel.cu:112-122, eight pixels per thread where rows allow.
 __device__ __forceinline__ uint32_t fmt1(const float h) {
 	return static_cast<uint32_t>(rintf(__saturatef(h) * 65535.0f));
@@ -582,6 +903,58 @@ uint32_t default_lanes(uint32_t brush_size) {
 	return std::min(8u, max_lanes(brush_size));
 }
 
+// The same rule for the brush-row update, in sequential 16-byte blocks per
+// lane: the reference's circular brush of this radius has rows of
+// 2 * floor(sqrt(r^2 - dy^2 - 1)) + 1 cells, a row of L cells spans
+// ceil((lead + L) / 4) blocks for lead 0..3 (averaged), and 4 or 2 lanes are
+// allowed while each keeps four blocks.  0 when even two lanes would not.
+uint32_t rows_max_lanes(uint32_t radius) {
+	const int64_t r = radius;
+	double blocks = 0.0;
+	for (int64_t dy = -(r - 1); dy <= r - 1; dy++) {
+		int64_t half = 0;
+		while ((half + 1) * (half + 1) + dy * dy < r * r) {
+			half++;
+		}
+		const int64_t len = 2 * half + 1;
+		for (int64_t lead = 0; lead < 4; lead++) {
+			blocks += 0.25 * static_cast<double>((lead + len + 3) / 4);
+		}
+	}
+	for (uint32_t g : { 4u, 2u }) {
+		if (blocks >= 4.0 * g) {
+			return g;
+		}
+	}
+	return 0u;
+}
+
+// Stability envelope of the kernel variants against droplet density (droplets
+// per pixel of the area the starts cover), measured on a 64^2 chunk of
+// multi-biome terrain with brushes 3 and 4: at 2.3 every variant stays in
+// range; at 3.5 brush 3 with four row lanes runs away; at 4.9 four lanes point
+// by point run away in some runs and not in others; one lane per droplet (the
+// reference kernel) holds at 7.  Above kDenseRows only the reference kernel is
+// used.
+bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_group, const bool rows,
+	const double density) {
+	(void)droplets_per_group;
+	(void)rows;
+	return lanes == 1u || density <= kDenseRows;
+}
+
+ErosionChoice erosion_choice(const uint32_t radius, const uint32_t brush_size, const double density,
+	const bool rows_allowed) {
+	if (density > kDenseRows) {
+		return ErosionChoice { 1u, 1u, false };
+	}
+	const uint32_t rl = rows_max_lanes(radius);
+	if (rows_allowed && rl != 0u) {
+		return ErosionChoice { rl, 1u, true };
+	}
+	return ErosionChoice { default_lanes(brush_size), 1u, false };
+}
+
 RainParams rain_params(const stpgb_raindrop_setting& s) {
 	RainParams p;
 	p.Inertia = s.Inertia;
@@ -611,11 +984,40 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp,
-	uint32_t droplets_per_group) {
+	uint32_t droplets_per_group, bool vector_rows) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
 	const size_t smem = static_cast<size_t>(max_brush) * (sizeof(int32_t) + sizeof(float));
+	if (vector_rows && !exact_clamp && (droplets_per_group == 1u || droplets_per_group == 2u)
+		&& (lanes_per_droplet == 2u || lanes_per_droplet == 4u)) {
+		const size_t rsmem = smem + static_cast<size_t>(max_brush) * sizeof(BrushRun);
+		const uint64_t groups = (static_cast<uint64_t>(max_count) + droplets_per_group - 1u) / droplets_per_group;
+		const uint64_t rthreads = groups * lanes_per_droplet;
+		if (rthreads > 0xFFFFFFFFull - kErodeBlock) {
+			return inval("erosion: too many droplets for one launch");
+		}
+		const dim3 rgrid(static_cast<uint32_t>((rthreads + kErodeBlock - 1u) / kErodeBlock), njobs);
+		auto go = [&](auto kernel) -> int {
+			if (rsmem > 48u * 1024u) {
+				STPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+					static_cast<int>(rsmem)));
+			}
+			kernel<<<rgrid, kErodeBlock, rsmem, stream>>>(jobs, single);
+			STPGB_CUDA_TRY(cudaGetLastError());
+			return STPGB_OK;
+		};
+		switch (lanes_per_droplet * 8u + droplets_per_group) {
+		case 2u * 8u + 1u:
+			return go(erosion_rows_kernel<2u, 1u>);
+		case 2u * 8u + 2u:
+			return go(erosion_rows_kernel<2u, 2u>);
+		case 4u * 8u + 1u:
+			return go(erosion_rows_kernel<4u, 1u>);
+		default:
+			return go(erosion_rows_kernel<4u, 2u>);
+		}
+	}
 	if (droplets_per_group > 1u) {
 		if (exact_clamp || lanes_per_droplet < 4u || (droplets_per_group != 2u && droplets_per_group != 4u)) {
 			return inval("erosion: 2 or 4 droplets per group need >= 4 lanes and the reference order");
@@ -719,7 +1121,7 @@ int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn, const stp
 	const float* starts_xy, uint32_t count, const int32_t* brush_index, const float* brush_weight,
 	uint32_t brush_size, double* residual_sediment, uint32_t* status, void* stream) {
 	return stpgb_hydraulic_erosion_ex(heightmap, nn, setting, starts_xy, count, brush_index, brush_weight,
-		brush_size, residual_sediment, status, default_lanes(brush_size), 1u, 0u, stream);
+		brush_size, residual_sediment, status, 0u, 1u, 0u, stream);
 }
 
 int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const stpgb_raindrop_setting* setting,
@@ -756,9 +1158,32 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	job.status = status;
 	job.fixed = nullptr;
 	job.counters = nullptr;
-	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream),
-		lanes_per_droplet == 0u ? default_lanes(brush_size) : lanes_per_droplet,
-		(flags & STPGB_EROSION_EXACT_CLAMP) != 0u, droplets_per_group == 0u ? 1u : droplets_per_group);
+	const bool exact = (flags & STPGB_EROSION_EXACT_CLAMP) != 0u;
+	bool rows = !exact && (flags & STPGB_EROSION_POINTWISE) == 0u
+		&& (reinterpret_cast<uintptr_t>(heightmap) & 15u) == 0u && (dx & 3u) == 0u;
+	uint32_t lanes = lanes_per_droplet, dpg = droplets_per_group == 0u ? 1u : droplets_per_group;
+	if (lanes == 0u) {
+		const double density = static_cast<double>(count) / (static_cast<double>(nn->MapSize[0]) * nn->MapSize[1]);
+		const ErosionChoice c = erosion_choice(setting->ErosionBrushRadius, brush_size, density, rows);
+		lanes = c.lanes;
+		rows = c.rows;
+	}
+	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), lanes, exact, dpg, rows);
+}
+
+int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area, uint32_t* lanes_per_droplet,
+	uint32_t* vector_rows) {
+	if (brush_radius == 0u || area == 0u || !lanes_per_droplet) {
+		return inval("stpgb_erosion_choice: radius and area must be positive");
+	}
+	uint32_t bs = 0u;
+	stpgb_erosion_brush_generate(4u * brush_radius + 4u, brush_radius, nullptr, nullptr, 0u, &bs);
+	const ErosionChoice c = erosion_choice(brush_radius, bs, static_cast<double>(droplets) / area, true);
+	*lanes_per_droplet = c.lanes;
+	if (vector_rows) {
+		*vector_rows = c.rows ? 1u : 0u;
+	}
+	return STPGB_OK;
 }
 
 int stpgb_format_heightmap(const float* in, uint16_t* out, uint32_t map_x, uint32_t map_y, void* stream) {

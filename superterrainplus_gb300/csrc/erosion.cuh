@@ -37,15 +37,37 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 // exact_clamp: brush updates by compare-and-swap (never more than a cell
 // holds) instead of the reference's read-then-subtract order;
 // droplets_per_group: 1, or 2 / 4 droplets advanced together by a group of
-// 4, 8 or 16 lanes (reference order only)
+// 4, 8 or 16 lanes (reference order only);
+// vector_rows: with 2 or 4 lanes and 1 or 2 droplets per group, update the
+// brush run by run in 16-byte blocks (every map 16-byte aligned, pitch a
+// multiple of four floats)
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
-	uint32_t droplets_per_group = 1u);
+	uint32_t droplets_per_group = 1u, bool vector_rows = false);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).
 uint32_t max_lanes(uint32_t brush_size);
 uint32_t default_lanes(uint32_t brush_size);
+
+// Lanes per droplet (4 or 2) that keep four sequential 16-byte blocks per
+// lane in the brush-row update of the circular brush of `radius`; 0 if none.
+uint32_t rows_max_lanes(uint32_t radius);
+
+// Racing droplets that share cells can dig a channel far below its
+// neighbours once they are packed densely enough; how densely depends on how
+// compressed in time a droplet's brush update is.  Up to kDenseRows droplets
+// per pixel of the start area every variant stays stable; beyond it only one
+// lane per droplet (the reference kernel) is used.
+constexpr double kDenseRows = 3.0;
+bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density);
+
+struct ErosionChoice {
+	uint32_t lanes, droplets_per_group;
+	bool rows;
+};
+// Default kernel for a brush of `radius` (`brush_size` points) at `density`.
+ErosionChoice erosion_choice(uint32_t radius, uint32_t brush_size, double density, bool rows_allowed);
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
 	cudaStream_t stream);

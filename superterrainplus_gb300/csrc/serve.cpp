@@ -486,7 +486,9 @@ struct stpgb_server {
 		double* res_dev = reinterpret_cast<double*>(sl.dev + o_res);
 		uint32_t* status_dev = reinterpret_cast<uint32_t*>(sl.dev + o_status);
 
-		uint32_t maxS = 0u, maxR = 0u, maxRS = 0u, maxCount = 0u, maxBrush = 0u, minBrush = 0xFFFFFFFFu;
+		uint32_t maxS = 0u, maxR = 0u, maxRS = 0u, maxCount = 0u, maxBrush = 0u, minBrush = 0xFFFFFFFFu,
+			minRadius = 0xFFFFFFFFu;
+		double maxDensity = 0.0;
 		size_t so = it.scratch_off;
 		for (size_t j = 0; j < ng; j++) {
 			const ChunkKey& k = it.generated[j];
@@ -570,6 +572,8 @@ struct stpgb_server {
 			maxCount = std::max(maxCount, r.droplets);
 			maxBrush = std::max(maxBrush, bsize);
 			minBrush = std::min(minBrush, bsize);
+			minRadius = std::min(minRadius, r.req.BrushRadius);
+			maxDensity = std::max(maxDensity, static_cast<double>(r.droplets) / (static_cast<double>(S) * S));
 		}
 		std::fill(it.residual_host, it.residual_host + nr, 0.0);
 		*it.status_host = 0u;
@@ -588,9 +592,15 @@ struct stpgb_server {
 		STPGB_TRY(gather_jobs_launch(reinterpret_cast<GatherJob*>(sl.dev + o_gather), static_cast<uint32_t>(nr), maxRS, s));
 		STPGB_TRY(starts_jobs_launch(reinterpret_cast<StartsJob*>(sl.dev + o_starts), static_cast<uint32_t>(nr), maxCount,
 			this->base.Seed, s));
-		const uint32_t lanes = default_lanes(minBrush);
+		// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
+		// pitches 3 * MapSize) with two droplets per group where the densest
+		// request stays in the rows' stable range, else the stable point-wise
+		// variant
+		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, true);
+		const uint32_t dpg = erosion_variant_stable(ec.lanes, 2u, ec.rows, maxDensity)
+			&& (ec.rows || ec.lanes >= 4u) ? 2u : 1u;
 		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
-			maxBrush, s, lanes, false, lanes >= 4u ? 2u : 1u));
+			maxBrush, s, ec.lanes, false, dpg, ec.rows));
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
 		STPGB_CUDA_TRY(cudaMemcpyAsync(it.residual_host, res_dev, nr * sizeof(double), cudaMemcpyDeviceToHost, s));

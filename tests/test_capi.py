@@ -139,3 +139,21 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(_capi, "_lib", None)
     with pytest.raises(ImportError):
         _capi.lib()
+
+
+@pytest.mark.parametrize("radius,density,lanes,rows", [
+    (4, 600000 / 512**2, 4, 1),  # the production chunk: brush rows, four lanes
+    (5, 2.3, 4, 1),
+    (3, 2.3, 2, 1),              # brush 3 keeps four row blocks per lane only with two lanes
+    (2, 2.3, 2, 0),              # brush 2 is too small for row blocks
+    (4, 4.0, 1, 0),              # above 3 droplets per pixel: one lane per droplet, the reference kernel
+    (3, 4.9, 1, 0),
+    (4, 7.0, 1, 0),
+])
+def test_erosion_choice_follows_density(stpgb, radius, density, lanes, rows):
+    import ctypes as C
+    area = 64 * 64
+    got_lanes, got_rows = C.c_uint32(0), C.c_uint32(0)
+    stpgb.check(stpgb.lib().stpgb_erosion_choice(radius, int(round(density * area)), area, C.byref(got_lanes),
+                                                 C.byref(got_rows)))
+    assert (got_lanes.value, got_rows.value) == (lanes, rows)

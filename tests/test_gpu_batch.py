@@ -70,8 +70,8 @@ def test_batch_erosion_mass_balance_and_format(stpgb, dev, oracle, tune):
         b.tune()
         choice, ms = b.tuning()
         # the smallest brush (radius 2, 9 points) allows at most 2 lanes per droplet,
-        # so only one droplet per group is a candidate
-        assert set(ms) == {(1, 1), (2, 1)} and choice in ms
+        # so only one droplet per group, point by point, is a candidate
+        assert set(ms) == {(1, 1, 0), (2, 1, 0)} and choice in ms
     b.run_stage(0)
     b.run_stage(1)
     before, _, _ = heights(b)

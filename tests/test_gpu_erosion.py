@@ -139,10 +139,13 @@ EROSION_CASES = {
 }
 
 
-@pytest.mark.parametrize("lanes,droplets_per_group", [(1, 1), (2, 1), (4, 1), (4, 2), (4, 4)])
-def test_erosion_stays_physical_where_droplets_channel(dev, oracle, stpgb, lanes, droplets_per_group):
+@pytest.mark.parametrize("lanes,droplets_per_group,pointwise", [
+    (1, 1, True), (2, 1, True), (2, 1, False), (2, 2, False), (4, 1, False), (4, 1, True), (4, 2, False),
+    (4, 2, True), (8, 2, True), (4, 4, True)])
+def test_erosion_stays_physical_where_droplets_channel(dev, oracle, stpgb, lanes, droplets_per_group, pointwise):
     """Multi-biome terrain with many biome borders gathers densely packed droplets (2.3 per pixel
-    of a 64^2 chunk) into shared channels; in no variant may the heights leave their range."""
+    of a 64^2 chunk) into shared channels; in no variant (point by point, or brush rows in
+    16-byte blocks) may the heights leave their range."""
     S = 64
     h = helpers.multibiome_terrain(oracle, stpgb, S, 6, 20, 11)
     count = int(round(2.3 * S * S))
@@ -150,15 +153,38 @@ def test_erosion_stays_physical_where_droplets_channel(dev, oracle, stpgb, lanes
     starts = oracle.droplet_starts(count, 11, 0, (S, S), (3, 3))
     total = h.astype(np.float64).sum()
     for out, res in erode_runs(dev, stpgb, h, (S, S), (3, 3), s, starts, 10, lanes=lanes,
-                               droplets_per_group=droplets_per_group):
+                               droplets_per_group=droplets_per_group, pointwise=pointwise):
         assert np.isfinite(out).all() and out.min() >= h.min() - 1e-3 and out.max() <= h.max() + 1e-3
         assert abs((total - out.sum()) - res) <= 1e-5 * total
 
 
+@pytest.mark.parametrize("brush,density", [(3, 4.9), (4, 4.9), (3, 7.0), (4, 7.0)])
+def test_default_choice_stays_physical_when_densely_packed(dev, oracle, stpgb, brush, density):
+    """Above 3 droplets per pixel the default runs one lane per droplet (the reference kernel): at 4.9
+    and 7 droplets per pixel of a 64^2 chunk the heights stay in range."""
+    S = 64
+    h = helpers.multibiome_terrain(oracle, stpgb, S, 6, 20, 11)
+    count = int(round(density * S * S))
+    s = helpers.raindrop_dict(count, radius=brush, lifetime=30, seed=11)
+    starts = oracle.droplet_starts(count, 11, 0, (S, S), (3, 3))
+    total = h.astype(np.float64).sum()
+    for out, res in erode_runs(dev, stpgb, h, (S, S), (3, 3), s, starts, 3):
+        assert np.isfinite(out).all() and out.min() >= h.min() - 1e-3 and out.max() <= h.max() + 1e-3
+        assert abs((total - out.sum()) - res) <= 1e-5 * total
+
+
+# "default" and the row variants update the brush in 16-byte row blocks (the
+# maps here are aligned and a multiple of four wide; the default takes the
+# lanes that keep four blocks per lane); "pointwise" keeps the point-by-point
+# kernels.
 VARIANTS = {
     "default": {},
+    "pointwise": {"pointwise": True},
     "exact-clamp": {"exact_clamp": True},
+    "rows-2-lanes-2-droplets": {"droplets_per_group": 2, "lanes": 2},
     "2-droplets-per-group": {"droplets_per_group": 2},
+    "2-droplets-pointwise": {"droplets_per_group": 2, "pointwise": True},
+    "8-lanes-2-droplets-pointwise": {"droplets_per_group": 2, "lanes": 8, "pointwise": True},
     "4-droplets-per-group": {"droplets_per_group": 4},
 }
 
@@ -179,12 +205,12 @@ def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, variant):
     starts = oracle.droplet_starts(count, 9, 0, (S, S), nn)
     idx, w = oracle.brush(3 * S, brush)
     ref, _, _ = oracle.erode(h, s, starts, idx, w, fp64=True)
-    ref_runs = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 5, lanes=1)
+    ref_runs = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 5, lanes=1, pointwise=True)
     ref_rms = [rms(r, ref) for r, _ in ref_runs]
     spread = max(rms(a, b) for i, (a, _) in enumerate(ref_runs) for b, _ in ref_runs[i + 1:])
     kw = dict(VARIANTS[variant])
     if kw.get("droplets_per_group", 1) > 1:
-        kw["lanes"] = 4  # several droplets per group need >= 4 lanes; every brush here allows 4
+        kw.setdefault("lanes", 4)  # several droplets per group need >= 4 lanes; every brush here allows 4
     prod = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 3, **kw)
     prod_rms = [rms(r, ref) for r, _ in prod]
     print(f"{case} {variant}: reference kernel RMS vs FP64 {min(ref_rms):.3g}..{max(ref_rms):.3g}, "
