@@ -539,8 +539,12 @@ __device__ __forceinline__ void red_add_v4(float4* addr, const float a, const fl
 // for every point; a block costs one L2 read and one L2 reduction instead
 // of one of each per point.  Needs a 16-byte aligned map whose pitch is a
 // multiple of four floats, so that no block leaves its row.
+// Residency bounds this chain-latency kernel more than the spilled registers
+// do: 10 blocks of 128 threads (48 registers) with one droplet per group,
+// 8 (64 registers) with two (measured: fewer, larger-register blocks, or 12
+// blocks of 40 registers, are slower).
 template<uint32_t G, uint32_t K>
-__global__ void __launch_bounds__(kErodeBlock, 8) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single) {
 	static_assert((G == 2u || G == 4u) && (K == 1u || K == 2u), "2 or 4 lanes, 1 or 2 droplets");
 	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
