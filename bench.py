@@ -344,6 +344,10 @@ def run_ours(args):
     if rank == 0 and args.serve_requests > 0:
         serving = serve_section(m, np, torch, args.serve_requests)
 
+    biomemap = None
+    if rank == 0:
+        biomemap = biomemap_section(m, np, torch, B, cpu=world == 1 and not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cores, sample = cpu_eroded_chunk(os.cpu_count() or 1)
@@ -368,6 +372,7 @@ def run_ours(args):
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
             "serving": serving,
+            "biomemap": biomemap,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
@@ -377,6 +382,49 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def biomemap_section(m, np, torch, batch, cpu=True, reps=3):
+    """The demo's biome layer chain (14 layers, STPLayerChainBuilder) on the GPU: the 5x5-chunk
+    biome region of each of `batch` requests (2560^2 uint16 each, 210 MB per pass for 16, more
+    than L2), one stpgb_layer_biomemap call per region; beside it the CPU restatement of the
+    reference's layer chain on one 512^2 chunk (one thread, as the reference's factory runs)."""
+    dev = m.DeviceOps()
+    chain, ids = m.layer_chain_demo()
+    S = MAP
+    regions = [torch.empty((5 * S, 5 * S), dtype=torch.int16, device="cuda") for _ in range(batch)]
+    origins = [((4 * n - 2) * S, -2 * S) for n in range(batch)]
+
+    def one_pass():
+        for reg, (ox, oz) in zip(regions, origins):
+            dev.layer_biomemap(chain, ids, SEED, reg, 5 * S, 5 * S, 5 * S, (ox, oz))
+
+    for _ in range(3):
+        one_pass()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        one_pass()
+    e1.record(st)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1000.0 / reps
+    px = batch * 25 * S * S
+    out = {"workload": f"demo layer chain, 14 layers, 5x5 chunks of {S}^2 per request, {batch} requests",
+           "value": batch * 25 / sec, "unit": f"{S}^2 biomemap chunks/s", "gpx_per_s": px / sec / 1e9,
+           "ms_per_pass": 1000.0 * sec, "launches_per_pass": batch, "l2": "output larger than L2 per pass"}
+    if cpu:
+        from oracle.oracle import Oracle
+        oc = Oracle()
+        chain_t = [(c.Kind, c.Param, c.Salt) for c in chain]
+        idv = np.array([ids.Ocean, ids.Plains, ids.Forest, *ids.ShallowOcean], np.uint16)
+        t0 = time.perf_counter()
+        oc.layer_biomemap(chain_t, idv, SEED, S, S, (0, 0))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": f"{S}^2 biomemap chunks/s", "cores": 1, "kind": "port",
+                               "sample": f"one {S}^2 chunk through the CPU restatement of the layer chain"}
+    return out
 
 
 def serve_section(m, np, torch, n):

@@ -579,10 +579,11 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 	const uint32_t gmask = G == 32u ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1u)));
 	const uint32_t glead = lane & ~(G - 1u);
 	float* const map = J.map;
-	const uint64_t pitch = J.pitch;
+	// cell offsets in 32 bits: a map holds fewer than 2^32 cells (checked at launch)
+	const uint32_t pitch = static_cast<uint32_t>(J.pitch);
 	// bilinear corners: with four lanes lane g reads corner g (x + (g & 1),
 	// y + (g >> 1)); with two lanes lane g reads both corners of row y + g
-	const uint64_t corner_off = G == 4u ? (((g & 2u) ? pitch : 0u) + (g & 1u)) : (g ? pitch : 0u);
+	const uint32_t corner_off = G == 4u ? (((g & 2u) ? pitch : 0u) + (g & 1u)) : (g ? pitch : 0u);
 	const uint32_t nrun = nruns;
 	const float lo = static_cast<float>(P.BrushRadius);
 	const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
@@ -593,7 +594,10 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 	float px[K], py[K], dirx[K], diry[K], speed[K], vol[K], sed[K];
 	uint32_t step[K];
 	bool alive[K];
-	double residual = 0.0;
+	// sediment that left with this thread's (at most two) droplets; summed in
+	// double per warp at the end (a double add per death would run on the
+	// narrow FP64 pipe once per lane group)
+	float residual = 0.0f;
 	bool capped = false;
 	uint32_t steps_done = 0u, erode_steps = 0u;
 #pragma unroll
@@ -609,7 +613,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 		sed[k] = 0.0f;
 		step[k] = 0u;
 	}
-	auto corners = [&](const uint64_t cell) {
+	auto corners = [&](const uint32_t cell) {
 		const float* const c = map + cell + corner_off;
 		return G == 4u ? make_float2(__ldcg(c), 0.0f) : make_float2(__ldcg(c), __ldcg(c + 1));
 	};
@@ -651,7 +655,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 			break;
 		}
 		// phase 1: corners of the current cell of every droplet
-		uint64_t mi[K];
+		uint32_t mi[K];
 		float ox[K], oy[K];
 		float2 v[K];
 		bool safe[K];
@@ -661,7 +665,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 			if (alive[k]) {
 				const uint32_t cx = static_cast<uint32_t>(px[k]), cy = static_cast<uint32_t>(py[k]);
 				safe[k] = cx >= safe_lo && cx <= safe_hx && cy >= safe_lo && cy <= safe_hy;
-				mi[k] = static_cast<uint64_t>(cy) * pitch + cx;
+				mi[k] = cy * pitch + cx;
 				ox[k] = px[k] - static_cast<float>(cx);
 				oy[k] = py[k] - static_cast<float>(cy);
 				v[k] = corners(mi[k]);
@@ -695,7 +699,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 #pragma unroll
 		for (uint32_t k = 0u; k < K; k++) {
 			if (alive[k]) {
-				const uint64_t ni = static_cast<uint64_t>(static_cast<uint32_t>(py[k])) * pitch + static_cast<uint32_t>(px[k]);
+				const uint32_t ni = static_cast<uint32_t>(py[k]) * pitch + static_cast<uint32_t>(px[k]);
 				v2[k] = corners(ni);
 			}
 		}
@@ -738,10 +742,8 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 		if constexpr (K == 2u) {
 			if (erode[0] && erode[1]) {
 				const int32_t reach = 2 * static_cast<int32_t>(P.BrushRadius) - 2;
-				const uint32_t a = static_cast<uint32_t>(mi[0]), b = static_cast<uint32_t>(mi[1]);
-				const uint32_t p32 = static_cast<uint32_t>(pitch);
-				const int32_t dx = static_cast<int32_t>(a % p32) - static_cast<int32_t>(b % p32);
-				const int32_t dy = static_cast<int32_t>(a / p32) - static_cast<int32_t>(b / p32);
+				const int32_t dx = static_cast<int32_t>(mi[0] % pitch) - static_cast<int32_t>(mi[1] % pitch);
+				const int32_t dy = static_cast<int32_t>(mi[0] / pitch) - static_cast<int32_t>(mi[1] / pitch);
 				serial = abs(dx) <= reach && abs(dy) <= reach;
 			}
 		}
@@ -758,7 +760,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 				for (uint32_t k = 0u; k < K; k++) {
 					nb[k] = 0;
 					if (erode[k] && (!serial || k == turn)) {
-						float* const first = map + static_cast<int64_t>(mi[k]) + off;
+						float* const first = map + (static_cast<int64_t>(mi[k]) + off);
 						lead[k] = static_cast<int32_t>((reinterpret_cast<uintptr_t>(first) >> 2) & 3u);
 						blk[k] = reinterpret_cast<float4*>(first - lead[k]);
 						nb[k] = (lead[k] + R.len + 3) >> 2;
@@ -814,7 +816,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 		__syncwarp(gmask);
 	}
 	if (g != 0u) {
-		residual = 0.0;
+		residual = 0.0f;
 		steps_done = 0u;
 		erode_steps = 0u;
 		capped = false;
@@ -831,11 +833,16 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 		}
 	}
 	if (J.residual) {
-		for (int o = 16; o > 0; o >>= 1) {
-			residual += __shfl_xor_sync(0xFFFFFFFFu, residual, o);
+		// the warp's 8 or 16 droplet residuals, gathered on lane 0 and summed in double
+		double total = 0.0;
+		for (uint32_t l = 0u; l < 32u; l += G) {
+			const float r = __shfl_sync(0xFFFFFFFFu, residual, static_cast<int>(l));
+			if (lane == 0u) {
+				total += static_cast<double>(r);
+			}
 		}
-		if (lane == 0u && residual != 0.0) {
-			atomicAdd(J.residual, residual);
+		if (lane == 0u && total != 0.0) {
+			atomicAdd(J.residual, total);
 		}
 	}
 	if (capped && J.status) {
