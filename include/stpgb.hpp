@@ -11,6 +11,8 @@
  *       (SuperAlgorithm+Host/STPSingleHistogramFilter.h:36-190)
  *   SuperTerrainPlus::STPHeightfieldGenerator::generate / erode
  *       (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,145,159)
+ *   SuperTerrainPlus::STPDiversity::STPBiomeFactory, STPDemo::STPLayerChainBuilder
+ *       (SuperTerrain+/World/Diversity/STPBiomeFactory.h:19-63, SuperDemo+/World/Layers/STPAllLayers.h)
  *   SuperTerrainPlus::STPException::{STPNumericDomainError, STPInvalidEnvironment, STPCUDAError}
  */
 #ifndef STPGB_HPP_
@@ -193,6 +195,66 @@ inline STPPermutationTable generate(const STPEnvironment::STPSimplexNoiseSetting
 
 } // namespace STPAlgorithm
 
+namespace STPDiversity {
+
+/* STPBiomeFactory (SuperTerrain+/World/Diversity/STPBiomeFactory.h:19-63)
+ * over a linear chain of the demo's layer kinds, evaluated on the GPU:
+ * factory(biomemap, offset) fills a host array of BiomeDimension.x *
+ * BiomeDimension.y samples of world pixels offset + (x, z), row-major, as
+ * STPBiomeFactory::operator() (STPBiomeFactory.cpp:24-41) does. */
+class STPBiomeFactory {
+public:
+	template<class V>
+	STPBiomeFactory(const V& dimension, STPSeed_t global_seed, std::vector<stpgb_layer> chain,
+		const stpgb_layer_biomes& ids) :
+		DimX(static_cast<uint32_t>(dimension.x)), DimY(static_cast<uint32_t>(dimension.y)), Seed(global_seed),
+		Chain(std::move(chain)), Ids(ids) {
+		if (dimension.x <= 0 || dimension.y <= 0) {
+			throw STPException::STPNumericDomainError(
+				"Biomemap should have strictly positive dimension in both vector components");
+		}
+	}
+
+	template<class IV>
+	void operator()(STPSample_t* biomemap, const IV& offset) const {
+		detail::check(stpgb_layer_biomemap_host(Chain.data(), static_cast<uint32_t>(Chain.size()), Seed, &Ids,
+			biomemap, DimX, DimY, static_cast<int32_t>(offset.x), static_cast<int32_t>(offset.y)));
+	}
+
+	uint32_t dimensionX() const noexcept {
+		return DimX;
+	}
+	uint32_t dimensionY() const noexcept {
+		return DimY;
+	}
+
+private:
+	uint32_t DimX, DimY;
+	STPSeed_t Seed;
+	std::vector<stpgb_layer> Chain;
+	stpgb_layer_biomes Ids;
+};
+
+} // namespace STPDiversity
+
+namespace detail {
+
+inline std::vector<stpgb_layer> demo_chain() {
+	std::vector<stpgb_layer> c(STPGB_MAX_LAYERS);
+	uint32_t n = 0u;
+	check(stpgb_layer_chain_demo(c.data(), static_cast<uint32_t>(c.size()), &n));
+	c.resize(n);
+	return c;
+}
+
+inline stpgb_layer_biomes demo_ids() {
+	stpgb_layer_biomes ids {};
+	stpgb_layer_biomes_demo(&ids);
+	return ids;
+}
+
+} // namespace detail
+
 /* STPHeightfieldGenerator with the multi-biome diversity plugin
  * (STPBiomefieldGenerator) folded in: the plugin's biome table and
  * interpolation radius are constructor arguments. */
@@ -237,5 +299,23 @@ private:
 };
 
 } // namespace SuperTerrainPlus
+
+namespace STPDemo {
+
+/* STPLayerChainBuilder (SuperDemo+/World/Layers/STPAllLayers.h): the demo's
+ * 14-layer production line (STPAllLayers.cpp:59-105) with the demo's biome
+ * IDs, or other IDs for the same chain. */
+class STPLayerChainBuilder : public SuperTerrainPlus::STPDiversity::STPBiomeFactory {
+public:
+	template<class V>
+	STPLayerChainBuilder(const V& dimension, SuperTerrainPlus::STPSeed_t global_seed) :
+		STPBiomeFactory(dimension, global_seed, SuperTerrainPlus::detail::demo_chain(),
+			SuperTerrainPlus::detail::demo_ids()) {}
+	template<class V>
+	STPLayerChainBuilder(const V& dimension, SuperTerrainPlus::STPSeed_t global_seed, const stpgb_layer_biomes& ids) :
+		STPBiomeFactory(dimension, global_seed, SuperTerrainPlus::detail::demo_chain(), ids) {}
+};
+
+} // namespace STPDemo
 
 #endif /* STPGB_HPP_ */

@@ -2,7 +2,8 @@
 // against the C++ façade (include/stpgb.hpp) the way a SuperTerrain+ caller
 // would: SuperTest+/SuperAlgorithm+/STPTestHistogram.cpp (known-answer
 // histograms and error cases), STPTestPermutation.cpp (gradients,
-// repetition, seeds, invalid setting), and a generate/erode round trip.
+// repetition, seeds, invalid setting), a generate/erode round trip, and the
+// demo's biome layer chain against maps of the compiled reference.
 // `--cpu` runs the parts that fail before any device work.
 #include "stpgb.hpp"
 
@@ -215,6 +216,39 @@ void generator_round_trip() {
 	CHECK(after <= before + 1e-3 * before); // sediment only leaves the map
 }
 
+struct ivec2 {
+	int x, y;
+};
+
+uint64_t fnv1a(const std::vector<STPSample_t>& v) {
+	uint64_t h = 0xcbf29ce484222325ull;
+	for (const STPSample_t s : v) {
+		for (int b = 0; b < 2; b++) {
+			h ^= static_cast<uint8_t>(s >> (8 * b));
+			h *= 0x100000001b3ull;
+		}
+	}
+	return h;
+}
+
+void biome_factory_errors() {
+	CHECK(throws<STPException::STPNumericDomainError>([] { STPDemo::STPLayerChainBuilder f(ivec2 { 0, 4 }, 1u); }));
+}
+
+// tests/golden/layer_biomemap.npz cases 4 and 7: the reference's own layer
+// chain (STPLayerChainBuilder, compiled from its sources), FNV-1a of the
+// little-endian uint16 map.
+void biome_factory_reference_maps() {
+	STPDemo::STPLayerChainBuilder a(ivec2 { 1024, 1024 }, 11u);
+	std::vector<STPSample_t> m(1024u * 1024u);
+	a(m.data(), ivec2 { -512, -512 });
+	CHECK(fnv1a(m) == 0x5a656f9c4454cb0cull);
+	STPDemo::STPLayerChainBuilder b(ivec2 { 512, 512 }, 0u);
+	std::vector<STPSample_t> n(512u * 512u);
+	b(n.data(), ivec2 { 1000000, -2000000 });
+	CHECK(fnv1a(n) == 0x9e90f7226ff73ea4ull);
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
@@ -222,9 +256,11 @@ int main(int argc, char** argv) {
 	histogram_errors();
 	permutation();
 	generator_errors();
+	biome_factory_errors();
 	if (!cpu_only) {
 		histogram_known_answer();
 		generator_round_trip();
+		biome_factory_reference_maps();
 	}
 	std::printf("%s: %d failure(s)\n", cpu_only ? "cpu" : "all", failures);
 	return failures == 0 ? 0 : 1;
