@@ -361,6 +361,76 @@ STPGB_API int stpgb_layer_biomemap_host(const stpgb_layer* chain, uint32_t count
 	const stpgb_layer_biomes* ids, uint16_t* biomemap, uint32_t width, uint32_t height, int32_t offset_x,
 	int32_t offset_z);
 
+/* ------------------------------------------------------------ splatmap --- */
+
+/* Splat rules (SuperTerrain+/Public/SuperTerrain+/World/Diversity/Texture/
+ * STPTextureInformation.hpp:27-106).  Rules are added per biome sample as
+ * the reference's STPTextureSplatBuilder adds them
+ * (SuperTerrain+/Private/World/Diversity/STPTextureDatabase.cpp:305-350):
+ * an altitude rule makes RegionIndex active up to UpperBound; a gradient rule
+ * makes it active for minGradient <= slope <= maxGradient and LowerBound <=
+ * altitude <= UpperBound.  RegionIndex is the index the renderer's texture
+ * region registry uses (the reference converts texture IDs to it). */
+typedef struct stpgb_altitude_rule {
+	uint16_t Sample;
+	float UpperBound;
+	uint32_t RegionIndex;
+} stpgb_altitude_rule;
+
+typedef struct stpgb_gradient_rule {
+	uint16_t Sample;
+	float minGradient, maxGradient, LowerBound, UpperBound;
+	uint32_t RegionIndex;
+} stpgb_gradient_rule;
+
+/* The demo's rules (SuperDemo+/Script/STPBiomeSplatRule.tdl), regions
+ * numbered in the script's texture order: redrock 0, grass 1, mossrock 2,
+ * sand 3, soil 4, darkrock 5. */
+STPGB_API int stpgb_splat_rules_demo(stpgb_altitude_rule* altitude, uint32_t altitude_capacity,
+	uint32_t* altitude_count, stpgb_gradient_rule* gradient, uint32_t gradient_capacity,
+	uint32_t* gradient_count);
+
+/* STPSplatGeneratorInformation::STPLocalChunkInformation
+ * (STPTextureInformation.hpp:114-135): which chunk of the rendering buffer
+ * to splat, and its chunk map offset (the noise offset). */
+typedef struct stpgb_splat_chunk {
+	uint32_t LocalChunkCoordinateX, LocalChunkCoordinateY;
+	float ChunkMapOffsetX, ChunkMapOffsetY;
+} stpgb_splat_chunk;
+
+typedef struct stpgb_splat_generator stpgb_splat_generator;
+
+/* The splatmap generator (SuperDemo+/World/Biomes/STPSplatmapGenerator.cpp
+ * with SuperDemo+/Script/STPSplatmapGenerator.cu and the rule database of
+ * STPTextureFactory, SuperTerrain+/Private/World/Diversity/
+ * STPTextureFactory.cpp:138-200): rules in host memory (sorted here as the
+ * texture database sorts them: altitude rules by sample then upper bound,
+ * gradient rules by sample in the order added), the simplex setting of the
+ * world (permutation table) and the chunk MapSize. */
+STPGB_API int stpgb_splat_generator_create(const stpgb_altitude_rule* altitude, uint32_t altitude_count,
+	const stpgb_gradient_rule* gradient, uint32_t gradient_count, const stpgb_simplex_setting* simplex,
+	uint32_t map_x, uint32_t map_y, stpgb_splat_generator** out);
+STPGB_API int stpgb_splat_generator_destroy(stpgb_splat_generator* generator);
+
+/* Replaces STPTextureFactory::operator() / generateTextureSplatmap
+ * (STPTextureFactory.cpp:211-232, STPSplatmapGenerator.cu).  The rendering
+ * buffer is width x height pixels of device memory: `biomemap` (uint16) and
+ * `heightmap` (uint16 fixed-point heights, as formatHeightmap writes them),
+ * rows `map_pitch` elements apart; `splatmap` (uint8 region per pixel, 255 =
+ * no region) rows `splat_pitch` bytes apart.  Each of the `count` chunks
+ * (host array) covers MapSize pixels at LocalChunkCoordinate * MapSize.  The
+ * heightmap is read through a texture with the reference's sampler (linear
+ * filter, normalised float, clamp, unnormalised coordinates), the biomemap
+ * through a point-filtered one, so both buffers must start on a 512-byte
+ * boundary with a row pitch that is a multiple of 32 bytes.  `slope` and
+ * `altitude` (device float, may be NULL, rows `splat_pitch` elements apart)
+ * receive the slope factor and the noisy altitude the rules are tested with.
+ * Asynchronous on `stream`. */
+STPGB_API int stpgb_splatmap(stpgb_splat_generator* generator, const uint16_t* biomemap,
+	const uint16_t* heightmap, uint32_t map_pitch, uint8_t* splatmap, uint32_t splat_pitch, uint32_t width,
+	uint32_t height, const stpgb_splat_chunk* chunks, uint32_t count, float* slope, float* altitude,
+	void* stream);
+
 /* ------------------------------------- plain per-chunk drop-in generator -- */
 
 typedef struct stpgb_generator stpgb_generator;

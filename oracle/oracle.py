@@ -61,6 +61,9 @@ class Oracle:
         L.orc_voronoi.restype = None
         L.orc_layer_biomemap.argtypes = [vp, u32, u64, vp, vp, u32, u32, i32, i32]
         L.orc_layer_biomemap.restype = None
+        L.orc_splatmap.argtypes = [vp, vp, u32, u32, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp, vp, vp, u32, vp,
+                                   u32, vp, vp]
+        L.orc_splatmap.restype = None
         L.orc_mix_seed.argtypes = [u64, C.c_int64]
         L.orc_layer_seed.argtypes = [u64, u64]
         L.orc_local_seed.argtypes = [u64, u64, i32, i32]
@@ -159,6 +162,54 @@ class Oracle:
 
     def local_seed(self, global_seed, salt, x, z):
         return self.lib.orc_local_seed(global_seed, salt, x, z)
+
+
+    # -- splatmap
+    def splatmap(self, biomemap, heightmap, chunks, map_size, altitude_rules, gradient_rules, perm, grad):
+        """Region map (uint8, 255 = none), slope factor and tested altitude of the requested chunks
+        of a rendering buffer; chunks: (local x, local y, map offset x, map offset y);
+        rules: (sample, upper bound, region) and (sample, min g, max g, lower, upper, region)."""
+        h, w = heightmap.shape
+        dict_, reg, alt, gra = splat_rule_tables(altitude_rules, gradient_rules)
+        ch = np.array([tuple(c) for c in chunks], SPLAT_CHUNK_DTYPE)
+        out = np.full((h, w), 0, np.uint8)
+        slope = np.zeros((h, w), np.float32)
+        altitude = np.zeros((h, w), np.float32)
+        self.lib.orc_splatmap(_p(np.ascontiguousarray(biomemap, np.uint16)), _p(np.ascontiguousarray(heightmap,
+                              np.uint16)), w, w, h, _p(ch), len(ch), map_size[0], map_size[1], _p(dict_), len(dict_),
+                              _p(reg), _p(alt), _p(gra), _p(perm), _p(grad), len(grad) // 2, _p(out), w, _p(slope),
+                              _p(altitude))
+        return out, slope, altitude
+
+
+SPLAT_CHUNK_DTYPE = np.dtype([("lx", "<u4"), ("ly", "<u4"), ("ox", "<f4"), ("oy", "<f4")])
+SPLAT_REG_DTYPE = np.dtype([("AltitudeEntry", "<u4"), ("AltitudeSize", "<u4"), ("GradientEntry", "<u4"),
+                            ("GradientSize", "<u4")])
+ALT_NODE_DTYPE = np.dtype([("RegionIndex", "<u4"), ("UpperBound", "<f4")])
+GRA_NODE_DTYPE = np.dtype([("RegionIndex", "<u4"), ("minGradient", "<f4"), ("maxGradient", "<f4"),
+                           ("LowerBound", "<f4"), ("UpperBound", "<f4")])
+
+
+def splat_rule_tables(altitude_rules, gradient_rules):
+    """The rule database as the reference's texture database orders it
+    (SuperTerrain+/Private/World/Diversity/STPTextureDatabase.cpp:357-411,
+    STPTextureFactory.cpp:138-172): samples ascending; per sample its
+    altitude rules by upper bound and its gradient rules in the order added."""
+    alt = sorted(enumerate(altitude_rules), key=lambda t: (t[1][0], t[1][1], t[0]))
+    gra = sorted(enumerate(gradient_rules), key=lambda t: (t[1][0], t[0]))
+    samples = sorted({r[0] for _, r in alt} | {r[0] for _, r in gra})
+    reg = np.zeros(max(len(samples), 1), SPLAT_REG_DTYPE)
+    an, gn = [], []
+    for d, smp in enumerate(samples):
+        reg[d]["AltitudeEntry"] = len(an)
+        an += [(r[2], r[1]) for _, r in alt if r[0] == smp]
+        reg[d]["AltitudeSize"] = len(an) - reg[d]["AltitudeEntry"]
+        reg[d]["GradientEntry"] = len(gn)
+        gn += [(r[5], r[1], r[2], r[3], r[4]) for _, r in gra if r[0] == smp]
+        reg[d]["GradientSize"] = len(gn) - reg[d]["GradientEntry"]
+    # the node arrays keep one unused entry when empty so that they have an address
+    return (np.array(samples, np.uint16), reg, np.array(an or [(0, 0.0)], ALT_NODE_DTYPE),
+            np.array(gn or [(0, 0.0, 0.0, 0.0, 0.0)], GRA_NODE_DTYPE))
 
 
 LAYER_DTYPE = np.dtype([("Kind", "<u4"), ("Param", "<u4"), ("Salt", "<u8")])

@@ -829,3 +829,124 @@ void orc_layer_biomemap(const void* chain, uint32_t count, uint64_t global_seed,
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------------
+ * Texture splatmap (SuperDemo+/Script/STPSplatmapGenerator.cu:56-128, rule
+ * lookups SuperTerrain+/SuperAlgorithm+/Device/Private/
+ * STPTextureSplatRuleWrapper.cu:55-126).  The texture reads follow the
+ * sampler the reference configures (STPWorldPipeline.cpp:682-696):
+ * unnormalised coordinates, clamped addressing; linear filtering blends
+ * texels floor(u - 0.5) and the next one with weight frac(u - 0.5) in
+ * 1/256 steps; point filtering takes texel floor(u).  For a uint16 texture
+ * read as normalised float, the GB300 texture unit forms the weighted sum of
+ * the integer texels exactly, rounds it to the nearest integer q with halves
+ * up, and returns float(q) / 65535 correctly rounded: measured bit for bit on
+ * 26,880 samples at the positions this kernel uses (weights 0 and 1/2).
+ * rnormf(3, g) is 1 / |g| rounded from double (CUDA's may differ by an ulp).
+ * ------------------------------------------------------------------------ */
+namespace {
+
+struct OrcSplatRegistry {
+	uint32_t AltitudeEntry, AltitudeSize, GradientEntry, GradientSize;
+};
+struct OrcAltitudeNode {
+	uint32_t RegionIndex;
+	float UpperBound;
+};
+struct OrcGradientNode {
+	uint32_t RegionIndex;
+	float minGradient, maxGradient, LowerBound, UpperBound;
+};
+struct OrcSplatChunk {
+	uint32_t lx, ly;
+	float off_x, off_y;
+};
+
+int64_t texel(const uint16_t* m, uint32_t pitch, uint32_t w, uint32_t h, int x, int y) {
+	x = std::min(std::max(x, 0), static_cast<int>(w) - 1);
+	y = std::min(std::max(y, 0), static_cast<int>(h) - 1);
+	return m[static_cast<size_t>(y) * pitch + x];
+}
+
+float tex_linear(const uint16_t* m, uint32_t pitch, uint32_t w, uint32_t h, float u, float v) {
+	const float xb = u - 0.5f, yb = v - 0.5f;
+	const float x0 = std::floor(xb), y0 = std::floor(yb);
+	const int64_t a = std::lround((xb - x0) * 256.0f), b = std::lround((yb - y0) * 256.0f);
+	const int i = static_cast<int>(x0), j = static_cast<int>(y0);
+	const int64_t sum = (256 - a) * (256 - b) * texel(m, pitch, w, h, i, j)
+		+ a * (256 - b) * texel(m, pitch, w, h, i + 1, j) + (256 - a) * b * texel(m, pitch, w, h, i, j + 1)
+		+ a * b * texel(m, pitch, w, h, i + 1, j + 1);
+	const int64_t q = (sum + 32768) >> 16;
+	return static_cast<float>(q) / 65535.0f;
+}
+
+} // namespace
+
+extern "C" {
+
+/* Region map of `count` chunks of a width x height rendering buffer; rules
+ * as the generator lays them out (dictionary of `dict_count` sorted samples,
+ * one registry per sample, altitude and gradient node arrays).  slope and
+ * altitude (may be NULL) receive the tested values. */
+void orc_splatmap(const uint16_t* biomemap, const uint16_t* heightmap, uint32_t map_pitch, uint32_t width,
+	uint32_t height, const void* chunks_v, uint32_t count, uint32_t map_x, uint32_t map_y, const uint16_t* dict,
+	uint32_t dict_count, const void* reg_v, const void* alt_v, const void* gra_v, const uint8_t* perm,
+	const float* grad, uint32_t grad_size, uint8_t* out, uint32_t out_pitch, float* slope_out, float* alt_out) {
+	const auto* chunks = static_cast<const OrcSplatChunk*>(chunks_v);
+	const auto* reg = static_cast<const OrcSplatRegistry*>(reg_v);
+	const auto* altn = static_cast<const OrcAltitudeNode*>(alt_v);
+	const auto* gran = static_cast<const OrcGradientNode*>(gra_v);
+	const float half_x = static_cast<float>(map_x) / 2.0f, half_y = static_cast<float>(map_y) / 2.0f;
+	for (uint32_t c = 0u; c < count; c++) {
+		for (uint32_t y = 0u; y < map_y; y++) {
+			for (uint32_t x = 0u; x < map_x; x++) {
+				const uint32_t sx = x + map_x * chunks[c].lx, sy = y + map_y * chunks[c].ly;
+				const float fx = static_cast<float>(sx), fy = static_cast<float>(sy);
+				const float top = tex_linear(heightmap, map_pitch, width, height, fx, fy - 2.5f) * 875.5f;
+				const float left = tex_linear(heightmap, map_pitch, width, height, fx - 2.5f, fy) * 875.5f;
+				const float right = tex_linear(heightmap, map_pitch, width, height, fx + 2.5f, fy) * 875.5f;
+				const float bottom = tex_linear(heightmap, map_pitch, width, height, fx, fy + 2.5f) * 875.5f;
+				const double g0 = top - bottom, g1 = 5.5, g2 = left - right;
+				const float rn = static_cast<float>(1.0 / std::sqrt(g0 * g0 + g1 * g1 + g2 * g2));
+				const float slope = 1.0f - 5.5f * rn;
+				const float noise = orc_fractal(perm, grad, grad_size, 1.0f * x, 1.0f * y, 0.7f, 1.88f, 3u, 91.5f,
+					chunks[c].off_x, chunks[c].off_y, half_x, half_y) * 0.15f;
+				const int bx = std::min(static_cast<int>(sx), static_cast<int>(width) - 1),
+					by = std::min(static_cast<int>(sy), static_cast<int>(height) - 1);
+				const uint16_t biome = biomemap[static_cast<size_t>(by) * map_pitch + bx];
+				const float alt = saturatef(tex_linear(heightmap, map_pitch, width, height, fx, fy) + noise);
+				// findSplatRegistry: lower bound; a missing sample takes the next larger one's registry
+				const uint32_t d = static_cast<uint32_t>(std::lower_bound(dict, dict + dict_count, biome) - dict);
+				uint32_t region = 0xFFFFFFFFu;
+				if (d < dict_count) {
+					const OrcSplatRegistry& r = reg[d];
+					for (uint32_t i = r.GradientEntry; i < r.GradientEntry + r.GradientSize; i++) {
+						const OrcGradientNode& n = gran[i];
+						if (slope >= n.minGradient && slope <= n.maxGradient && alt >= n.LowerBound && alt <= n.UpperBound) {
+							region = n.RegionIndex;
+							break;
+						}
+					}
+					if (region == 0xFFFFFFFFu) {
+						for (uint32_t i = r.AltitudeEntry; i < r.AltitudeEntry + r.AltitudeSize; i++) {
+							if (!(altn[i].UpperBound < alt)) {
+								region = altn[i].RegionIndex;
+								break;
+							}
+						}
+					}
+				}
+				const size_t o = static_cast<size_t>(sy) * out_pitch + sx;
+				out[o] = static_cast<uint8_t>(region);
+				if (slope_out) {
+					slope_out[o] = slope;
+				}
+				if (alt_out) {
+					alt_out[o] = alt;
+				}
+			}
+		}
+	}
+}
+
+} // extern "C"

@@ -19,8 +19,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import (STPGB_MAX_LAYERS, BiomeProperty, ChunkSetting, Layer, LayerBiomes, NNInfo, Permutation,
-                    RaindropSetting, SimplexSetting, STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
+from ._capi import (STPGB_MAX_LAYERS, AltitudeRule, BiomeProperty, ChunkSetting, GradientRule, Layer, LayerBiomes,
+                    NNInfo, Permutation, RaindropSetting, SimplexSetting, SplatChunk, STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
                     STPNumericDomainError, STPTimeout, check, lib)
 
 __all__ = [
@@ -29,7 +29,8 @@ __all__ = [
     "STPNumericDomainError", "STPTimeout", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
     "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch", "Layer", "LayerBiomes",
-    "layer_chain_demo", "STPLayerChainBuilder",
+    "layer_chain_demo", "STPLayerChainBuilder", "AltitudeRule", "GradientRule", "SplatChunk", "splat_rules_demo",
+    "STPSplatmapGenerator",
 ]
 
 BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
@@ -115,6 +116,51 @@ class STPLayerChainBuilder:
             raise STPNumericDomainError("biomemap must be a contiguous uint16 array of the factory's dimension")
         check(lib().stpgb_layer_biomemap_host(self.chain, len(self.chain), self.GlobalSeed, C.byref(self.ids),
                                               _p(biomemap), w, h, int(offset[0]), int(offset[1])))
+
+
+# ---------------------------------------------------------------- splatmap
+
+
+def splat_rules_demo():
+    """The demo's splat rules (SuperDemo+/Script/STPBiomeSplatRule.tdl): (altitude, gradient) ctypes arrays."""
+    a, g = (AltitudeRule * 16)(), (GradientRule * 16)()
+    na, ng = C.c_uint32(0), C.c_uint32(0)
+    check(lib().stpgb_splat_rules_demo(a, 16, C.byref(na), g, 16, C.byref(ng)))
+    return (AltitudeRule * na.value)(*a[:na.value]), (GradientRule * ng.value)(*g[:ng.value])
+
+
+class STPSplatmapGenerator:
+    """The splatmap generator (SuperDemo+/World/Biomes/STPSplatmapGenerator.h with the rule database
+    of STPTextureFactory): `gen(biomemap, heightmap, map_pitch, splatmap, splat_pitch, width, height,
+    chunks)` on torch CUDA tensors fills the region of every pixel of the requested chunks
+    (STPTextureFactory::operator(), SuperTerrain+/Private/World/Diversity/STPTextureFactory.cpp:211-232)."""
+
+    def __init__(self, altitude_rules, gradient_rules, simplex_setting, map_size):
+        h = C.c_void_p()
+        alt = altitude_rules if isinstance(altitude_rules, C.Array) else \
+            (AltitudeRule * len(altitude_rules))(*[AltitudeRule(*r) for r in altitude_rules])
+        gra = gradient_rules if isinstance(gradient_rules, C.Array) else \
+            (GradientRule * len(gradient_rules))(*[GradientRule(*r) for r in gradient_rules])
+        check(lib().stpgb_splat_generator_create(alt, len(alt), gra, len(gra), C.byref(simplex_setting),
+                                                 map_size[0], map_size[1], C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().stpgb_splat_generator_destroy(h)
+            self._h = None
+
+    def __call__(self, biomemap, heightmap, map_pitch, splatmap, splat_pitch, width, height, chunks, slope=None,
+                 altitude=None, stream=None):
+        import torch
+        ch = (SplatChunk * max(len(chunks), 1))(*[c if isinstance(c, SplatChunk) else SplatChunk(*c)
+                                                  for c in chunks])
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().stpgb_splatmap(self._h, C.c_void_p(biomemap.data_ptr()), C.c_void_p(heightmap.data_ptr()),
+                                   map_pitch, C.c_void_p(splatmap.data_ptr()), splat_pitch, width, height, ch,
+                                   len(chunks), C.c_void_p(slope.data_ptr() if slope is not None else 0),
+                                   C.c_void_p(altitude.data_ptr() if altitude is not None else 0), C.c_void_p(s)))
 
 
 class STPFilterBuffer:

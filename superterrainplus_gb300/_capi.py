@@ -130,6 +130,20 @@ STPGB_LAYER_CONTINENT, STPGB_LAYER_SCALE, STPGB_LAYER_LAND, STPGB_LAYER_ISLAND, 
 STPGB_SCALE_NORMAL, STPGB_SCALE_FUZZY = 0, 1
 STPGB_MAX_LAYERS = 32
 
+class AltitudeRule(C.Structure):
+    _fields_ = [("Sample", u16), ("UpperBound", f32), ("RegionIndex", u32)]
+
+
+class GradientRule(C.Structure):
+    _fields_ = [("Sample", u16), ("minGradient", f32), ("maxGradient", f32), ("LowerBound", f32),
+                ("UpperBound", f32), ("RegionIndex", u32)]
+
+
+class SplatChunk(C.Structure):
+    _fields_ = [("LocalChunkCoordinateX", u32), ("LocalChunkCoordinateY", u32), ("ChunkMapOffsetX", f32),
+                ("ChunkMapOffsetY", f32)]
+
+
 STPGB_BATCH_GRAPH = 1
 STPGB_BATCH_AUTOTUNE = 2
 
@@ -158,6 +172,11 @@ PROTOTYPES = {
     "stpgb_erosion_choice": (C.c_int, [u32, u32, u32, C.POINTER(u32), C.POINTER(u32)]),
     "stpgb_voronoi_biomemap": (C.c_int, [vp, u32, u32, u32, i64, i64, u32, u32, u64, vp]),
     "stpgb_layer_chain_demo": (C.c_int, [vp, u32, C.POINTER(u32)]),
+    "stpgb_splat_rules_demo": (C.c_int, [vp, u32, C.POINTER(u32), vp, u32, C.POINTER(u32)]),
+    "stpgb_splat_generator_create": (C.c_int, [vp, u32, vp, u32, C.POINTER(SimplexSetting), u32, u32,
+                                               C.POINTER(vp)]),
+    "stpgb_splat_generator_destroy": (C.c_int, [vp]),
+    "stpgb_splatmap": (C.c_int, [vp, vp, vp, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp]),
     "stpgb_layer_biomes_demo": (None, [C.POINTER(LayerBiomes)]),
     "stpgb_layer_biomemap": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, u32, i32, i32, vp]),
     "stpgb_layer_biomemap_host": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, i32, i32]),

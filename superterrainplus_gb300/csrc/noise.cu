@@ -12,6 +12,7 @@
 //    reference multiplies it by the octave frequency afterwards), so the IEEE
 //    division is done once per bin instead of once per octave.
 #include "noise.cuh"
+#include "simplex.cuh"
 
 namespace stpgb {
 
@@ -19,57 +20,12 @@ namespace {
 
 constexpr uint32_t kNoiseBlock = 256u;
 
-// STPSimplexNoise.cu:5-7
-constexpr float kF2 = 0.3660254038f;
-constexpr float kG2 = 0.2113248654f;
-constexpr float kH2 = -1.0f + 2.0f * kG2;
-
-// STPSimplexNoise.cu:14-16: not floorf (an exact negative integer maps one lower)
-__device__ __forceinline__ int floori(const float x) {
-	return x > 0.0f ? static_cast<int>(x) : static_cast<int>(x - 1.0f);
-}
-
-__device__ __forceinline__ float corner(const float dx, const float dy, const float2 g) {
-	float w = 0.5f - dx * dx - dy * dy;
-	if (w <= 0.0f) {
-		return 0.0f;
-	}
-	w *= w;
-	return w * w * (g.x * dx + g.y * dy);
-}
-
-// STPSimplexNoise.cu:18-82.  The skew and unskew (x + (x+y)*F2 and
-// i - (i+j)*G2) are written with separately rounded operations: fused into
-// one multiply-add they shift the cell origin by up to an ulp of the sample
-// coordinate, which at world offsets of 10^4-10^5 pixels is a visible error.
-__device__ __forceinline__ float simplex2d(const uint8_t* __restrict__ perm, const float2* __restrict__ gtab,
-	const float x, const float y) {
-	const float s = __fmul_rn(__fadd_rn(x, y), kF2);
-	const int i = floori(__fadd_rn(x, s)), j = floori(__fadd_rn(y, s));
-	const float t = __fmul_rn(static_cast<float>(i + j), kG2);
-	const float dx0 = __fsub_rn(x, __fsub_rn(static_cast<float>(i), t));
-	const float dy0 = __fsub_rn(y, __fsub_rn(static_cast<float>(j), t));
-	const unsigned int i1 = (dx0 > dy0) ? 1u : 0u, j1 = 1u - i1;
-	const float dx1 = dx0 - static_cast<float>(i1) + kG2, dy1 = dy0 - static_cast<float>(j1) + kG2;
-	const float dx2 = dx0 + kH2, dy2 = dy0 + kH2;
-	const unsigned int ii = static_cast<unsigned int>(i) & 255u, jj = static_cast<unsigned int>(j) & 255u;
-	const float2 g0 = gtab[ii + perm[jj]];
-	const float2 g1 = gtab[ii + i1 + perm[jj + j1]];
-	const float2 g2 = gtab[ii + 1u + perm[jj + 1u]];
-	return 70.0f * (corner(dx0, dy0, g0) + corner(dx1, dy1, g1) + corner(dx2, dy2, g2));
-}
-
 __global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob* __restrict__ jobs,
 	const NoiseJob single, const stpgb_permutation perm, const stpgb_biome_property* __restrict__ table,
 	const uint32_t biome_count) {
 	__shared__ uint8_t sperm[512];
 	__shared__ float2 gtab[512];
-	for (uint32_t k = threadIdx.x; k < 512u; k += kNoiseBlock) {
-		const uint32_t p = perm.Permutation[k];
-		sperm[k] = static_cast<uint8_t>(p);
-		const uint32_t g = p % perm.Gradient2DSize;
-		gtab[k] = make_float2(perm.Gradient2D[2u * g], perm.Gradient2D[2u * g + 1u]);
-	}
+	simplex::load_tables(perm, sperm, gtab);
 	__syncthreads();
 
 	const NoiseJob& J = jobs ? jobs[blockIdx.y] : single;
@@ -93,15 +49,8 @@ __global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob*
 			continue;
 		}
 		const stpgb_biome_property p = table[id];
-		const float ux = fx / p.Scale, uy = fy / p.Scale;
-		float fractal = 0.0f, amplitude = 1.0f, frequency = 1.0f, range = 0.0f;
-		for (uint32_t o = 0u; o < p.Octave; o++) {
-			fractal += simplex2d(sperm, gtab, ux * frequency, uy * frequency) * amplitude;
-			range += amplitude;
-			amplitude *= p.Persistence;
-			frequency *= p.Lacunarity;
-		}
-		const float f = __saturatef((fractal + range) / (2.0f * range));
+		const float f = simplex::fractal(sperm, gtab, fx / p.Scale, fy / p.Scale, p.Octave, p.Persistence,
+			p.Lacunarity);
 		height += weight * (f * p.Variation + p.Depth);
 	}
 	J.out[static_cast<uint64_t>(y) * J.pitch + x] = height;
