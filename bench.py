@@ -344,9 +344,10 @@ def run_ours(args):
     if rank == 0 and args.serve_requests > 0:
         serving = serve_section(m, np, torch, args.serve_requests)
 
-    biomemap = None
+    biomemap = splatmap = None
     if rank == 0:
         biomemap = biomemap_section(m, np, torch, B, cpu=world == 1 and not args.no_cpu_baseline)
+        splatmap = splatmap_section(m, np, torch, batch, reqs, cpu=world == 1 and not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -373,6 +374,7 @@ def run_ours(args):
             "roofline": roof, "cpu_baseline": cpu, "clocks": cs,
             "serving": serving,
             "biomemap": biomemap,
+            "splatmap": splatmap,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
@@ -424,6 +426,71 @@ def biomemap_section(m, np, torch, batch, cpu=True, reps=3):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": f"{S}^2 biomemap chunks/s", "cores": 1, "kind": "port",
                                "sample": f"one {S}^2 chunk through the CPU restatement of the layer chain"}
+    return out
+
+
+def splat_rules(m):
+    """The demo's splat rules (STPBiomeSplatRule.tdl, written for samples 0 and 1) repeated for the
+    workload's 8 biomes: even biomes take sample 0's rules, odd ones sample 1's."""
+    alt, gra = m.splat_rules_demo()
+    a = [(b, r.UpperBound, r.RegionIndex) for b in range(BIOMES) for r in alt if r.Sample == b % 2]
+    g = [(b, r.minGradient, r.maxGradient, r.LowerBound, r.UpperBound, r.RegionIndex)
+         for b in range(BIOMES) for r in gra if r.Sample == b % 2]
+    return a, g
+
+
+def splatmap_section(m, np, torch, batch, reqs, cpu=True, reps=3):
+    """Splatmaps of the eroded neighbourhoods the batch just produced: per request the 3x3 chunks
+    of its fixed heightmap (uint16, 1536^2) with the centre 3x3 of its biome region, one
+    stpgb_splatmap call of 9 chunks per request; beside it the CPU restatement on one chunk."""
+    S = MAP
+    alt_rules, gra_rules = splat_rules(m)
+    gen = m.STPSplatmapGenerator(alt_rules, gra_rules, m.SimplexSetting(*SIMPLEX), (S, S))
+    outs = [torch.empty((3 * S, 3 * S), dtype=torch.uint8, device="cuda") for _ in reqs]
+    calls = []
+    for n, r in enumerate(reqs):
+        biome, _, fixed, _ = batch.buffers(n)
+        centre = biome + (S * 5 * S + S) * 2  # chunk (1, 1) of the 5x5 region
+        chunks = [(c % 3, c // 3, float((r["ChunkX"] + c % 3 - 1) * S), float((r["ChunkY"] + c // 3 - 1) * S))
+                  for c in range(9)]
+        calls.append((centre, fixed, outs[n], chunks))
+
+    def one_pass():
+        for centre, fixed, out, chunks in calls:
+            gen(centre, fixed, (5 * S, 3 * S), out, 3 * S, 3 * S, 3 * S, chunks)
+
+    for _ in range(3):
+        one_pass()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        one_pass()
+    e1.record(st)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1000.0 / reps
+    nchunks = 9 * len(reqs)
+    regions = np.bincount(outs[0].cpu().numpy().ravel(), minlength=256)
+    out = {"workload": f"demo splat rules over 8 biomes, 3x3 chunks of {S}^2 per request, {len(reqs)} requests",
+           "value": nchunks / sec, "unit": f"{S}^2 splatmap chunks/s", "gpx_per_s": nchunks * S * S / sec / 1e9,
+           "ms_per_pass": 1000.0 * sec, "launches_per_pass": len(reqs),
+           "regions_of_request0": {int(k): int(v) for k, v in enumerate(regions) if v}}
+    if cpu:
+        from oracle.oracle import Oracle
+        oc = Oracle()
+        region = [np.empty((5 * S, 5 * S), np.uint16) for _ in reqs]
+        fixed_h = [np.empty((3 * S, 3 * S), np.uint16) for _ in reqs]
+        batch.download_inputs(biome_regions=region)
+        batch.download(fixed=fixed_h)
+        torch.cuda.synchronize()
+        perm, grad = m.permutation_generate(*SIMPLEX)
+        t0 = time.perf_counter()
+        oc.splatmap(np.ascontiguousarray(region[0][S:4 * S, S:4 * S]), fixed_h[0], calls[0][3][4:5], (S, S),
+                    alt_rules, gra_rules, perm, grad)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": f"{S}^2 splatmap chunks/s", "cores": 1, "kind": "port",
+                               "sample": f"the centre {S}^2 chunk of request 0 through the CPU restatement"}
     return out
 
 

@@ -414,10 +414,11 @@ STPGB_API int stpgb_splat_generator_destroy(stpgb_splat_generator* generator);
 
 /* Replaces STPTextureFactory::operator() / generateTextureSplatmap
  * (STPTextureFactory.cpp:211-232, STPSplatmapGenerator.cu).  The rendering
- * buffer is width x height pixels of device memory: `biomemap` (uint16) and
- * `heightmap` (uint16 fixed-point heights, as formatHeightmap writes them),
- * rows `map_pitch` elements apart; `splatmap` (uint8 region per pixel, 255 =
- * no region) rows `splat_pitch` bytes apart.  Each of the `count` chunks
+ * buffer is width x height pixels of device memory: `biomemap` (uint16, rows
+ * `biome_pitch` elements apart) and `heightmap` (uint16 fixed-point heights,
+ * as formatHeightmap writes them, rows `height_pitch` elements apart);
+ * `splatmap` (uint8 region per pixel, 255 = no region) rows `splat_pitch`
+ * bytes apart.  Each of the `count` chunks
  * (host array) covers MapSize pixels at LocalChunkCoordinate * MapSize.  The
  * heightmap is read through a texture with the reference's sampler (linear
  * filter, normalised float, clamp, unnormalised coordinates), the biomemap
@@ -427,9 +428,9 @@ STPGB_API int stpgb_splat_generator_destroy(stpgb_splat_generator* generator);
  * receive the slope factor and the noisy altitude the rules are tested with.
  * Asynchronous on `stream`. */
 STPGB_API int stpgb_splatmap(stpgb_splat_generator* generator, const uint16_t* biomemap,
-	const uint16_t* heightmap, uint32_t map_pitch, uint8_t* splatmap, uint32_t splat_pitch, uint32_t width,
-	uint32_t height, const stpgb_splat_chunk* chunks, uint32_t count, float* slope, float* altitude,
-	void* stream);
+	uint32_t biome_pitch, const uint16_t* heightmap, uint32_t height_pitch, uint8_t* splatmap,
+	uint32_t splat_pitch, uint32_t width, uint32_t height, const stpgb_splat_chunk* chunks, uint32_t count,
+	float* slope, float* altitude, void* stream);
 
 /* ------------------------------------- plain per-chunk drop-in generator -- */
 

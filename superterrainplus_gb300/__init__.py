@@ -132,8 +132,10 @@ def splat_rules_demo():
 class STPSplatmapGenerator:
     """The splatmap generator (SuperDemo+/World/Biomes/STPSplatmapGenerator.h with the rule database
     of STPTextureFactory): `gen(biomemap, heightmap, map_pitch, splatmap, splat_pitch, width, height,
-    chunks)` on torch CUDA tensors fills the region of every pixel of the requested chunks
-    (STPTextureFactory::operator(), SuperTerrain+/Private/World/Diversity/STPTextureFactory.cpp:211-232)."""
+    chunks)` on torch CUDA tensors (or raw device addresses) fills the region of every pixel of the
+    requested chunks (STPTextureFactory::operator(),
+    SuperTerrain+/Private/World/Diversity/STPTextureFactory.cpp:211-232); `map_pitch` is one pitch for
+    both maps or a (biome pitch, height pitch) pair."""
 
     def __init__(self, altitude_rules, gradient_rules, simplex_setting, map_size):
         h = C.c_void_p()
@@ -157,10 +159,12 @@ class STPSplatmapGenerator:
         ch = (SplatChunk * max(len(chunks), 1))(*[c if isinstance(c, SplatChunk) else SplatChunk(*c)
                                                   for c in chunks])
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        check(lib().stpgb_splatmap(self._h, C.c_void_p(biomemap.data_ptr()), C.c_void_p(heightmap.data_ptr()),
-                                   map_pitch, C.c_void_p(splatmap.data_ptr()), splat_pitch, width, height, ch,
-                                   len(chunks), C.c_void_p(slope.data_ptr() if slope is not None else 0),
-                                   C.c_void_p(altitude.data_ptr() if altitude is not None else 0), C.c_void_p(s)))
+        bp, hp = map_pitch if isinstance(map_pitch, tuple) else (map_pitch, map_pitch)
+        addr = lambda t: t if isinstance(t, int) else t.data_ptr()
+        check(lib().stpgb_splatmap(self._h, C.c_void_p(addr(biomemap)), bp, C.c_void_p(addr(heightmap)), hp,
+                                   C.c_void_p(addr(splatmap)), splat_pitch, width, height, ch, len(chunks),
+                                   C.c_void_p(addr(slope) if slope is not None else 0),
+                                   C.c_void_p(addr(altitude) if altitude is not None else 0), C.c_void_p(s)))
 
 
 class STPFilterBuffer:

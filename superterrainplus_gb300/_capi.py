@@ -176,7 +176,7 @@ PROTOTYPES = {
     "stpgb_splat_generator_create": (C.c_int, [vp, u32, vp, u32, C.POINTER(SimplexSetting), u32, u32,
                                                C.POINTER(vp)]),
     "stpgb_splat_generator_destroy": (C.c_int, [vp]),
-    "stpgb_splatmap": (C.c_int, [vp, vp, vp, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp]),
+    "stpgb_splatmap": (C.c_int, [vp, vp, u32, vp, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp]),
     "stpgb_layer_biomes_demo": (None, [C.POINTER(LayerBiomes)]),
     "stpgb_layer_biomemap": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, u32, i32, i32, vp]),
     "stpgb_layer_biomemap_host": (C.c_int, [vp, u32, u64, C.POINTER(LayerBiomes), vp, u32, u32, i32, i32]),

@@ -34,8 +34,10 @@ using namespace stpgb;
 
 namespace {
 
+// 512-byte sub-allocations: a fixed heightmap or a biome region can then be
+// bound to a texture as it is (the texture base alignment of the GPU)
 size_t al(size_t v) {
-	return (v + 255u) & ~static_cast<size_t>(255u);
+	return (v + 511u) & ~static_cast<size_t>(511u);
 }
 
 struct RequestLayout {

@@ -362,23 +362,24 @@ int stpgb_splat_generator_destroy(stpgb_splat_generator* generator) {
 	return STPGB_OK;
 }
 
-int stpgb_splatmap(stpgb_splat_generator* g, const uint16_t* biomemap, const uint16_t* heightmap,
-	const uint32_t map_pitch, uint8_t* splatmap, const uint32_t splat_pitch, const uint32_t width,
-	const uint32_t height, const stpgb_splat_chunk* chunks, const uint32_t count, float* slope, float* altitude,
-	void* stream) {
+int stpgb_splatmap(stpgb_splat_generator* g, const uint16_t* biomemap, const uint32_t biome_pitch,
+	const uint16_t* heightmap, const uint32_t height_pitch, uint8_t* splatmap, const uint32_t splat_pitch,
+	const uint32_t width, const uint32_t height, const stpgb_splat_chunk* chunks, const uint32_t count, float* slope,
+	float* altitude, void* stream) {
 	if (!g || !biomemap || !heightmap || !splatmap || (count && !chunks)) {
 		return inval("stpgb_splatmap: null argument");
 	}
-	if (width == 0u || height == 0u || map_pitch < width || splat_pitch < width) {
+	if (width == 0u || height == 0u || biome_pitch < width || height_pitch < width || splat_pitch < width) {
 		return inval("stpgb_splatmap: empty buffer or pitch below width");
 	}
 	int dev = 0, base_align = 0, pitch_align = 0;
 	STPGB_CUDA_TRY(cudaGetDevice(&dev));
 	STPGB_CUDA_TRY(cudaDeviceGetAttribute(&base_align, cudaDevAttrTextureAlignment, dev));
 	STPGB_CUDA_TRY(cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, dev));
-	const size_t pitch_bytes = static_cast<size_t>(map_pitch) * sizeof(uint16_t);
+	const size_t bp = static_cast<size_t>(biome_pitch) * sizeof(uint16_t),
+		hp = static_cast<size_t>(height_pitch) * sizeof(uint16_t);
 	if (reinterpret_cast<uintptr_t>(biomemap) % base_align != 0u || reinterpret_cast<uintptr_t>(heightmap) % base_align != 0u
-		|| pitch_bytes % pitch_align != 0u) {
+		|| bp % pitch_align != 0u || hp % pitch_align != 0u) {
 		return inval("stpgb_splatmap: biomemap and heightmap must start on a " + std::to_string(base_align)
 			+ "-byte boundary with a row pitch that is a multiple of " + std::to_string(pitch_align) + " bytes");
 	}
@@ -390,8 +391,8 @@ int stpgb_splatmap(stpgb_splat_generator* g, const uint16_t* biomemap, const uin
 		}
 	}
 	cudaTextureObject_t bt = 0, ht = 0;
-	STPGB_TRY(g->texture(biomemap, width, height, map_pitch, false, &bt));
-	STPGB_TRY(g->texture(heightmap, width, height, map_pitch, true, &ht));
+	STPGB_TRY(g->texture(biomemap, width, height, biome_pitch, false, &bt));
+	STPGB_TRY(g->texture(heightmap, width, height, height_pitch, true, &ht));
 	SplatLaunch L {};
 	L.rules = g->rules;
 	L.perm = g->perm;
