@@ -235,6 +235,43 @@ private:
 	stpgb_layer_biomes Ids;
 };
 
+/* The splatmap generator (STPTextureFactory::operator(),
+ * SuperTerrain+/Private/World/Diversity/STPTextureFactory.cpp:211-232, with
+ * the demo's STPSplatmapGenerator kernel): rules added per biome sample as
+ * STPTextureSplatBuilder::addAltitude / addGradient add them, then one call
+ * per rendering buffer on device pointers. */
+class STPTextureSplatGenerator {
+public:
+	template<class V>
+	STPTextureSplatGenerator(const std::vector<stpgb_altitude_rule>& altitude,
+		const std::vector<stpgb_gradient_rule>& gradient, const STPEnvironment::STPSimplexNoiseSetting& simplex,
+		const V& map_size) {
+		simplex.validate();
+		stpgb_splat_generator* g = nullptr;
+		detail::check(stpgb_splat_generator_create(altitude.data(), static_cast<uint32_t>(altitude.size()),
+			gradient.data(), static_cast<uint32_t>(gradient.size()), &simplex, static_cast<uint32_t>(map_size.x),
+			static_cast<uint32_t>(map_size.y), &g));
+		Handle.reset(g);
+	}
+
+	/* Regions (uint8, 255 = none) of the requested chunks of a width x height
+	 * rendering buffer; the maps' pitches are in elements. */
+	void operator()(const STPSample_t* biomemap, uint32_t biome_pitch, const STPHeightFixed_t* heightmap,
+		uint32_t height_pitch, uint8_t* splatmap, uint32_t splat_pitch, uint32_t width, uint32_t height,
+		const std::vector<stpgb_splat_chunk>& chunks, void* stream) {
+		detail::check(stpgb_splatmap(Handle.get(), biomemap, biome_pitch, heightmap, height_pitch, splatmap, splat_pitch,
+			width, height, chunks.data(), static_cast<uint32_t>(chunks.size()), nullptr, nullptr, stream));
+	}
+
+private:
+	struct Deleter {
+		void operator()(stpgb_splat_generator* g) const {
+			stpgb_splat_generator_destroy(g);
+		}
+	};
+	std::unique_ptr<stpgb_splat_generator, Deleter> Handle;
+};
+
 } // namespace STPDiversity
 
 namespace detail {

@@ -235,6 +235,22 @@ void biome_factory_errors() {
 	CHECK(throws<STPException::STPNumericDomainError>([] { STPDemo::STPLayerChainBuilder f(ivec2 { 0, 4 }, 1u); }));
 }
 
+void splat_generator_errors() {
+	STPEnvironment::STPSimplexNoiseSetting s {};
+	s.Seed = 1u;
+	s.Distribution = 8u;
+	s.Offset = 0.1;
+	// a gradient rule whose slope range is empty (min > max)
+	CHECK(throws<STPException::STPNumericDomainError>([&] {
+		STPDiversity::STPTextureSplatGenerator g({}, { { 0u, 0.5f, 0.2f, 0.0f, 1.0f, 1u } }, s, uvec2 { 64u, 64u });
+	}));
+	STPEnvironment::STPSimplexNoiseSetting bad = s;
+	bad.Distribution = 0u;
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] {
+		STPDiversity::STPTextureSplatGenerator g({ { 0u, 1.0f, 4u } }, {}, bad, uvec2 { 64u, 64u });
+	}));
+}
+
 // tests/golden/layer_biomemap.npz cases 4 and 7: the reference's own layer
 // chain (STPLayerChainBuilder, compiled from its sources), FNV-1a of the
 // little-endian uint16 map.
@@ -257,6 +273,7 @@ int main(int argc, char** argv) {
 	permutation();
 	generator_errors();
 	biome_factory_errors();
+	splat_generator_errors();
 	if (!cpu_only) {
 		histogram_known_answer();
 		generator_round_trip();
