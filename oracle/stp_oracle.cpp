@@ -10,9 +10,11 @@
  *  SuperTest+/SuperAlgorithm+/STPTestPermutation.cpp:37-41,108-115) and
  * against the reference's own host sources compiled in this container
  * (oracle/build_ref.sh -> oracle/_ref), through committed fixtures in
- * tests/golden/.  Noise and erosion have no reference test or CPU path:
- * their restatement follows the device code line by line (cited per
- * function) and is "parity unpinned" by reference outputs.
+ * tests/golden/.  The biome layer chain is pinned the same way against the
+ * reference's STPLayer / STPBiomeFactory / demo layer sources.  Noise,
+ * erosion and the splatmap have no reference test or CPU path: their
+ * restatement follows the device code line by line (cited per function) and
+ * is "parity unpinned" by reference outputs.
  *
  * Build: g++ -O2 -std=c++17 -ffp-contract=off -shared -fPIC (oracle/build.py).
  * -ffp-contract=off keeps every float operation separately rounded.
