@@ -343,6 +343,8 @@ def run_ours(args):
     serving = None
     if rank == 0 and args.serve_requests > 0:
         serving = serve_section(m, np, torch, args.serve_requests)
+        serving["at_120_per_s"] = serve_section(m, np, torch, args.serve_requests, rate=120.0, plain=False)
+        serving["layer_chain_biomes"] = serve_section(m, np, torch, args.serve_requests, layer=True, plain=False)
 
     biomemap = splatmap = None
     if rank == 0:
@@ -494,19 +496,20 @@ def splatmap_section(m, np, torch, batch, reqs, cpu=True, reps=3):
     return out
 
 
-def serve_section(m, np, torch, n):
-    """Camera walk (1 chunk/s, new heading every 5 s), Poisson arrivals at 200/s, LOD sides
-    256/512/1024 with p 0.5/0.35/0.15, 3x3 neighbourhoods, 8 biomes, radius 32, 2.3 droplets/px,
-    brush 4, lifetime 50, through the continuous-batching server on a 40 GB pool; beside it the
-    plain per-request call sequence (9 generate + 1 erode through the drop-in generator API, host
+def serve_section(m, np, torch, n, rate=200.0, layer=False, plain=True):
+    """Camera walk (1 chunk/s, new heading every 5 s), Poisson arrivals at `rate`/s (200 in the
+    workload), LOD sides 256/512/1024 with p 0.5/0.35/0.15, 3x3 neighbourhoods, 8 biomes (or the
+    demo's biome layer chain with `layer`), radius 32, 2.3 droplets/px, brush 4, lifetime 50,
+    through the continuous-batching server on a 40 GB pool; with `plain`, beside it the plain
+    per-request call sequence (9 generate + 1 erode through the drop-in generator API, host
     buffers) on a sample of the same requests."""
     from superterrainplus_gb300.serve import Server, camera_walk
-    reqs, times = camera_walk(n, SEED, rate=200.0)
+    reqs, times = camera_walk(n, SEED, rate=rate)
     base = raindrop(m, 1)
     simplex = m.SimplexSetting(*SIMPLEX)
     table = biome_table(np, m.BIOME_DTYPE)
     sv = Server(base, simplex, table, hbm_budget=40 << 30, max_in_flight=64, max_batch=16, streams=3,
-                voronoi_cell=VORONOI_CELL, biome_seed=SEED)
+                voronoi_cell=VORONOI_CELL, biome_seed=SEED, layer_chain_biomes=layer)
     warm, wt = camera_walk(16, SEED + 1, rate=1e6)
     for w in warm:  # warm-up far from the measured walk, so it leaves no resident chunk behind for it
         w["ChunkX"] += 100000
@@ -515,10 +518,13 @@ def serve_section(m, np, torch, n):
     stats = sv.stats()
     sv.close()
     px512 = sum((r["MapSize"] / 512.0) ** 2 for r in reqs)
-    out = {"requests": n, "arrival_rate_per_s": 200.0, "wall_s": wall, "chunks_per_s": n / wall,
+    out = {"requests": n, "arrival_rate_per_s": rate, "wall_s": wall, "chunks_per_s": n / wall,
            "chunks_512_equivalent_per_s": px512 / wall, "p50_latency_ms": float(np.percentile(lat, 50)),
            "p99_latency_ms": float(np.percentile(lat, 99)), "chunks_generated": stats["ChunksGenerated"],
-           "launch_sequences": stats["Launches"], "hbm_pool_gb": 40}
+           "launch_sequences": stats["Launches"], "hbm_pool_gb": 40,
+           "biomes": "demo layer chain" if layer else "synthetic Voronoi, 8 biomes"}
+    if not plain:
+        return out
     # plain per-request calls on a sample of the same requests
     dev = m.DeviceOps()
     gens, sample = {}, reqs[: min(12, n)]

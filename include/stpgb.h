@@ -578,7 +578,13 @@ typedef struct stpgb_server_config {
 	uint32_t Streams;      /* launch sequences in flight at once */
 	uint32_t VoronoiCell;  /* synthetic biome-map cell, in pixels of a 512 chunk (scaled with the side) */
 	uint64_t BiomeSeed;
+	/* STPGB_BIOMES_VORONOI: the synthetic Voronoi map above; STPGB_BIOMES_LAYER_CHAIN:
+	 * the demo's biome layer chain (stpgb_layer_chain_demo, seed BiomeSeed, the
+	 * demo's IDs 0 / 1 / 3, which the biome table must cover), as the
+	 * reference's world pipeline generates biomemaps */
+	uint32_t BiomeSource;
 } stpgb_server_config;
+enum { STPGB_BIOMES_VORONOI = 0, STPGB_BIOMES_LAYER_CHAIN = 1 };
 
 typedef struct stpgb_serve_request {
 	int32_t ChunkX, ChunkY;       /* centre chunk of the 3x3 neighbourhood */

@@ -97,7 +97,11 @@ class BatchRequest(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("HbmBudget", C.c_uint64), ("MaxInFlight", C.c_uint32), ("MaxBatch", C.c_uint32),
-                ("Streams", C.c_uint32), ("VoronoiCell", C.c_uint32), ("BiomeSeed", C.c_uint64)]
+                ("Streams", C.c_uint32), ("VoronoiCell", C.c_uint32), ("BiomeSeed", C.c_uint64),
+                ("BiomeSource", C.c_uint32)]
+
+
+STPGB_BIOMES_VORONOI, STPGB_BIOMES_LAYER_CHAIN = 0, 1
 
 
 class ServeRequest(C.Structure):

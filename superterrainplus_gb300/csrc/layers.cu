@@ -581,6 +581,19 @@ static uint32_t fit_tile(const LayerChain& chain, uint32_t tile) {
 	return tile;
 }
 
+uint32_t layer_tile(const LayerChain& chain, const uint64_t pixels) {
+	return fit_tile(chain, layer_tile_for(pixels));
+}
+
+int layer_chain_demo(const uint64_t global_seed, LayerChain* out) {
+	stpgb_layer chain[kMaxLayers];
+	uint32_t n = 0u;
+	STPGB_TRY(stpgb_layer_chain_demo(chain, kMaxLayers, &n));
+	stpgb_layer_biomes ids;
+	stpgb_layer_biomes_demo(&ids);
+	return layer_chain_prepare(chain, n, global_seed, &ids, out);
+}
+
 } // namespace stpgb
 
 using namespace stpgb;

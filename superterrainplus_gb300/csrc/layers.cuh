@@ -35,6 +35,12 @@ int layer_chain_prepare(const stpgb_layer* chain, uint32_t count, uint64_t globa
 // Tile edge for a launch covering `pixels` output pixels in total.
 uint32_t layer_tile_for(uint64_t pixels);
 
+// The same, reduced until the chain's shared-memory plan fits.
+uint32_t layer_tile(const LayerChain& chain, uint64_t pixels);
+
+// The demo's 14-layer chain with the demo's biome IDs.
+int layer_chain_demo(uint64_t global_seed, LayerChain* out);
+
 // Fills the tiling fields of `job` for tile edge `tile`; EINVAL when the
 // rectangle leaves the supported coordinate range.
 int layer_job_tiling(BiomemapJob& job, uint32_t tile);

@@ -28,6 +28,7 @@
 #include "erosion.cuh"
 #include "noise.cuh"
 #include "serve.cuh"
+#include "layers.cuh"
 #include "shf.cuh"
 
 #include <algorithm>
@@ -175,6 +176,7 @@ struct stpgb_server {
 	float* grad = nullptr;
 	stpgb_permutation permutation {};
 	stpgb_biome_property* table = nullptr;
+	LayerChain chain {}; // the biome layer chain, when cfg.BiomeSource selects it
 	unsigned char* pool_mem = nullptr;
 	Pool pool;
 	std::vector<StreamSlot> slots;
@@ -467,7 +469,8 @@ struct stpgb_server {
 			return at_;
 		};
 		const size_t ng = it.generated.size(), nr = it.tickets.size();
-		const size_t o_vor = carve(ng * sizeof(VoronoiJob)), o_shf = carve(ng * sizeof(ShfJob)),
+		const size_t o_vor = carve(ng * sizeof(VoronoiJob)), o_lay = carve(ng * sizeof(BiomemapJob)),
+			o_shf = carve(ng * sizeof(ShfJob)),
 			o_noise = carve(ng * sizeof(NoiseJob)), o_gather = carve(nr * sizeof(GatherJob)),
 			o_starts = carve(nr * sizeof(StartsJob)), o_ero = carve(nr * sizeof(ErosionJob)),
 			o_fmt = carve(nr * sizeof(FormatJob)), o_res = carve(nr * sizeof(double)), o_status = carve(sizeof(uint32_t));
@@ -475,6 +478,16 @@ struct stpgb_server {
 			return inval("stpgb_server: job tables exceed the staging area; lower MaxBatch");
 		}
 		VoronoiJob* vor = reinterpret_cast<VoronoiJob*>(sl.host + o_vor);
+		BiomemapJob* lay = reinterpret_cast<BiomemapJob*>(sl.host + o_lay);
+		const bool layers = cfg.BiomeSource == STPGB_BIOMES_LAYER_CHAIN;
+		uint32_t tile = 0u, maxTiles = 0u;
+		if (layers) {
+			uint64_t px = 0u;
+			for (const ChunkKey& k : it.generated) {
+				px += 9ull * k.S * k.S;
+			}
+			tile = layer_tile(chain, px);
+		}
 		ShfJob* shf = reinterpret_cast<ShfJob*>(sl.host + o_shf);
 		NoiseJob* noise = reinterpret_cast<NoiseJob*>(sl.host + o_noise);
 		GatherJob* gat = reinterpret_cast<GatherJob*>(sl.host + o_gather);
@@ -510,6 +523,17 @@ struct stpgb_server {
 				static_cast<uint64_t>(cfg.VoronoiCell) * S / 512u));
 			vor[j] = VoronoiJob { region, (static_cast<int64_t>(k.x) - 1) * S, (static_cast<int64_t>(k.y) - 1) * S, 3u * S,
 				3u * S, cell };
+			if (layers) {
+				// the 3x3 chunks around chunk k, world pixels ((k - 1) * S, ...)
+				BiomemapJob& lj = lay[j];
+				lj = BiomemapJob {};
+				lj.out = region;
+				lj.x0 = static_cast<int32_t>((static_cast<int64_t>(k.x) - 1) * S);
+				lj.z0 = static_cast<int32_t>((static_cast<int64_t>(k.y) - 1) * S);
+				lj.pitch = lj.width = lj.height = 3u * S;
+				STPGB_TRY(layer_job_tiling(lj, tile));
+				maxTiles = std::max(maxTiles, lj.tiles);
+			}
 			ShfJob& sj = shf[j];
 			sj = ShfJob {};
 			sj.samplemap = region;
@@ -579,8 +603,13 @@ struct stpgb_server {
 		*it.status_host = 0u;
 		STPGB_CUDA_TRY(cudaMemcpyAsync(sl.dev, sl.host, o, cudaMemcpyHostToDevice, s));
 		if (ng) {
-			STPGB_TRY(voronoi_jobs_launch(reinterpret_cast<VoronoiJob*>(sl.dev + o_vor), static_cast<uint32_t>(ng),
-				3u * maxS, 3u * maxS, cfg.BiomeSeed, biome_count, s));
+			if (layers) {
+				STPGB_TRY(layer_biomemap_launch(chain, reinterpret_cast<BiomemapJob*>(sl.dev + o_lay), lay[0],
+					static_cast<uint32_t>(ng), maxTiles, tile, s));
+			} else {
+				STPGB_TRY(voronoi_jobs_launch(reinterpret_cast<VoronoiJob*>(sl.dev + o_vor), static_cast<uint32_t>(ng),
+					3u * maxS, 3u * maxS, cfg.BiomeSeed, biome_count, s));
+			}
 			STPGB_TRY(shf_launch(reinterpret_cast<ShfJob*>(sl.dev + o_shf), shf[0], static_cast<uint32_t>(ng), maxS, maxS,
 				maxR, shf_kcap_v(maxR, max_items), shf_kcap_h(maxR, max_items), s));
 			STPGB_TRY(noise_launch(reinterpret_cast<NoiseJob*>(sl.dev + o_noise), noise[0], static_cast<uint32_t>(ng),
@@ -670,6 +699,12 @@ int stpgb_server_create(const stpgb_server_config* cfg, const stpgb_raindrop_set
 	auto sv = std::make_unique<stpgb_server>();
 	sv->cfg = *cfg;
 	sv->base = *base;
+	if (cfg->BiomeSource > STPGB_BIOMES_LAYER_CHAIN) {
+		return inval("stpgb_server_create: BiomeSource must be STPGB_BIOMES_VORONOI or STPGB_BIOMES_LAYER_CHAIN");
+	}
+	if (cfg->BiomeSource == STPGB_BIOMES_LAYER_CHAIN) {
+		STPGB_TRY(layer_chain_demo(cfg->BiomeSeed, &sv->chain));
+	}
 	sv->biome_count = biome_count;
 	sv->max_items = std::min<uint32_t>(biome_count, kShfMaxItems);
 	STPGB_CUDA_TRY(cudaGetDevice(&sv->device));

@@ -47,9 +47,12 @@ def camera_walk(n, seed, rate=200.0, speed=1.0, turn_every=5.0, lods=(256, 512, 
 
 class Server:
     def __init__(self, base_setting, simplex_setting, biome_table, hbm_budget=40 << 30, max_in_flight=64,
-                 max_batch=16, streams=3, voronoi_cell=192, biome_seed=42):
+                 max_batch=16, streams=3, voronoi_cell=192, biome_seed=42, layer_chain_biomes=False):
+        """`layer_chain_biomes`: generate biomemaps with the demo's layer chain (the reference's
+        STPLayerChainBuilder) instead of the synthetic Voronoi map."""
         table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
-        cfg = ServerConfig(hbm_budget, max_in_flight, max_batch, streams, voronoi_cell, biome_seed)
+        cfg = ServerConfig(hbm_budget, max_in_flight, max_batch, streams, voronoi_cell, biome_seed,
+                           int(bool(layer_chain_biomes)))
         h = C.c_void_p()
         check(lib().stpgb_server_create(C.byref(cfg), C.byref(base_setting), C.byref(simplex_setting),
                                         table.ctypes.data_as(C.c_void_p), len(table), C.byref(h)))

@@ -38,8 +38,10 @@ def run_all(server, reqs):
     return out
 
 
-def expected_merged(oracle, stpgb, r):
-    """Pre-erosion neighbourhood of a request from the oracle (Voronoi, filter, noise)."""
+def expected_merged(oracle, stpgb, r, layer_chain=False):
+    """Pre-erosion neighbourhood of a request from the oracle (Voronoi or the demo's biome layer
+    chain, filter, noise)."""
+    from test_layers import DEMO_CHAIN, demo_ids
     S, rad = r["MapSize"], r["InterpolationRadius"]
     table = helpers.biome_table(NB, SEED)
     perm, grad = stpgb.permutation_generate(SEED, 8, 0.2181661565)
@@ -47,7 +49,10 @@ def expected_merged(oracle, stpgb, r):
     out = np.zeros((3 * S, 3 * S), np.float32)
     for c in range(9):
         kx, ky = r["ChunkX"] + c % 3 - 1, r["ChunkY"] + c // 3 - 1
-        region = oracle.voronoi(3 * S, 3 * S, ((kx - 1) * S, (ky - 1) * S), cell, NB, SEED)
+        if layer_chain:
+            region = oracle.layer_biomemap(DEMO_CHAIN, demo_ids(), SEED, 3 * S, 3 * S, ((kx - 1) * S, (ky - 1) * S))
+        else:
+            region = oracle.voronoi(3 * S, 3 * S, ((kx - 1) * S, (ky - 1) * S), cell, NB, SEED)
         rc, off, bins = oracle.shf(region, (S, S), (3, 3), rad)
         assert rc == 0
         h = oracle.multibiome(off, bins, table, perm, grad, (S, S), (float(kx * S), float(ky * S)))
@@ -68,6 +73,24 @@ def test_serve_generation_mass_balance_and_format(stpgb, dev, oracle):
         assert abs((total - h.astype(np.float64).sum()) - residual) <= 1e-5 * total, r
         assert np.array_equal(f, oracle.format(h))
         assert lat > 0.0
+    sv.close()
+
+
+def test_serve_with_layer_chain_biomes(stpgb, dev, oracle):
+    """BiomeSource = the demo's layer chain: every eroded result balances against the oracle's
+    neighbourhood built from the oracle's layer chain (biome IDs 0 / 1 / 3 in a 6-biome table),
+    and the chain's biomes differ from the Voronoi ones."""
+    reqs = [dict(r, ChunkX=x, ChunkY=y) for r, (x, y) in zip(REQS[:4], [(0, 0), (10, -7), (-25, 30), (31, 31)])]
+    sv = make_server(stpgb, layer_chain_biomes=True)
+    res = run_all(sv, reqs)
+    vor = run_all(make_server(stpgb), reqs[:1])
+    for r in reqs:
+        h, f, residual, _ = res[r["UserTag"]]
+        pre = expected_merged(oracle, stpgb, r, layer_chain=True).astype(np.float64)
+        total = pre.sum()
+        assert abs((total - h.astype(np.float64).sum()) - residual) <= 1e-5 * total, r
+        assert np.array_equal(f, oracle.format(h))
+    assert not np.allclose(vor[0][0], res[0][0])
     sv.close()
 
 
