@@ -8,18 +8,21 @@
 // count drops to zero is erased and the rest close up.  It depends on the
 // whole history of a sliding window, so each pass keeps the reference's
 // sequential slide per column (vertical pass) and per row (horizontal pass),
-// one thread per column / row, with the accumulator in shared memory; the
-// parallelism comes from the many columns and rows of many chunks at once.
+// with the accumulator in shared memory.  When few chunks are filtered at
+// once, a column / row is cut into segments that slide in parallel: each
+// segment rebuilds its first accumulator from the window's counts and, for
+// the order, the start of every present item's current run, found by one
+// sweep back (an item's place is fixed by the step that last inserted it).
 //
-//   shf_vertical   thread per column k in [0, W+2r): window of rows
-//                  [y-r, y+r] of column sx-r+k, slid down the H rows of the
-//                  central chunk (reference :522-563).  Output: ordered
-//                  (item, count) lists per (k, y) in the workspace.
-//   shf_horizontal thread per row y: window of vertical histograms of
-//                  columns [x, x+2r], slid across the W columns
-//                  (reference :608-679).  COUNT mode sums the bins of the row,
-//                  WRITE mode writes offsets and normalised bins.
-//   shf_rowscan    exclusive prefix over the row totals -> row base offsets.
+//   shf_vertical   thread per (column k in [0, W+2r), segment): window of
+//                  rows [y-r, y+r] of column sx-r+k, slid down the segment's
+//                  rows of the central chunk (reference :522-563).  Output:
+//                  ordered (item, count) lists per (k, y) in the workspace.
+//   shf_horizontal thread per (row y, segment): window of vertical histograms
+//                  of columns [x, x+2r], slid across the segment's columns
+//                  (reference :608-679).  COUNT mode sums the bins of the
+//                  segment, WRITE mode writes offsets and normalised bins.
+//   shf_rowscan    exclusive prefix over the (row, segment) totals -> bases.
 //
 // Every pixel's counts sum to (2r+1)^2, so the reference's normalisation
 // factor 1.0f / float(sum) (:495-497) is the same for every pixel.
@@ -34,6 +37,8 @@ namespace {
 constexpr uint32_t kVBlock = 64u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
+// threads the segmented passes aim for: 1024 per SM of the 152
+constexpr uint64_t kShfTargetThreads = 152u * 1024u;
 
 size_t align256(size_t v) {
 	return (v + 255u) & ~static_cast<size_t>(255u);
@@ -43,16 +48,34 @@ __device__ __forceinline__ const ShfJob& pick(const ShfJob* jobs, const ShfJob& 
 	return jobs ? jobs[blockIdx.y] : single;
 }
 
+// Flag of an accumulator entry whose run start is known (segment start).
+constexpr uint32_t kResolved = 0x80000000u;
+
+// Thread (column k, segment s) of a job: rows [s*L, min(H, s*L+L)) of column
+// sx - r + k.  Segment 0 starts as the reference does (fill rows -r..r);
+// a later segment rebuilds the accumulator of its first row: the counts of
+// the window, and the order the sequential slide would have produced.  An
+// item's place is fixed by the step that last inserted it: it stays present
+// while its occurrences in the column are at most 2r+1 rows apart (the
+// window always holds one of them; add before remove keeps a 2r+1 gap
+// joined), so the order of the present items is the order of the first
+// occurrences of their current runs (an item present from step 0 starts its
+// run at its first occurrence in rows -r..r, which orders the initial fill).
+// One upward sweep from the window finds every run start.
 __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t kcap) {
+	const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
 	const uint32_t ncols = J.W + 2u * J.r;
-	const uint32_t k = blockIdx.x * kVBlock + threadIdx.x;
-	if (k >= ncols) {
+	const uint32_t t = blockIdx.x * kVBlock + threadIdx.x;
+	const uint32_t k = t % ncols, s = t / ncols;
+	const uint32_t y_a = s * seg_len;
+	if (s >= segs || y_a >= J.H) {
 		return;
 	}
+	const uint32_t y_b = min(J.H, y_a + seg_len);
 	extern __shared__ uint32_t vsm[];
-	uint32_t* const acc = vsm + threadIdx.x; // entry j at acc[j * kVBlock]
+	uint32_t* const acc = vsm + threadIdx.x;              // entry j at acc[j * kVBlock]
+	uint32_t* const key = vsm + kcap * kVBlock + threadIdx.x; // run start of entry j (segment start)
 	uint32_t n = 0u;
 	bool overflow = false;
 
@@ -89,6 +112,10 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	};
 	const uint16_t* const col = J.samplemap + (J.sx - J.r + k);
 	const uint64_t pitch = J.pitch;
+	// sample of window row q (relative to the chunk's first row, q >= -r)
+	auto at = [&](const int q) {
+		return static_cast<uint32_t>(__ldg(col + static_cast<uint64_t>(static_cast<int64_t>(J.sy) + q) * pitch));
+	};
 	auto emit = [&](const uint32_t y) {
 		J.vn[static_cast<size_t>(y) * ncols + k] = static_cast<uint16_t>(n);
 		uint32_t* const out = J.vbuf + static_cast<size_t>(y) * kcap * ncols + k;
@@ -97,13 +124,56 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 		}
 	};
 
-	for (uint32_t row = J.sy - J.r; row <= J.sy + J.r; row++) {
-		inc(__ldg(col + row * pitch));
+	const int r = static_cast<int>(J.r);
+	if (y_a == 0u) {
+		for (int q = -r; q <= r; q++) {
+			inc(at(q));
+		}
+	} else {
+		// counts of the window, each item keyed by its topmost row in it (+r, >= 0)
+		for (int q = static_cast<int>(y_a) - r; q <= static_cast<int>(y_a) + r; q++) {
+			const uint32_t v = at(q);
+			const uint32_t before = n;
+			inc(v);
+			if (n > before) {
+				key[(n - 1u) * kVBlock] = static_cast<uint32_t>(q + r);
+			}
+		}
+		// upward sweep: extend each run while its occurrences stay within 2r+1 rows
+		uint32_t open = n;
+		for (int q = static_cast<int>(y_a) - r - 1; q >= -r && open > 0u; q--) {
+			const uint32_t v = at(q), qk = static_cast<uint32_t>(q + r);
+			for (uint32_t j = 0u; j < n; j++) {
+				const uint32_t kj = key[j * kVBlock];
+				if (kj & kResolved) {
+					continue;
+				}
+				if (kj - qk >= 2u * J.r + 2u) {
+					// 2r+1 rows without the item: an earlier occurrence starts another run
+					key[j * kVBlock] = kj | kResolved;
+					open--;
+				} else if ((acc[j * kVBlock] >> 16) == v) {
+					key[j * kVBlock] = qk;
+				}
+			}
+		}
+		// order by run start (insertion sort, entries are few)
+		for (uint32_t j = 1u; j < n; j++) {
+			const uint32_t e = acc[j * kVBlock], kj = key[j * kVBlock] & ~kResolved;
+			uint32_t m = j;
+			while (m > 0u && (key[(m - 1u) * kVBlock] & ~kResolved) > kj) {
+				acc[m * kVBlock] = acc[(m - 1u) * kVBlock];
+				key[m * kVBlock] = key[(m - 1u) * kVBlock];
+				m--;
+			}
+			acc[m * kVBlock] = e;
+			key[m * kVBlock] = kj;
+		}
 	}
-	emit(0u);
-	for (uint32_t y = 1u; y < J.H; y++) {
-		inc(__ldg(col + static_cast<uint64_t>(J.sy + y + J.r) * pitch));
-		dec(__ldg(col + static_cast<uint64_t>(J.sy + y - 1u - J.r) * pitch));
+	emit(y_a);
+	for (uint32_t y = y_a + 1u; y < y_b; y++) {
+		inc(at(static_cast<int>(y) + r));
+		dec(at(static_cast<int>(y) - 1 - r));
 		emit(y);
 	}
 	if (overflow) {
@@ -111,17 +181,33 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	}
 }
 
+// Thread (row y, segment s): output columns [s*L, min(W, s*L+L)).  A later
+// segment rebuilds its first accumulator as the vertical pass does, over
+// columns of vertical histograms: an item stays present while the columns
+// holding it are at most 2r+1 apart, and the items a step adds enter in the
+// order of the added column's histogram, so the order is by (first column of
+// the item's current run, its place in that column's histogram).
 template<bool Write>
 __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t kcap_v, const uint32_t kcap) {
+	const uint32_t kcap_v, const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
-	const uint32_t y = blockIdx.x * kHBlock + threadIdx.x;
-	if (y >= J.H) {
+	const uint32_t t = blockIdx.x * kHBlock + threadIdx.x;
+	const uint32_t y = t % J.H, s = t / J.H;
+	const uint32_t x_a = s * seg_len;
+	if (s >= segs) {
 		return;
 	}
+	if (x_a >= J.W) {
+		if constexpr (!Write) {
+			J.rows[static_cast<size_t>(y) * segs + s] = 0u; // a segment past this job's width
+		}
+		return;
+	}
+	const uint32_t x_b = min(J.W, x_a + seg_len);
 	extern __shared__ uint32_t hsm[];
-	uint32_t* const cnt = hsm + threadIdx.x;                                           // [kcap][kHBlock]
-	uint16_t* const item = reinterpret_cast<uint16_t*>(hsm + kcap * kHBlock) + threadIdx.x; // [kcap][kHBlock]
+	uint32_t* const cnt = hsm + threadIdx.x;                                               // [kcap][kHBlock]
+	uint32_t* const key = hsm + kcap * kHBlock + threadIdx.x;                              // [kcap][kHBlock]
+	uint16_t* const item = reinterpret_cast<uint16_t*>(hsm + 2u * kcap * kHBlock) + threadIdx.x; // [kcap][kHBlock]
 	uint32_t n = 0u;
 	bool overflow = false;
 
@@ -175,8 +261,66 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	};
 
 	const uint32_t side = 2u * J.r + 1u;
+	if (x_a == 0u) {
+		for (uint32_t kc = 0u; kc < side; kc++) {
+			add_col(kc);
+		}
+	} else {
+		// counts of the window, each item keyed by (first column, place in its histogram)
+		for (uint32_t kc = x_a; kc < x_a + side; kc++) {
+			const uint32_t nv = vn[kc];
+			for (uint32_t j = 0u; j < nv; j++) {
+				const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+				const uint32_t before = n;
+				inc(e >> 16, e & 0xFFFFu);
+				if (n > before) {
+					key[(n - 1u) * kHBlock] = (kc << 12) | j;
+				}
+			}
+		}
+		// leftward sweep: extend each run while its columns stay within 2r+1
+		uint32_t open = n;
+		for (int kc = static_cast<int>(x_a) - 1; kc >= 0 && open > 0u; kc--) {
+			const uint32_t nv = vn[kc];
+			for (uint32_t i = 0u; i < n; i++) {
+				const uint32_t ki = key[i * kHBlock];
+				if (ki & kResolved) {
+					continue;
+				}
+				if ((ki >> 12) - static_cast<uint32_t>(kc) >= 2u * J.r + 2u) {
+					// 2r+1 columns without the item: an earlier one starts another run
+					key[i * kHBlock] = ki | kResolved;
+					open--;
+					continue;
+				}
+				const uint32_t v = item[i * kHBlock];
+				for (uint32_t j = 0u; j < nv; j++) {
+					if ((vrow[static_cast<size_t>(j) * ncols + kc] >> 16) == v) {
+						key[i * kHBlock] = (static_cast<uint32_t>(kc) << 12) | j;
+						break;
+					}
+				}
+			}
+		}
+		for (uint32_t j = 1u; j < n; j++) {
+			const uint16_t v = item[j * kHBlock];
+			const uint32_t c = cnt[j * kHBlock], kj = key[j * kHBlock] & ~kResolved;
+			uint32_t m = j;
+			while (m > 0u && (key[(m - 1u) * kHBlock] & ~kResolved) > kj) {
+				item[m * kHBlock] = item[(m - 1u) * kHBlock];
+				cnt[m * kHBlock] = cnt[(m - 1u) * kHBlock];
+				key[m * kHBlock] = key[(m - 1u) * kHBlock];
+				m--;
+			}
+			item[m * kHBlock] = v;
+			cnt[m * kHBlock] = c;
+			key[m * kHBlock] = kj;
+		}
+	}
+
 	const float norm = 1.0f / static_cast<float>(side * side);
-	uint64_t running = Write ? J.rows[y] : 0u;
+	const size_t slot = static_cast<size_t>(y) * segs + s;
+	uint64_t running = Write ? J.rows[slot] : 0u;
 	uint32_t* const off_row = J.offsets + static_cast<size_t>(y) * J.W;
 	uint2* const bins = reinterpret_cast<uint2*>(J.bins);
 	auto emit = [&](const uint32_t x) {
@@ -193,27 +337,26 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 		running += n;
 	};
 
-	for (uint32_t kc = 0u; kc < side; kc++) {
-		add_col(kc);
-	}
-	emit(0u);
-	for (uint32_t x = 1u; x < J.W; x++) {
+	emit(x_a);
+	for (uint32_t x = x_a + 1u; x < x_b; x++) {
 		add_col(x + 2u * J.r);
 		sub_col(x - 1u);
 		emit(x);
 	}
 	if constexpr (!Write) {
-		J.rows[y] = static_cast<uint32_t>(min(running, static_cast<uint64_t>(0xFFFFFFFFu)));
+		J.rows[slot] = static_cast<uint32_t>(min(running, static_cast<uint64_t>(0xFFFFFFFFu)));
 	}
 	if (overflow) {
 		atomicOr(J.status, STATUS_CAPACITY);
 	}
 }
 
-// One block per job: rows[0..H) -> exclusive prefix, rows[H] = total;
-// offsets[W*H] = total.
-__global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restrict__ jobs, const ShfJob single) {
+// One block per job: rows[0..H*segs) (row-major over row, segment) ->
+// exclusive prefix, rows[H*segs] = total; offsets[W*H] = total.
+__global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restrict__ jobs, const ShfJob single,
+	const uint32_t segs) {
 	const ShfJob& J = pick(jobs, single);
+	const uint32_t slots = J.H * segs;
 	__shared__ uint64_t warp_sum[kScanBlock / 32u];
 	__shared__ uint64_t carry_s;
 	if (threadIdx.x == 0u) {
@@ -221,9 +364,9 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 	}
 	__syncthreads();
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-	for (uint32_t base = 0u; base < J.H; base += kScanBlock) {
+	for (uint32_t base = 0u; base < slots; base += kScanBlock) {
 		const uint32_t i = base + threadIdx.x;
-		const uint64_t v = i < J.H ? J.rows[i] : 0u;
+		const uint64_t v = i < slots ? J.rows[i] : 0u;
 		uint64_t s = v;
 #pragma unroll
 		for (uint32_t d = 1u; d < 32u; d <<= 1) {
@@ -242,7 +385,7 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 		}
 		const uint64_t carry = carry_s;
 		const uint64_t excl = carry + wbase + s - v;
-		if (i < J.H) {
+		if (i < slots) {
 			J.rows[i] = static_cast<uint32_t>(min(excl, static_cast<uint64_t>(0xFFFFFFFFu)));
 		}
 		__syncthreads();
@@ -253,7 +396,7 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 	}
 	if (threadIdx.x == 0u) {
 		const uint64_t total = carry_s;
-		J.rows[J.H] = static_cast<uint32_t>(min(total, static_cast<uint64_t>(0xFFFFFFFFu)));
+		J.rows[slots] = static_cast<uint32_t>(min(total, static_cast<uint64_t>(0xFFFFFFFFu)));
 		J.offsets[static_cast<size_t>(J.W) * J.H] = static_cast<uint32_t>(min(total, static_cast<uint64_t>(0xFFFFFFFFu)));
 		if (total > J.bins_capacity || total > 0xFFFFFFFFull) {
 			atomicOr(J.status, STATUS_CAPACITY);
@@ -283,7 +426,7 @@ ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
 	l.vbuf = 0u;
 	l.vn = align256(static_cast<size_t>(H) * kcap_v * ncols * sizeof(uint32_t));
 	l.rows = l.vn + align256(static_cast<size_t>(H) * ncols * sizeof(uint16_t));
-	l.total = l.rows + align256((static_cast<size_t>(H) + 1u) * sizeof(uint32_t));
+	l.total = l.rows + align256((static_cast<size_t>(H) * kShfMaxSegments + 1u) * sizeof(uint32_t));
 	return l;
 }
 
@@ -295,17 +438,32 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 		g_attr_set = true;
 	}
-	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * sizeof(uint32_t);
-	const size_t hsmem = static_cast<size_t>(kcap_h) * kHBlock * (sizeof(uint32_t) + sizeof(uint16_t));
-	const dim3 vgrid((max_W + 2u * max_r + kVBlock - 1u) / kVBlock, njobs);
-	const dim3 hgrid((max_H + kHBlock - 1u) / kHBlock, njobs);
-	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v);
+	// Segments per column / row: enough threads to fill the GPU when few
+	// chunks are filtered at once, none while the launch already has a
+	// quarter of that (a segment start sweeps back to the start of every run:
+	// on the 16-request production batch, 2-3 segments made the filter 40 %
+	// slower; on one chunk, 16 make it several times faster).
+	const uint64_t ncols = static_cast<uint64_t>(max_W) + 2u * max_r;
+	auto segments = [&](const uint64_t lanes, const uint32_t len) {
+		const uint64_t want = (kShfTargetThreads + lanes * njobs - 1u) / (lanes * njobs);
+		if (want < 4u) {
+			return 1u;
+		}
+		return static_cast<uint32_t>(std::min<uint64_t>({ want, uint64_t(kShfMaxSegments), uint64_t(len) }));
+	};
+	const uint32_t segs_v = segments(ncols, max_H), segs_h = segments(max_H, max_W);
+	const uint32_t len_v = (max_H + segs_v - 1u) / segs_v, len_h = (max_W + segs_h - 1u) / segs_h;
+	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * 2u * sizeof(uint32_t);
+	const size_t hsmem = static_cast<size_t>(kcap_h) * kHBlock * (2u * sizeof(uint32_t) + sizeof(uint16_t));
+	const dim3 vgrid(static_cast<uint32_t>((ncols * segs_v + kVBlock - 1u) / kVBlock), njobs);
+	const dim3 hgrid(static_cast<uint32_t>((static_cast<uint64_t>(max_H) * segs_h + kHBlock - 1u) / kHBlock), njobs);
+	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v, segs_v, len_v);
 	STPGB_CUDA_TRY(cudaGetLastError());
-	shf_horizontal<false><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h);
+	shf_horizontal<false><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
 	STPGB_CUDA_TRY(cudaGetLastError());
-	shf_rowscan<<<dim3(1u, njobs), kScanBlock, 0, stream>>>(jobs, single);
+	shf_rowscan<<<dim3(1u, njobs), kScanBlock, 0, stream>>>(jobs, single, segs_h);
 	STPGB_CUDA_TRY(cudaGetLastError());
-	shf_horizontal<true><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h);
+	shf_horizontal<true><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }

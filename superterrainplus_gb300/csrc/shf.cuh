@@ -10,6 +10,10 @@ namespace stpgb {
 // window; it sizes the per-thread accumulators in shared memory.
 constexpr uint32_t kShfMaxItems = 256u;
 
+// Most segments a column (vertical pass) or row (horizontal pass) is cut
+// into; the workspace holds one bin count per (row, segment).
+constexpr uint32_t kShfMaxSegments = 16u;
+
 // One filter invocation over one chunk.  `samplemap` points at the top-left
 // pixel of the chunk's nearest-neighbour region (TotalMapSize), rows `pitch`
 // elements apart; the central chunk starts at (sx, sy).
@@ -21,7 +25,7 @@ struct ShfJob {
 	// workspace
 	uint32_t* vbuf;  // [H][kcap_v][W+2r] packed (item << 16 | count)
 	uint16_t* vn;    // [H][W+2r] entries per vertical histogram
-	uint32_t* rows;  // [H+1] bins per output row, then exclusive prefix + total
+	uint32_t* rows;  // [H*segments+1] bins per (row, segment), then exclusive prefix + total
 	// output
 	uint32_t* offsets;  // [W*H+1]
 	stpgb_bin* bins;
