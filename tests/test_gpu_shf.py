@@ -98,3 +98,23 @@ def test_shf_host_api_matches(stpgb, dev, oracle):
         assert np.array_equal(off, kat["offsets"])
         assert np.array_equal(bins["Item"], kat["items"])
         assert np.array_equal(bins["Weight"].view(np.uint32), kat["weights"].view(np.uint32))
+
+
+@pytest.mark.parametrize("radius", [2, 4, 8])
+def test_shf_run_boundaries_across_segments(dev, oracle, radius):
+    """One chunk filtered alone runs in segments that rebuild their starting order from the rule that
+    occurrences at most 2r+1 apart keep an item present.  Here items recur exactly 2r+1 and 2r+2
+    rows / columns apart (joined and split runs), several interleaved with phase shifts, over a
+    64x96 chunk, so segment starts fall inside both kinds of gap; the result must be the oracle's."""
+    S_x, S_y = 64, 96
+    H, W = 3 * S_y, 3 * S_x
+    y, x = np.mgrid[0:H, 0:W]
+    sm = np.zeros((H, W), np.uint16)
+    for item, (period, phase) in enumerate([(2 * radius + 1, 0), (2 * radius + 2, 3), (2 * radius + 1, 5),
+                                            (4 * radius + 3, 1), (2 * radius + 2, 7)], start=1):
+        sm[(y + phase) % period == 0] = item
+        sm[((x + 2 * phase) % (period + 1) == 0) & (y % 3 == item % 3)] = item + 10
+    got = run_gpu(dev, sm, (S_x, S_y), (3, 3), radius)
+    rc, off, bins = oracle.shf(sm, (S_x, S_y), (3, 3), radius)
+    assert rc == 0
+    assert_same(got, (off, bins["Item"], bins["Weight"]), f"r={radius}")
