@@ -85,6 +85,17 @@ def requests(batch, rank):
                  DropletCount=DROPLETS, BrushRadius=BRUSH, Lifetime=LIFETIME) for n in range(batch)]
 
 
+def max_over_ranks(value, dist, device):
+    """The largest value over the ranks (the slowest replica's elapsed time); `dist` is
+    torch.distributed after init_process_group, or None for one process."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -254,10 +265,7 @@ def run_ours(args):
     batch.status(sh)
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1000.0
-    if dist:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, dist, "cuda")
     value = world * B * args.steps / elapsed
 
     # per-stage device time (stage kernels launched alone, CUDA events on the launching stream)
