@@ -516,6 +516,12 @@ STPGB_API int stpgb_batch_buffers(stpgb_batch* batch, uint32_t request, uint16_t
 STPGB_API int stpgb_batch_synthesize_inputs(stpgb_batch* batch, uint32_t voronoi_cell, uint64_t seed,
 	void* stream);
 
+/* Replaces every request's biome region with the demo's biome layer chain
+ * (stpgb_layer_chain_demo, demo IDs, `seed`), as the reference's world
+ * pipeline generates biomemaps; call after stpgb_batch_synthesize_inputs
+ * (which also makes the starts).  The biome table must cover IDs 0, 1, 3. */
+STPGB_API int stpgb_batch_synthesize_layer_biomes(stpgb_batch* batch, uint64_t seed, void* stream);
+
 /* Runs the whole batch (graph launch when captured). Asynchronous. */
 STPGB_API int stpgb_batch_run(stpgb_batch* batch, void* stream);
 

@@ -306,6 +306,10 @@ class Batch:
     def synthesize(self, voronoi_cell, seed, stream=None):
         check(lib().stpgb_batch_synthesize_inputs(self._h, voronoi_cell, seed, self._s(stream)))
 
+    def synthesize_layer_biomes(self, seed, stream=None):
+        """Biome regions from the demo's layer chain (after synthesize(), which makes the starts)."""
+        check(lib().stpgb_batch_synthesize_layer_biomes(self._h, seed, self._s(stream)))
+
     def run(self, stream=None):
         check(lib().stpgb_batch_run(self._h, self._s(stream)))
 

@@ -196,6 +196,7 @@ PROTOTYPES = {
     "stpgb_batch_device_bytes": (u64, [vp]),
     "stpgb_batch_buffers": (C.c_int, [vp, u32, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "stpgb_batch_synthesize_inputs": (C.c_int, [vp, u32, u64, vp]),
+    "stpgb_batch_synthesize_layer_biomes": (C.c_int, [vp, u64, vp]),
     "stpgb_batch_run": (C.c_int, [vp, vp]),
     "stpgb_batch_run_plain": (C.c_int, [vp, vp]),
     "stpgb_batch_upload": (C.c_int, [vp, vp, vp, vp]),

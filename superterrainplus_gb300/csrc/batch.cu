@@ -15,6 +15,7 @@
 // No merge/unmerge copies are needed: a chunk's filter input is a window of
 // the biome region and its heightmap a window of the merged map.
 #include "erosion.cuh"
+#include "layers.cuh"
 #include "noise.cuh"
 #include "shf.cuh"
 
@@ -518,6 +519,28 @@ int stpgb_batch_synthesize_inputs(stpgb_batch* b, uint32_t voronoi_cell, uint64_
 			^ (static_cast<uint64_t>(static_cast<uint32_t>(r.ChunkY)) << 20);
 		STPGB_TRY(starts_launch(reinterpret_cast<float*>(b->mem + L.starts), r.DropletCount, b->base.Seed, base, S, S,
 			3u, 3u, s));
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_synthesize_layer_biomes(stpgb_batch* b, uint64_t seed, void* stream) {
+	if (!b) {
+		return inval("stpgb_batch_synthesize_layer_biomes: null batch");
+	}
+	LayerChain chain;
+	STPGB_TRY(layer_chain_demo(seed, &chain));
+	const cudaStream_t s = as_stream(stream);
+	for (size_t n = 0; n < b->req.size(); n++) {
+		const auto& r = b->req[n];
+		const uint32_t S = r.MapSize;
+		BiomemapJob job {};
+		job.out = reinterpret_cast<uint16_t*>(b->mem + b->layout[n].biome);
+		job.x0 = static_cast<int32_t>((static_cast<int64_t>(r.ChunkX) - 2) * S);
+		job.z0 = static_cast<int32_t>((static_cast<int64_t>(r.ChunkY) - 2) * S);
+		job.pitch = job.width = job.height = 5u * S;
+		const uint32_t tile = layer_tile(chain, 25ull * S * S);
+		STPGB_TRY(layer_job_tiling(job, tile));
+		STPGB_TRY(layer_biomemap_launch(chain, nullptr, job, 1u, job.tiles, tile, s));
 	}
 	return STPGB_OK;
 }

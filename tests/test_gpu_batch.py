@@ -103,3 +103,27 @@ def test_batch_budget_refusal(stpgb):
     simplex = stpgb.SimplexSetting(5, 8, 0.2181661565)
     with pytest.raises(stpgb.STPInsufficientMemory):
         stpgb.Batch(REQS, base, simplex, helpers.biome_table(NB, 5), hbm_budget=1 << 20)
+
+
+def test_batch_with_layer_chain_biomes(stpgb, dev, oracle):
+    """Biome regions from the demo's layer chain are the oracle's chain, bit for bit, and the batch
+    erodes them with the mass balance kept."""
+    from test_layers import DEMO_CHAIN, demo_ids
+    b, _ = make_batch(stpgb)
+    b.synthesize_layer_biomes(23)
+    regions = [np.zeros((5 * r["MapSize"], 5 * r["MapSize"]), np.uint16) for r in REQS]
+    b.download_inputs(regions)
+    b.status()
+    for r, reg in zip(REQS, regions):
+        S = r["MapSize"]
+        want = oracle.layer_biomemap(DEMO_CHAIN, demo_ids(), 23, 5 * S, 5 * S, ((r["ChunkX"] - 2) * S,
+                                                                                 (r["ChunkY"] - 2) * S))
+        assert np.array_equal(reg, want)
+    b.run_stage(0)
+    b.run_stage(1)
+    before, _, _ = heights(b)
+    b.run()
+    after, fixed, res = heights(b)
+    for n in range(len(REQS)):
+        t0 = before[n].astype(np.float64).sum()
+        assert abs((t0 - after[n].astype(np.float64).sum()) - res[n]) <= 1e-5 * t0
