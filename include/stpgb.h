@@ -239,7 +239,12 @@ STPGB_API int stpgb_droplet_starts(float* starts_xy, uint32_t count, uint64_t se
  * may be NULL) accumulates the sediment that left with dying droplets, so
  * that sum(h_before) - sum(h_after) == *residual_sediment up to rounding.
  * `status` (device uint32, may be NULL) reports a droplet that hit the step
- * cap.  Asynchronous on `stream`. */
+ * cap.  A brush point removes min(max(cell, 0), w) where the reference
+ * removes min(cell, w) (STPRainDrop.cu:149): the same on every non-negative
+ * cell, which is every cell of a map that starts non-negative unless racing
+ * droplets take one below zero; there the reference's form gives the
+ * negative height back once per racing reader, which grows without bound in
+ * dense channels.  Asynchronous on `stream`. */
 STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
 	const stpgb_raindrop_setting* setting, const float* starts_xy, uint32_t count,
 	const int32_t* brush_index, const float* brush_weight, uint32_t brush_size,

@@ -83,6 +83,7 @@ struct stpgb_batch {
 	// most rows_limit lanes: rows_max_lanes() of the smallest brush
 	bool rows = true;
 	uint32_t rows_limit = 4u;
+	uint32_t min_radius = 0xFFFFFFFFu; // smallest brush radius of the batch
 	// largest droplet density (droplets per centre-chunk pixel) of the batch;
 	// the autotuner only tries the variants stable at this density
 	double density = 0.0;
@@ -160,7 +161,7 @@ struct stpgb_batch {
 				table, biome_count, s);
 		case 2u:
 			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
-				false, dpg, rows);
+				false, dpg, rows, erosion_rows_paired(min_radius, density));
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -248,7 +249,8 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows,
+				erosion_rows_paired(min_radius, density)));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -329,6 +331,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		b->max_brush = std::max(b->max_brush, bs);
 		b->lane_limit = std::min(b->lane_limit, max_lanes(bs));
 		b->rows_limit = std::min(b->rows_limit, rows_max_lanes(r.BrushRadius));
+		b->min_radius = std::min(b->min_radius, r.BrushRadius);
 		b->density = std::max(b->density, static_cast<double>(r.DropletCount) / (static_cast<double>(S) * S));
 		// the default until the autotuner runs: brush rows where stable, else
 		// several lanes point by point, above kDenseRows the reference kernel

@@ -25,6 +25,19 @@ namespace {
 
 constexpr uint32_t kErodeBlock = 128u;
 
+// Every brush update subtracts min(max(cell, 0), w) where the reference
+// subtracts min(cell, w) (STPRainDrop.cu:149).  The two agree on every
+// non-negative cell, and without concurrent droplets no cell goes negative:
+// the maps start non-negative (normalised noise), deposits add, and an
+// erosion removes at most what the cell holds.  Concurrent droplets that read
+// the same cell before either update lands can take it below zero; the
+// reference's min() then returns the negative height, so each droplet that
+// read it adds its magnitude back, and with three or more such readers the
+// magnitude grows every round: measured on 64^2 chunks of multi-biome
+// terrain, 2.7 to 3 droplets per pixel with brush radius 3 drove heights to
+// -10^5 and beyond in some runs.  With the clamp a negative cell is left to
+// the deposits, and no feedback remains.
+
 struct HG {
 	float h, gx, gy;
 };
@@ -156,13 +169,14 @@ __global__ void __launch_bounds__(kErodeBlock) erosion_kernel(const ErosionJob* 
 				if constexpr (!ExactClamp) {
 					// The reference's order (STPRainDrop.cu:146-157): read the
 					// cell, subtract min(cell, w), then the next point; the next
-					// read stays behind the previous atomic.
+					// read stays behind the previous atomic.  The amount is
+					// clamped at 0, as noted at kErodeBlock.
 #pragma unroll 1
 					for (uint32_t p = g; p < bsize; p += G) {
 						float* const cell = map + static_cast<int64_t>(mi) + bidx[p];
 						const float we = ero * bw[p];
 						const float cur = __ldcg(cell);
-						const float ds = (cur < we) ? cur : we;
+						const float ds = fminf(fmaxf(cur, 0.0f), we);
 						atomicAdd(cell, -ds);
 						part += ds;
 						asm volatile("" ::: "memory");
@@ -462,7 +476,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 1) erosion_multi_ke
 				for (uint32_t k = 0u; k < K; k++) {
 					if (erode[k] && (!serial || k == turn)) {
 						const float we = ero[k] * wp;
-						const float ds = (cur[k] < we) ? cur[k] : we;
+						const float ds = fminf(fmaxf(cur[k], 0.0f), we);
 						atomicAdd(map + static_cast<int64_t>(mi[k]) + off, -ds);
 						part[k] += ds;
 					}
@@ -540,12 +554,13 @@ __device__ __forceinline__ void red_add_v4(float4* addr, const float a, const fl
 // of one of each per point.  Needs a 16-byte aligned map whose pitch is a
 // multiple of four floats, so that no block leaves its row.
 // Residency bounds this chain-latency kernel more than the spilled registers
-// do: 10 blocks of 128 threads (48 registers) with one droplet per group,
-// 8 (64 registers) with two (measured: fewer, larger-register blocks, or 12
-// blocks of 40 registers, are slower).
+// do: 9 blocks of 128 threads (56 registers) with one droplet per group,
+// 8 (64 registers) with two (measured: 10 blocks of 48 registers are 1 %
+// slower with two blocks per round trip, 12 blocks of 40 registers slower
+// still).
 template<uint32_t G, uint32_t K>
-__global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
-	const ErosionJob single) {
+__global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
+	const ErosionJob single, const uint32_t trip) {
 	static_assert((G == 2u || G == 4u) && (K == 1u || K == 2u), "2 or 4 lanes, 1 or 2 droplets");
 	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
 	extern __shared__ unsigned char esm[];
@@ -767,31 +782,41 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 10) erosion_rows_ke
 						nmax = max(nmax, nb[k]);
 					}
 				}
+				// `trip` (1 or 2) blocks per round trip: a run's blocks are
+				// distinct cells, so reading the second before the first one's
+				// update changes nothing for this droplet
 #pragma unroll 1
-				for (int32_t b = 0; b < nmax; b++) {
-					float4 cur[K];
+				for (int32_t b0 = 0; b0 < nmax; b0 += static_cast<int32_t>(trip)) {
+					float4 cur[K][2];
 #pragma unroll
 					for (uint32_t k = 0u; k < K; k++) {
-						if (b < nb[k]) {
-							cur[k] = __ldcg(blk[k] + b);
+#pragma unroll
+						for (int32_t u = 0; u < 2; u++) {
+							if ((u == 0 || trip == 2u) && b0 + u < nb[k]) {
+								cur[k][u] = __ldcg(blk[k] + b0 + u);
+							}
 						}
 					}
 #pragma unroll
 					for (uint32_t k = 0u; k < K; k++) {
-						if (b < nb[k]) {
-							float c[4] = { cur[k].x, cur[k].y, cur[k].z, cur[k].w }, d[4];
 #pragma unroll
-							for (int i = 0; i < 4; i++) {
-								const int32_t j = 4 * b + i - lead[k];
-								d[i] = -0.0f;
-								if (j >= 0 && j < R.len) {
-									const float we = ero[k] * bw[R.first + j];
-									const float ds = (c[i] < we) ? c[i] : we;
-									d[i] = -ds;
-									part[k] += ds;
+						for (int32_t u = 0; u < 2; u++) {
+							const int32_t b = b0 + u;
+							if ((u == 0 || trip == 2u) && b < nb[k]) {
+								float c[4] = { cur[k][u].x, cur[k][u].y, cur[k][u].z, cur[k][u].w }, d[4];
+#pragma unroll
+								for (int i = 0; i < 4; i++) {
+									const int32_t j = 4 * b + i - lead[k];
+									d[i] = -0.0f;
+									if (j >= 0 && j < R.len) {
+										const float we = ero[k] * bw[R.first + j];
+										const float ds = fminf(fmaxf(c[i], 0.0f), we);
+										d[i] = -ds;
+										part[k] += ds;
+									}
 								}
+								red_add_v4(blk[k] + b, d[0], d[1], d[2], d[3]);
 							}
-							red_add_v4(blk[k] + b, d[0], d[1], d[2], d[3]);
 						}
 					}
 				}
@@ -942,11 +967,13 @@ uint32_t rows_max_lanes(uint32_t radius) {
 
 // Stability envelope of the kernel variants against droplet density (droplets
 // per pixel of the area the starts cover), measured on a 64^2 chunk of
-// multi-biome terrain with brushes 3 and 4: at 2.3 every variant stays in
-// range; at 3.5 brush 3 with four row lanes runs away; at 4.9 four lanes point
-// by point run away in some runs and not in others; one lane per droplet (the
-// reference kernel) holds at 7.  Above kDenseRows only the reference kernel is
-// used.
+// multi-biome terrain with brushes 3 and 4, ten runs each, the lowest height
+// against the map's lowest start height: with the brush amount clamped at
+// zero every row variant (one block per round trip) stays in range up to 3.5,
+// and falls up to 0.1 below it at 7 (brush 3, four lanes); without the clamp
+// brush 3 ran away to -10^5 at 2.7 to 3.  Four lanes point by point went out
+// of range at 4.9 in some runs; one lane per droplet (the reference kernel)
+// holds at 7.  Above kDenseRows only the reference kernel is used.
 bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_group, const bool rows,
 	const double density) {
 	(void)droplets_per_group;
@@ -954,16 +981,20 @@ bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_gr
 	return lanes == 1u || density <= kDenseRows;
 }
 
+bool erosion_rows_paired(const uint32_t min_radius, const double density) {
+	return min_radius >= kPairedMinRadius && density <= kDenseRows;
+}
+
 ErosionChoice erosion_choice(const uint32_t radius, const uint32_t brush_size, const double density,
 	const bool rows_allowed) {
 	if (density > kDenseRows) {
-		return ErosionChoice { 1u, 1u, false };
+		return ErosionChoice { 1u, 1u, false, false };
 	}
 	const uint32_t rl = rows_max_lanes(radius);
 	if (rows_allowed && rl != 0u) {
-		return ErosionChoice { rl, 1u, true };
+		return ErosionChoice { rl, 1u, true, erosion_rows_paired(radius, density) };
 	}
-	return ErosionChoice { default_lanes(brush_size), 1u, false };
+	return ErosionChoice { default_lanes(brush_size), 1u, false, false };
 }
 
 RainParams rain_params(const stpgb_raindrop_setting& s) {
@@ -995,7 +1026,7 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp,
-	uint32_t droplets_per_group, bool vector_rows) {
+	uint32_t droplets_per_group, bool vector_rows, bool paired_blocks) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
@@ -1014,7 +1045,7 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 				STPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 					static_cast<int>(rsmem)));
 			}
-			kernel<<<rgrid, kErodeBlock, rsmem, stream>>>(jobs, single);
+			kernel<<<rgrid, kErodeBlock, rsmem, stream>>>(jobs, single, paired_blocks ? 2u : 1u);
 			STPGB_CUDA_TRY(cudaGetLastError());
 			return STPGB_OK;
 		};
@@ -1173,13 +1204,14 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	bool rows = !exact && (flags & STPGB_EROSION_POINTWISE) == 0u
 		&& (reinterpret_cast<uintptr_t>(heightmap) & 15u) == 0u && (dx & 3u) == 0u;
 	uint32_t lanes = lanes_per_droplet, dpg = droplets_per_group == 0u ? 1u : droplets_per_group;
+	const double density = static_cast<double>(count) / (static_cast<double>(nn->MapSize[0]) * nn->MapSize[1]);
 	if (lanes == 0u) {
-		const double density = static_cast<double>(count) / (static_cast<double>(nn->MapSize[0]) * nn->MapSize[1]);
 		const ErosionChoice c = erosion_choice(setting->ErosionBrushRadius, brush_size, density, rows);
 		lanes = c.lanes;
 		rows = c.rows;
 	}
-	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), lanes, exact, dpg, rows);
+	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), lanes, exact, dpg, rows,
+		erosion_rows_paired(setting->ErosionBrushRadius, density));
 }
 
 int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area, uint32_t* lanes_per_droplet,

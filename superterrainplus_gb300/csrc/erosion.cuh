@@ -40,10 +40,11 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 // 4, 8 or 16 lanes (reference order only);
 // vector_rows: with 2 or 4 lanes and 1 or 2 droplets per group, update the
 // brush run by run in 16-byte blocks (every map 16-byte aligned, pitch a
-// multiple of four floats)
+// multiple of four floats);
+// paired_blocks: with vector_rows, read two blocks of a run per round trip
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
-	uint32_t droplets_per_group = 1u, bool vector_rows = false);
+	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool paired_blocks = false);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).
@@ -54,17 +55,23 @@ uint32_t default_lanes(uint32_t brush_size);
 // lane in the brush-row update of the circular brush of `radius`; 0 if none.
 uint32_t rows_max_lanes(uint32_t radius);
 
-// Racing droplets that share cells can dig a channel far below its
-// neighbours once they are packed densely enough; how densely depends on how
-// compressed in time a droplet's brush update is.  Up to kDenseRows droplets
-// per pixel of the start area every variant stays stable; beyond it only one
-// lane per droplet (the reference kernel) is used.
+// Racing droplets that share cells can dig a channel below its neighbours
+// once they are packed densely enough; how densely depends on how compressed
+// in time a droplet's brush update is.  Up to kDenseRows droplets per pixel
+// of the start area every variant stays in range; beyond it only one lane per
+// droplet (the reference kernel) is used.
 constexpr double kDenseRows = 3.0;
 bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density);
 
+// Two brush blocks per round trip compress the update further: in range up to
+// kDenseRows with brush radius 4 and above, not with radius 3 beyond 2.3
+// droplets per pixel, so only brushes from kPairedMinRadius use them.
+constexpr uint32_t kPairedMinRadius = 4u;
+bool erosion_rows_paired(uint32_t min_radius, double density);
+
 struct ErosionChoice {
 	uint32_t lanes, droplets_per_group;
-	bool rows;
+	bool rows, paired;
 };
 // Default kernel for a brush of `radius` (`brush_size` points) at `density`.
 ErosionChoice erosion_choice(uint32_t radius, uint32_t brush_size, double density, bool rows_allowed);

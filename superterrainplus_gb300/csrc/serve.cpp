@@ -629,7 +629,7 @@ struct stpgb_server {
 		const uint32_t dpg = erosion_variant_stable(ec.lanes, 2u, ec.rows, maxDensity)
 			&& (ec.rows || ec.lanes >= 4u) ? 2u : 1u;
 		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
-			maxBrush, s, ec.lanes, false, dpg, ec.rows));
+			maxBrush, s, ec.lanes, false, dpg, ec.rows, ec.paired));
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
 		STPGB_CUDA_TRY(cudaMemcpyAsync(it.residual_host, res_dev, nr * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -173,6 +173,25 @@ def test_default_choice_stays_physical_when_densely_packed(dev, oracle, stpgb, b
         assert abs((total - out.sum()) - res) <= 1e-5 * total
 
 
+@pytest.mark.parametrize("brush,lanes,droplets_per_group", [(3, 0, 1), (4, 0, 1), (3, 4, 2), (4, 2, 2)])
+def test_rows_stay_physical_at_the_dense_limit(dev, oracle, stpgb, brush, lanes, droplets_per_group):
+    """At 3 droplets per pixel, the densest load the brush-row kernels take (the default choice,
+    two blocks per round trip from brush radius 4, and explicit row variants), the heights stay
+    in range in every run.  Without the brush amount clamped at zero, brush 3 drove heights to
+    -10^5 here: racing readers of one cell took it below zero, and every reader then added the
+    negative height's magnitude back."""
+    S = 64
+    h = helpers.multibiome_terrain(oracle, stpgb, S, 6, 20, 11)
+    count = int(round(3.0 * S * S))
+    s = helpers.raindrop_dict(count, radius=brush, lifetime=30, seed=11)
+    starts = oracle.droplet_starts(count, 11, 0, (S, S), (3, 3))
+    total = h.astype(np.float64).sum()
+    for out, res in erode_runs(dev, stpgb, h, (S, S), (3, 3), s, starts, 10, lanes=lanes,
+                               droplets_per_group=droplets_per_group):
+        assert np.isfinite(out).all() and out.min() >= h.min() - 1e-3 and out.max() <= h.max() + 1e-3
+        assert abs((total - out.sum()) - res) <= 1e-5 * total
+
+
 # "default" and the row variants update the brush in 16-byte row blocks (the
 # maps here are aligned and a multiple of four wide; the default takes the
 # lanes that keep four blocks per lane); "pointwise" keeps the point-by-point
