@@ -150,6 +150,16 @@ struct stpgb_batch {
 		return STPGB_OK;
 	}
 
+	// several brush blocks per round trip where every request keeps few
+	// droplets in flight per pixel of its centre chunk
+	bool wide() const {
+		double c = 0.0;
+		for (const ErosionJob& e : ero_h) {
+			c = std::max(c, erosion_concurrency(e.count, static_cast<double>(e.dim_x) * e.dim_y / 9.0, lanes, dpg));
+		}
+		return erosion_rows_wide(min_radius, c);
+	}
+
 	// stage 0: filter, 1: noise, 2: erosion, 3: format
 	int stage(uint32_t st, cudaStream_t s) {
 		const uint32_t nchunks = static_cast<uint32_t>(shf_h.size());
@@ -161,7 +171,7 @@ struct stpgb_batch {
 				table, biome_count, s);
 		case 2u:
 			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
-				false, dpg, rows, erosion_rows_paired(min_radius, density));
+				false, dpg, rows, wide());
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -249,8 +259,7 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows,
-				erosion_rows_paired(min_radius, density)));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows, wide()));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));

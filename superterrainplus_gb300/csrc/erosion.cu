@@ -600,6 +600,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 	// y + (g >> 1)); with two lanes lane g reads both corners of row y + g
 	const uint32_t corner_off = G == 4u ? (((g & 2u) ? pitch : 0u) + (g & 1u)) : (g ? pitch : 0u);
 	const uint32_t nrun = nruns;
+	constexpr int32_t kTripMax = K == 1u ? 3 : 2;
 	const float lo = static_cast<float>(P.BrushRadius);
 	const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
 	// cells whose brush (reach BrushRadius - 1) and deposit corners stay inside the map
@@ -782,17 +783,17 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 						nmax = max(nmax, nb[k]);
 					}
 				}
-				// `trip` (1 or 2) blocks per round trip: a run's blocks are
-				// distinct cells, so reading the second before the first one's
-				// update changes nothing for this droplet
+				// `trip` (1 to kTripMax) blocks per round trip: a run's blocks
+				// are distinct cells, so reading the next ones before the first
+				// one's update changes nothing for this droplet
 #pragma unroll 1
 				for (int32_t b0 = 0; b0 < nmax; b0 += static_cast<int32_t>(trip)) {
-					float4 cur[K][2];
+					float4 cur[K][kTripMax];
 #pragma unroll
 					for (uint32_t k = 0u; k < K; k++) {
 #pragma unroll
-						for (int32_t u = 0; u < 2; u++) {
-							if ((u == 0 || trip == 2u) && b0 + u < nb[k]) {
+						for (int32_t u = 0; u < kTripMax; u++) {
+							if (u < static_cast<int32_t>(trip) && b0 + u < nb[k]) {
 								cur[k][u] = __ldcg(blk[k] + b0 + u);
 							}
 						}
@@ -800,9 +801,9 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 #pragma unroll
 					for (uint32_t k = 0u; k < K; k++) {
 #pragma unroll
-						for (int32_t u = 0; u < 2; u++) {
+						for (int32_t u = 0; u < kTripMax; u++) {
 							const int32_t b = b0 + u;
-							if ((u == 0 || trip == 2u) && b < nb[k]) {
+							if (u < static_cast<int32_t>(trip) && b < nb[k]) {
 								float c[4] = { cur[k][u].x, cur[k][u].y, cur[k][u].z, cur[k][u].w }, d[4];
 #pragma unroll
 								for (int i = 0; i < 4; i++) {
@@ -981,20 +982,36 @@ bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_gr
 	return lanes == 1u || density <= kDenseRows;
 }
 
-bool erosion_rows_paired(const uint32_t min_radius, const double density) {
-	return min_radius >= kPairedMinRadius && density <= kDenseRows;
+double erosion_resident_droplets(const uint32_t lanes, const uint32_t dpg) {
+	// SM count of the current device (a property query, no stream work)
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess
+		|| sms <= 0) {
+		cudaGetLastError();
+		sms = 152; // GB300
+	}
+	const uint32_t blocks = dpg == 2u ? 8u : 9u; // the row kernel's launch bounds
+	return static_cast<double>(sms) * blocks * kErodeBlock / std::max(lanes, 1u) * std::max(dpg, 1u);
+}
+
+double erosion_concurrency(const uint32_t count, const double area, const uint32_t lanes, const uint32_t dpg) {
+	return std::min(static_cast<double>(count), erosion_resident_droplets(lanes, dpg)) / std::max(area, 1.0);
+}
+
+bool erosion_rows_wide(const uint32_t min_radius, const double concurrency) {
+	return min_radius >= kWideMinRadius && concurrency <= kWideConcurrency;
 }
 
 ErosionChoice erosion_choice(const uint32_t radius, const uint32_t brush_size, const double density,
 	const bool rows_allowed) {
 	if (density > kDenseRows) {
-		return ErosionChoice { 1u, 1u, false, false };
+		return ErosionChoice { 1u, 1u, false };
 	}
 	const uint32_t rl = rows_max_lanes(radius);
 	if (rows_allowed && rl != 0u) {
-		return ErosionChoice { rl, 1u, true, erosion_rows_paired(radius, density) };
+		return ErosionChoice { rl, 1u, true };
 	}
-	return ErosionChoice { default_lanes(brush_size), 1u, false, false };
+	return ErosionChoice { default_lanes(brush_size), 1u, false };
 }
 
 RainParams rain_params(const stpgb_raindrop_setting& s) {
@@ -1026,7 +1043,7 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp,
-	uint32_t droplets_per_group, bool vector_rows, bool paired_blocks) {
+	uint32_t droplets_per_group, bool vector_rows, bool wide_trips) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
@@ -1045,7 +1062,8 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 				STPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 					static_cast<int>(rsmem)));
 			}
-			kernel<<<rgrid, kErodeBlock, rsmem, stream>>>(jobs, single, paired_blocks ? 2u : 1u);
+			const uint32_t trip = wide_trips ? (droplets_per_group == 1u ? 3u : 2u) : 1u;
+			kernel<<<rgrid, kErodeBlock, rsmem, stream>>>(jobs, single, trip);
 			STPGB_CUDA_TRY(cudaGetLastError());
 			return STPGB_OK;
 		};
@@ -1204,14 +1222,15 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	bool rows = !exact && (flags & STPGB_EROSION_POINTWISE) == 0u
 		&& (reinterpret_cast<uintptr_t>(heightmap) & 15u) == 0u && (dx & 3u) == 0u;
 	uint32_t lanes = lanes_per_droplet, dpg = droplets_per_group == 0u ? 1u : droplets_per_group;
-	const double density = static_cast<double>(count) / (static_cast<double>(nn->MapSize[0]) * nn->MapSize[1]);
+	const double area = static_cast<double>(nn->MapSize[0]) * nn->MapSize[1];
+	const double density = static_cast<double>(count) / area;
 	if (lanes == 0u) {
 		const ErosionChoice c = erosion_choice(setting->ErosionBrushRadius, brush_size, density, rows);
 		lanes = c.lanes;
 		rows = c.rows;
 	}
 	return erosion_launch(nullptr, job, 1u, count, brush_size, as_stream(stream), lanes, exact, dpg, rows,
-		erosion_rows_paired(setting->ErosionBrushRadius, density));
+		erosion_rows_wide(setting->ErosionBrushRadius, erosion_concurrency(count, area, lanes, dpg)));
 }
 
 int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area, uint32_t* lanes_per_droplet,

@@ -41,10 +41,11 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 // vector_rows: with 2 or 4 lanes and 1 or 2 droplets per group, update the
 // brush run by run in 16-byte blocks (every map 16-byte aligned, pitch a
 // multiple of four floats);
-// paired_blocks: with vector_rows, read two blocks of a run per round trip
+// wide_trips: with vector_rows, read up to three blocks of a run per round
+// trip (one droplet per group) or two (two droplets)
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
-	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool paired_blocks = false);
+	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool wide_trips = false);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).
@@ -63,15 +64,28 @@ uint32_t rows_max_lanes(uint32_t radius);
 constexpr double kDenseRows = 3.0;
 bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density);
 
-// Two brush blocks per round trip compress the update further: in range up to
-// kDenseRows with brush radius 4 and above, not with radius 3 beyond 2.3
-// droplets per pixel, so only brushes from kPairedMinRadius use them.
-constexpr uint32_t kPairedMinRadius = 4u;
-bool erosion_rows_paired(uint32_t min_radius, double density);
+// Several brush blocks per round trip compress a droplet's brush update
+// further, which moves the racy result away from the serial one where many
+// droplets share the map at once.  What counts is the droplets in flight per
+// pixel of the start area (min(count, resident droplets) / area): measured
+// against the one-thread-per-droplet kernel's band around the FP64 serial
+// result, brush 4 at 0.67 in flight per pixel stays at 0.55 of the band with
+// three blocks per trip, while at 2.26 two blocks already reach 1.34 (one
+// block: 0.93).  Wide trips are therefore taken only up to kWideConcurrency
+// droplets in flight per pixel, and from brush radius kWideMinRadius (brush 3
+// on densely packed 64^2 chunks dug channels below range with them).
+constexpr uint32_t kWideMinRadius = 4u;
+constexpr double kWideConcurrency = 0.75;
+// Droplets the row kernel keeps resident on this device with `lanes` lanes
+// per droplet and `dpg` droplets per group.
+double erosion_resident_droplets(uint32_t lanes, uint32_t dpg);
+// Droplets in flight per pixel for `count` droplets starting in `area` pixels.
+double erosion_concurrency(uint32_t count, double area, uint32_t lanes, uint32_t dpg);
+bool erosion_rows_wide(uint32_t min_radius, double concurrency);
 
 struct ErosionChoice {
 	uint32_t lanes, droplets_per_group;
-	bool rows, paired;
+	bool rows;
 };
 // Default kernel for a brush of `radius` (`brush_size` points) at `density`.
 ErosionChoice erosion_choice(uint32_t radius, uint32_t brush_size, double density, bool rows_allowed);

@@ -622,14 +622,19 @@ struct stpgb_server {
 		STPGB_TRY(starts_jobs_launch(reinterpret_cast<StartsJob*>(sl.dev + o_starts), static_cast<uint32_t>(nr), maxCount,
 			this->base.Seed, s));
 		// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
-		// pitches 3 * MapSize) with two droplets per group where the densest
-		// request stays in the rows' stable range, else the stable point-wise
-		// variant
+		// pitches 3 * MapSize), one droplet per group (with several blocks
+		// per round trip the fastest row variant, and the one that keeps the
+		// fewest droplets in flight per pixel); the stable point-wise variant
+		// with two droplets per group where rows are not allowed
 		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, true);
-		const uint32_t dpg = erosion_variant_stable(ec.lanes, 2u, ec.rows, maxDensity)
-			&& (ec.rows || ec.lanes >= 4u) ? 2u : 1u;
+		const uint32_t dpg = !ec.rows && ec.lanes >= 4u && erosion_variant_stable(ec.lanes, 2u, false, maxDensity) ? 2u : 1u;
+		double inflight = 0.0;
+		for (size_t i = 0; i < nr; i++) {
+			inflight = std::max(inflight, erosion_concurrency(ero[i].count,
+				static_cast<double>(ero[i].dim_x) * ero[i].dim_y / 9.0, ec.lanes, dpg));
+		}
 		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
-			maxBrush, s, ec.lanes, false, dpg, ec.rows, ec.paired));
+			maxBrush, s, ec.lanes, false, dpg, ec.rows, erosion_rows_wide(minRadius, inflight)));
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
 		STPGB_CUDA_TRY(cudaMemcpyAsync(it.residual_host, res_dev, nr * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -173,11 +173,11 @@ def test_default_choice_stays_physical_when_densely_packed(dev, oracle, stpgb, b
         assert abs((total - out.sum()) - res) <= 1e-5 * total
 
 
-@pytest.mark.parametrize("brush,lanes,droplets_per_group", [(3, 0, 1), (4, 0, 1), (3, 4, 2), (4, 2, 2)])
+@pytest.mark.parametrize("brush,lanes,droplets_per_group", [(3, 0, 1), (4, 0, 1), (5, 0, 1), (3, 4, 2), (4, 2, 2)])
 def test_rows_stay_physical_at_the_dense_limit(dev, oracle, stpgb, brush, lanes, droplets_per_group):
-    """At 3 droplets per pixel, the densest load the brush-row kernels take (the default choice,
-    two blocks per round trip from brush radius 4, and explicit row variants), the heights stay
-    in range in every run.  Without the brush amount clamped at zero, brush 3 drove heights to
+    """At 3 droplets per pixel, the densest load the brush-row kernels take (the default choice and
+    explicit row variants, one brush block per round trip at this many droplets in flight), the
+    heights stay in range in every run.  Without the brush amount clamped at zero, brush 3 drove heights to
     -10^5 here: racing readers of one cell took it below zero, and every reader then added the
     negative height's magnitude back."""
     S = 64
@@ -211,13 +211,24 @@ VARIANTS = {
 @pytest.mark.parametrize("case", sorted(EROSION_CASES))
 @pytest.mark.parametrize("variant", sorted(VARIANTS))
 def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, variant):
+    erosion_rms_within_reference_spread(dev, oracle, stpgb, EROSION_CASES[case], variant, case)
+
+
+def test_production_brush_rms_within_reference_spread(dev, oracle, stpgb):
+    """The production brush (radius 4) at the production density (2.29 droplets per pixel) on 256^2
+    chunks: the default choice reads several brush blocks per round trip here (fewer than 0.75
+    droplets in flight per pixel), and stays within the reference kernel's band."""
+    erosion_rms_within_reference_spread(dev, oracle, stpgb, (256, 150000, 4, 50), "default", "brush4-256")
+
+
+def erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, case):
     """Per-pixel RMS against the FP64 serial oracle stays within the reference kernel's own band.
 
     The reference kernel is one thread per droplet reading and updating the brush point by point
     (lanes=1, the reference's memory order); five runs of it give its RMS against the oracle and its
     run-to-run spread (max pairwise RMS).  The production kernel (default lanes) must satisfy
     RMS_prod <= max(RMS_ref) + spread_ref on every run, and conserve mass."""
-    S, count, brush, life = EROSION_CASES[case]
+    S, count, brush, life = params
     nn = (3, 3)
     h = terrain(3 * S, 3 * S, S)
     s = helpers.raindrop_dict(count, radius=brush, lifetime=life)
