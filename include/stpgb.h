@@ -263,9 +263,15 @@ STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
  * 16-byte blocks instead: one vector read, then one vector reduction
  * subtracting min(cell, w) from the row's cells (-0.0 elsewhere); a droplet's
  * cells are distinct, so per droplet this is the same read-then-subtract,
- * with a quarter of the memory operations.  The default keeps four points
- * (or four 16-byte blocks) per lane: below that a step's reads happen nearly
- * together and densely packed droplets can run the map away.
+ * with a quarter of the memory operations.  From brush radius 4, and with two
+ * lanes, a block is instead updated by one returning vector atomic that
+ * subtracts the amounts and yields the cells' values at that moment, and a
+ * lane gives back what a cell lacked: the reference's c - min(c, w) on the
+ * exact current value.  Where few droplets are in flight per pixel (at most
+ * 3/4), a lane reads up to three blocks of a run per round trip.  The default
+ * runs brush rows with two lanes per droplet (row blocks need at least four
+ * points or blocks per lane; with fewer a step's reads happen nearly together
+ * and densely packed droplets can run the map away).
  * STPGB_EROSION_POINTWISE keeps the point-by-point kernels.
  * STPGB_EROSION_EXACT_CLAMP erodes each point by compare-and-swap instead, so
  * racing droplets never remove more than a cell holds (closer to the serial

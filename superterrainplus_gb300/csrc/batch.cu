@@ -150,16 +150,6 @@ struct stpgb_batch {
 		return STPGB_OK;
 	}
 
-	// several brush blocks per round trip where every request keeps few
-	// droplets in flight per pixel of its centre chunk
-	bool wide() const {
-		double c = 0.0;
-		for (const ErosionJob& e : ero_h) {
-			c = std::max(c, erosion_concurrency(e.count, static_cast<double>(e.dim_x) * e.dim_y / 9.0, lanes, dpg));
-		}
-		return erosion_rows_wide(min_radius, c);
-	}
-
 	// stage 0: filter, 1: noise, 2: erosion, 3: format
 	int stage(uint32_t st, cudaStream_t s) {
 		const uint32_t nchunks = static_cast<uint32_t>(shf_h.size());
@@ -171,7 +161,7 @@ struct stpgb_batch {
 				table, biome_count, s);
 		case 2u:
 			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
-				false, dpg, rows, wide());
+				false, dpg, rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes));
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -259,7 +249,8 @@ struct stpgb_batch {
 			}
 			const ErosionJob& e = ero_h[n];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows, wide()));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows,
+				erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes)));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -345,7 +336,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		// the default until the autotuner runs: brush rows where stable, else
 		// several lanes point by point, above kDenseRows the reference kernel
 		b->rows = b->rows_limit != 0u && b->density <= kDenseRows;
-		b->lanes = b->rows ? b->rows_limit : b->density <= kDenseRows ? std::min(8u, b->lane_limit) : 1u;
+		b->lanes = b->rows ? 2u : b->density <= kDenseRows ? std::min(8u, b->lane_limit) : 1u;
 		b->dpg = 1u;
 		L.brush_idx = off;
 		off += al(bs * sizeof(int32_t));
@@ -455,6 +446,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		e.residual = b->residual + n;
 		e.status = b->status;
 		e.counters = b->counters;
+		e.start_area = S * S;
 		e.fixed = reinterpret_cast<uint16_t*>(m + L.fixed);
 		b->ero_h.push_back(e);
 		b->fmt_h.push_back(FormatJob { height, 3ull * S, e.fixed, 3ull * S, 3u * S, 3u * S });

@@ -29,6 +29,10 @@ struct ErosionJob {
 	uint16_t* fixed; // formatted output (optional, batched path)
 	// optional counters: [0] realised steps, [1] steps that eroded over the brush
 	unsigned long long* counters;
+	// pixels of the area the starts cover (the centre chunk); with `count`
+	// it gives the droplets in flight per pixel that bound the row kernel's
+	// blocks per round trip (0: one block per trip)
+	uint32_t start_area;
 };
 
 RainParams rain_params(const stpgb_raindrop_setting& s);
@@ -41,11 +45,15 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 // vector_rows: with 2 or 4 lanes and 1 or 2 droplets per group, update the
 // brush run by run in 16-byte blocks (every map 16-byte aligned, pitch a
 // multiple of four floats);
-// wide_trips: with vector_rows, read up to three blocks of a run per round
-// trip (one droplet per group) or two (two droplets)
+// wide_trips: with vector_rows, let every job that keeps at most
+// kWideConcurrency droplets in flight per pixel of its start area read up to
+// three blocks of a run per round trip (one droplet per group) or two (two
+// droplets);
+// atomic_brush: with vector_rows, take each block's brush amounts with one
+// returning vector atomic and give back what a cell lacked
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
-	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool wide_trips = false);
+	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool wide_trips = false, bool atomic_brush = false);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).
@@ -78,10 +86,24 @@ constexpr uint32_t kWideMinRadius = 4u;
 constexpr double kWideConcurrency = 0.75;
 // Droplets the row kernel keeps resident on this device with `lanes` lanes
 // per droplet and `dpg` droplets per group.
-double erosion_resident_droplets(uint32_t lanes, uint32_t dpg);
-// Droplets in flight per pixel for `count` droplets starting in `area` pixels.
-double erosion_concurrency(uint32_t count, double area, uint32_t lanes, uint32_t dpg);
-bool erosion_rows_wide(uint32_t min_radius, double concurrency);
+uint32_t erosion_resident_droplets(uint32_t lanes, uint32_t dpg);
+// Whether a launch whose smallest brush has `min_radius` may take wide trips
+// (each job then decides by its own droplets in flight per pixel).
+bool erosion_rows_wide(uint32_t min_radius);
+
+// The brush update as one returning vector atomic per 16-byte block (the
+// cell's value at the moment of the update, w subtracted, and the part of w
+// the cell lacked given back) in place of a read and a later reduction: half
+// the L2 requests, and no read-to-update window in which racing droplets see
+// a stale height.  A cell waiting for its give-back is transiently w too low
+// for other droplets' corner reads; with brush radius 3 and four lanes those
+// dips fed on each other on densely packed 64^2 chunks (heights below range
+// from 3 droplets per pixel, one run ran away at 7), while two lanes with
+// brush 3, and brushes 4 and 5 in every variant, stayed in range up to 7
+// droplets per pixel.  So it is taken from brush radius kAtomicMinRadius, and
+// with two lanes per droplet.
+constexpr uint32_t kAtomicMinRadius = 4u;
+bool erosion_rows_atomic(uint32_t min_radius, uint32_t lanes);
 
 struct ErosionChoice {
 	uint32_t lanes, droplets_per_group;

@@ -590,6 +590,7 @@ struct stpgb_server {
 			e.p = rain_params(rs);
 			e.residual = res_dev + i;
 			e.status = status_dev;
+			e.start_area = S * S;
 			ero[i] = e;
 			fmt[i] = FormatJob { e.map, 3ull * S, reinterpret_cast<uint16_t*>(at(r.fixed)), 3ull * S, 3u * S, 3u * S };
 			maxRS = std::max(maxRS, S);
@@ -622,19 +623,15 @@ struct stpgb_server {
 		STPGB_TRY(starts_jobs_launch(reinterpret_cast<StartsJob*>(sl.dev + o_starts), static_cast<uint32_t>(nr), maxCount,
 			this->base.Seed, s));
 		// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
-		// pitches 3 * MapSize), one droplet per group (with several blocks
-		// per round trip the fastest row variant, and the one that keeps the
-		// fewest droplets in flight per pixel); the stable point-wise variant
-		// with two droplets per group where rows are not allowed
+		// pitches 3 * MapSize), the default two lanes and one droplet per
+		// group; each job reads several blocks per round trip where few of its
+		// droplets are in flight per pixel.  The stable point-wise variant with
+		// two droplets per group where rows are not allowed
 		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, true);
 		const uint32_t dpg = !ec.rows && ec.lanes >= 4u && erosion_variant_stable(ec.lanes, 2u, false, maxDensity) ? 2u : 1u;
-		double inflight = 0.0;
-		for (size_t i = 0; i < nr; i++) {
-			inflight = std::max(inflight, erosion_concurrency(ero[i].count,
-				static_cast<double>(ero[i].dim_x) * ero[i].dim_y / 9.0, ec.lanes, dpg));
-		}
 		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
-			maxBrush, s, ec.lanes, false, dpg, ec.rows, erosion_rows_wide(minRadius, inflight)));
+			maxBrush, s, ec.lanes, false, dpg, ec.rows, erosion_rows_wide(minRadius),
+			erosion_rows_atomic(minRadius, ec.lanes)));
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
 		STPGB_CUDA_TRY(cudaMemcpyAsync(it.residual_host, res_dev, nr * sizeof(double), cudaMemcpyDeviceToHost, s));

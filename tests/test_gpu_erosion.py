@@ -94,16 +94,19 @@ def test_erosion_mass_balance(dev, oracle, stpgb, map_size, nn, count, radius, l
     assert abs(balance) <= 1e-5 * total, f"mass balance off by {balance:.3g} of {total:.3g}"
 
 
-def test_erosion_sparse_droplets_follow_fp64_oracle(dev, oracle, stpgb):
-    """Droplets whose paths cannot meet (starts 80 px apart, 30 steps, brush 3) run as the serial oracle."""
+@pytest.mark.parametrize("brush", [3, 4, 5])
+def test_erosion_sparse_droplets_follow_fp64_oracle(dev, oracle, stpgb, brush):
+    """Droplets whose paths cannot meet (starts 80 px apart, 30 steps, brush reach below 5) run as
+    the serial oracle: brush 3 reads then reduces each 16-byte block, brushes 4 and 5 take the
+    amounts with one returning atomic per block and give back what a cell lacked."""
     mx = my = 320
     h = terrain(mx, my, 2)
     g = np.arange(40, 300, 80, dtype=np.float32) + 0.37
     xs, ys = np.meshgrid(g, g)
     starts = np.stack([xs.ravel(), ys.ravel()], 1).ravel().astype(np.float32)
-    s = helpers.raindrop_dict(len(starts) // 2, radius=3, lifetime=30)
+    s = helpers.raindrop_dict(len(starts) // 2, radius=brush, lifetime=30)
     out, res = gpu_erode(dev, stpgb, h, (mx, my), (1, 1), s, starts)
-    idx, w = oracle.brush(mx, 3)
+    idx, w = oracle.brush(mx, brush)
     ref, ref_res, _ = oracle.erode(h, s, starts, idx, w, fp64=True)
     rms = float(np.sqrt(np.mean((out.astype(np.float64) - ref) ** 2)))
     assert rms <= 1e-5 * float(h.max() - h.min()), rms
@@ -214,11 +217,13 @@ def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, variant):
     erosion_rms_within_reference_spread(dev, oracle, stpgb, EROSION_CASES[case], variant, case)
 
 
-def test_production_brush_rms_within_reference_spread(dev, oracle, stpgb):
-    """The production brush (radius 4) at the production density (2.29 droplets per pixel) on 256^2
-    chunks: the default choice reads several brush blocks per round trip here (fewer than 0.75
-    droplets in flight per pixel), and stays within the reference kernel's band."""
-    erosion_rms_within_reference_spread(dev, oracle, stpgb, (256, 150000, 4, 50), "default", "brush4-256")
+@pytest.mark.parametrize("params", [(512, 600000, 4, 50), (256, 150000, 4, 50)], ids=["512", "256"])
+def test_production_brush_rms_within_reference_spread(dev, oracle, stpgb, params):
+    """The production chunk (3x3 x 512^2, 600,000 droplets, brush 4, lifetime 50) and the same
+    density on 256^2 chunks: the default choice (brush rows, the brush taken by returning atomics,
+    several blocks per round trip on the production chunk) stays within the reference kernel's
+    band around the FP64 serial result."""
+    erosion_rms_within_reference_spread(dev, oracle, stpgb, params, "default", f"brush4-{params[0]}")
 
 
 def erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, case):
