@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--batch", type=int, default=16)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-large-field", action="store_true",
+                   help="skip the 4096^2 large-field section")
     p.add_argument("--serve-requests", type=int, default=600,
                    help="camera-walk requests replayed through the server (0 skips the serving section)")
     return p.parse_args()
@@ -354,8 +356,10 @@ def run_ours(args):
         serving["at_120_per_s"] = serve_section(m, np, torch, args.serve_requests, rate=120.0, plain=False)
         serving["layer_chain_biomes"] = serve_section(m, np, torch, args.serve_requests, layer=True, plain=False)
 
-    biomemap = splatmap = None
+    biomemap = splatmap = large = None
     if rank == 0:
+        if not args.no_large_field:
+            large = large_field_section(m, np, torch)
         biomemap = biomemap_section(m, np, torch, B, cpu=world == 1 and not args.no_cpu_baseline)
         splatmap = splatmap_section(m, np, torch, batch, reqs, cpu=world == 1 and not args.no_cpu_baseline)
 
@@ -385,6 +389,7 @@ def run_ours(args):
             "serving": serving,
             "biomemap": biomemap,
             "splatmap": splatmap,
+            "large_field": large,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
@@ -437,6 +442,85 @@ def biomemap_section(m, np, torch, batch, cpu=True, reps=3):
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": f"{S}^2 biomemap chunks/s", "cores": 1, "kind": "port",
                                "sample": f"one {S}^2 chunk through the CPU restatement of the layer chain"}
     return out
+
+
+def large_field_section(m, np, torch, reps=3):
+    """The large single field: a 4096^2 float32 heightfield from 8-octave fractal simplex noise,
+    32 biomes from a seeded Voronoi uint16 map (the filter's window of its 3x3 neighbourhood),
+    filter radius 64, then 16,000,000 droplets with brush 5 and lifetime 64 eroding the field as its
+    own free-slip neighbourhood, formatted to uint16.  Kernel-level calls on one stream, each stage
+    timed alone with CUDA events; the erosion restarts from the same heights every repetition."""
+    S, r, nb, cell, seed, count, brush, life = 4096, 64, 32, 512, 7, 16_000_000, 5, 64
+    dev = m.DeviceOps()
+    st = torch.cuda.current_stream()
+    rng = np.random.default_rng(seed)
+    table = np.zeros(nb, m.BIOME_DTYPE)
+    table["Scale"] = np.exp(rng.uniform(np.log(64.0), np.log(512.0), nb)).astype(np.float32)
+    table["Octave"] = 8
+    table["Persistence"] = 0.5
+    table["Lacunarity"] = 2.0
+    table["Variation"] = rng.uniform(0.2, 1.0, nb).astype(np.float32)
+    perm, grad = m.permutation_generate(seed, 8, 0.2181661565)
+    d_perm, d_grad = torch.from_numpy(perm).cuda(), torch.from_numpy(grad).cuda()
+    d_table = torch.from_numpy(table.view(np.float32)).cuda()
+    biomes = torch.zeros((3 * S, 3 * S), dtype=torch.int16, device="cuda")
+    w = S + 2 * r
+    dev.voronoi_biomemap(biomes[S - r:, S - r:], 3 * S, w, w, (-r, -r), cell, nb, seed)
+    starts = torch.empty(2 * count, dtype=torch.float32, device="cuda")
+    dev.droplet_starts(starts, count, seed, 0, (S, S), (1, 1))
+    evap = 0.01
+    rd = m.RaindropSetting(Seed=seed, RainDropCount=count, Inertia=0.05, SedimentCapacityFactor=4.0,
+                           minSedimentCapacity=0.01, initWaterVolume=1.0,
+                           minWaterVolume=m.lifetime_min_water_volume(1.0, evap, life), Friction=0.1, initSpeed=1.0,
+                           ErodeSpeed=0.3, DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0,
+                           ErosionBrushRadius=brush)
+    idx, wgt = m.erosion_brush(S, brush)
+    d_idx, d_wgt = torch.from_numpy(idx).cuda(), torch.from_numpy(wgt).cuda()
+    h0 = torch.empty((S, S), dtype=torch.float32, device="cuda")
+    h = torch.empty_like(h0)
+    fixed = torch.empty((S, S), dtype=torch.int16, device="cuda")
+    residual = torch.zeros(1, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ms = {"single_histogram_filter": [], "multibiome_noise": [], "hydraulic_erosion": [], "format": []}
+    nbins = 0
+    for k in range(1 + reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+        ev[0].record(st)
+        off, bins, fstatus = dev.shf_filter(biomes, (S, S), (3, 3), r, max_items=nb, bins_capacity=8 * S * S)
+        ev[1].record(st)
+        ev[2].record(st)
+        dev.multibiome_heightmap(h0, S, off, bins, (S, S), (0.0, 0.0), d_perm, d_grad, d_table)
+        ev[3].record(st)
+        h.copy_(h0)
+        residual.zero_()
+        ev[4].record(st)
+        dev.hydraulic_erosion(h, (S, S), (1, 1), rd, starts, count, d_idx, d_wgt, residual, status)
+        ev[5].record(st)
+        ev[6].record(st)
+        dev.format_heightmap(h, fixed, S, S)
+        ev[7].record(st)
+        torch.cuda.synchronize()
+        dev.status_check(fstatus)
+        dev.status_check(status)
+        if k == 0:
+            nbins = int(off[-1].item())
+            continue
+        for j, name in enumerate(ms):
+            ms[name].append(ev[2 * j].elapsed_time(ev[2 * j + 1]))
+        del off, bins, fstatus
+    med = {k: statistics.median(v) for k, v in ms.items()}
+    total = sum(med.values())
+    shf_bytes = 2 * w * w + 4 * (S * S + 1) + 8 * nbins
+    noise_flops = nbins * (60 * 8 + 4) + 8 * S * S
+    peak, peak_kind = load_peaks()
+    shf_gbs = shf_bytes / (med["single_histogram_filter"] / 1000.0) / 1e9
+    return {"workload": "4096^2 float32 field, 8-octave noise, 32 Voronoi biomes, filter radius 64, 16,000,000 "
+                        "droplets, brush 5, lifetime 64, free-slip 1x1",
+            "ms_per_field": total, "fields_per_s": 1000.0 / total, "stage_ms": med,
+            "droplets_per_s": count / (med["hydraulic_erosion"] / 1000.0),
+            "filter_bins": nbins, "filter_algorithmic_gb_per_s": shf_gbs, "filter_frac_of_hbm": shf_gbs / peak,
+            "noise_algorithmic_tflop_per_s": noise_flops / (med["multibiome_noise"] / 1000.0) / 1e12,
+            "peak_source": peak_kind, "launches_per_field": 7}
 
 
 def splat_rules(m):

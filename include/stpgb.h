@@ -154,6 +154,43 @@ STPGB_API int stpgb_erosion_brush_generate(uint32_t dimension_x, uint32_t radius
 STPGB_API float stpgb_lifetime_min_water_volume(float init_water_volume,
 	float evaporate_speed, uint32_t lifetime);
 
+/* ------------------------------------------------- chunk coordinates ---- */
+
+/* The static coordinate functions of STPChunk
+ * (SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/World/Chunk/STPChunk.h:110-157,
+ * SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPChunk.cpp:63-108).  A
+ * chunk coordinate is in world units (a multiple of the chunk size); vectors
+ * are two-element arrays (x, then y / z).  Where the reference has undefined
+ * behaviour (a zero size or range, an int32 overflow, a non-finite
+ * position) these return STPGB_EINVAL. */
+
+/* STPChunk::calcWorldChunkCoordinate (STPChunk.cpp:63-69): the coordinate of
+ * the chunk holding world point (x, z), chunks scaled by `scale`. */
+STPGB_API int stpgb_chunk_world_coordinate(double point_x, double point_z,
+	const uint32_t* chunk_size, const double* scale, int32_t* out);
+/* STPChunk::calcLocalChunkCoordinate (STPChunk.cpp:71-73): chunk index of a
+ * row-major region -> (index % range.x, index / range.x). */
+STPGB_API int stpgb_chunk_local_coordinate(uint32_t chunk_id, const uint32_t* chunk_range,
+	uint32_t* out);
+/* STPChunk::calcLocalChunkOrigin (STPChunk.cpp:75-79): the top-left chunk of
+ * a neighbourhood of `neighbour_size` chunks around `centre`. */
+STPGB_API int stpgb_chunk_local_origin(const int32_t* centre, const uint32_t* chunk_size,
+	const uint32_t* neighbour_size, int32_t* out);
+/* STPChunk::calcChunkMapOffset (STPChunk.cpp:81-85): the map offset a chunk's
+ * maps are generated at, (coord / chunk_size) * map_size + map_offset in
+ * double (a rounded product, then a rounded sum). */
+STPGB_API int stpgb_chunk_map_offset(const int32_t* chunk_coord, const uint32_t* chunk_size,
+	const uint32_t* map_size, const double* map_offset, double* out);
+/* STPChunk::offsetChunk (STPChunk.cpp:87-89): coord + chunk_size * offset. */
+STPGB_API int stpgb_chunk_offset(const int32_t* chunk_coord, const uint32_t* chunk_size,
+	const int32_t* offset, int32_t* out);
+/* STPChunk::calcChunkNeighbourOffset (STPChunk.cpp:91-108): the offset of
+ * every chunk of a `region_size` neighbourhood from its centre chunk, in
+ * chunk-index order, as `*count` (x, y) pairs in `offsets_xy` (STPGB_ECAPACITY
+ * with the needed count when `capacity` pairs are too few). */
+STPGB_API int stpgb_chunk_neighbour_offset(const uint32_t* chunk_size, const uint32_t* region_size,
+	int32_t* offsets_xy, uint32_t capacity, uint32_t* count);
+
 /* ----------------------------------------------- single histogram filter -- */
 
 /* Workspace bytes stpgb_shf_filter needs for a chunk of `nn`, `radius`, and

@@ -13,6 +13,8 @@
  *       (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,145,159)
  *   SuperTerrainPlus::STPDiversity::STPBiomeFactory, STPDemo::STPLayerChainBuilder
  *       (SuperTerrain+/World/Diversity/STPBiomeFactory.h:19-63, SuperDemo+/World/Layers/STPAllLayers.h)
+ *   SuperTerrainPlus::STPChunk coordinate functions
+ *       (SuperTerrain+/World/Chunk/STPChunk.h:110-157)
  *   SuperTerrainPlus::STPException::{STPNumericDomainError, STPInvalidEnvironment, STPCUDAError}
  */
 #ifndef STPGB_HPP_
@@ -333,6 +335,113 @@ private:
 		}
 	};
 	std::unique_ptr<stpgb_generator, Deleter> Handle;
+};
+
+namespace detail {
+
+// Two-component results of STPChunk; they convert to any vector type built
+// as V { x, y }, such as glm::ivec2 / glm::uvec2 / glm::dvec2.
+template<class T>
+struct vec2_of {
+	T x, y;
+	template<class V>
+	operator V() const {
+		return V { x, y };
+	}
+	bool operator==(const vec2_of& o) const {
+		return x == o.x && y == o.y;
+	}
+	bool operator!=(const vec2_of& o) const {
+		return !(*this == o);
+	}
+};
+
+template<class T, class V>
+void put2(T* out, const V& v) {
+	out[0] = static_cast<T>(v.x);
+	out[1] = static_cast<T>(v.y);
+}
+
+} // namespace detail
+
+/* The static coordinate functions of STPChunk
+ * (SuperTerrain+/World/Chunk/STPChunk.h:110-157): chunk coordinates are in
+ * world units.  Arguments the reference leaves undefined (zero sizes, int32
+ * overflow, a non-finite position) throw STPNumericDomainError. */
+struct STPChunk {
+	using ivec2 = detail::vec2_of<int32_t>;
+	using uvec2 = detail::vec2_of<uint32_t>;
+	using dvec2 = detail::vec2_of<double>;
+	using STPChunkNeighbourOffset = std::vector<ivec2>;
+
+	template<class P, class U, class D>
+	static ivec2 calcWorldChunkCoordinate(const P& pointPos, const U& chunkSize, const D& scale) {
+		uint32_t cs[2];
+		double sc[2];
+		detail::put2(cs, chunkSize);
+		detail::put2(sc, scale);
+		int32_t out[2];
+		detail::check(stpgb_chunk_world_coordinate(static_cast<double>(pointPos.x), static_cast<double>(pointPos.z),
+			cs, sc, out));
+		return ivec2 { out[0], out[1] };
+	}
+
+	template<class U>
+	static uvec2 calcLocalChunkCoordinate(unsigned int chunkID, const U& chunkRange) {
+		uint32_t r[2], out[2];
+		detail::put2(r, chunkRange);
+		detail::check(stpgb_chunk_local_coordinate(chunkID, r, out));
+		return uvec2 { out[0], out[1] };
+	}
+
+	template<class I, class U, class N>
+	static ivec2 calcLocalChunkOrigin(const I& centreChunkCoord, const U& chunkSize, const N& neighbourSize) {
+		int32_t c[2], out[2];
+		uint32_t cs[2], ns[2];
+		detail::put2(c, centreChunkCoord);
+		detail::put2(cs, chunkSize);
+		detail::put2(ns, neighbourSize);
+		detail::check(stpgb_chunk_local_origin(c, cs, ns, out));
+		return ivec2 { out[0], out[1] };
+	}
+
+	template<class I, class U, class M, class D>
+	static dvec2 calcChunkMapOffset(const I& chunkCoord, const U& chunkSize, const M& mapSize, const D& mapOffset) {
+		int32_t c[2];
+		uint32_t cs[2], ms[2];
+		double mo[2], out[2];
+		detail::put2(c, chunkCoord);
+		detail::put2(cs, chunkSize);
+		detail::put2(ms, mapSize);
+		detail::put2(mo, mapOffset);
+		detail::check(stpgb_chunk_map_offset(c, cs, ms, mo, out));
+		return dvec2 { out[0], out[1] };
+	}
+
+	template<class I, class U, class O>
+	static ivec2 offsetChunk(const I& chunkCoord, const U& chunkSize, const O& offset) {
+		int32_t c[2], o[2], out[2];
+		uint32_t cs[2];
+		detail::put2(c, chunkCoord);
+		detail::put2(cs, chunkSize);
+		detail::put2(o, offset);
+		detail::check(stpgb_chunk_offset(c, cs, o, out));
+		return ivec2 { out[0], out[1] };
+	}
+
+	template<class U, class R>
+	static STPChunkNeighbourOffset calcChunkNeighbourOffset(const U& chunkSize, const R& regionSize) {
+		uint32_t cs[2], rs[2], n = 0u;
+		detail::put2(cs, chunkSize);
+		detail::put2(rs, regionSize);
+		std::vector<int32_t> xy(2u * static_cast<size_t>(rs[0]) * rs[1]);
+		detail::check(stpgb_chunk_neighbour_offset(cs, rs, xy.data(), static_cast<uint32_t>(xy.size() / 2u), &n));
+		STPChunkNeighbourOffset out(n);
+		for (uint32_t i = 0u; i < n; i++) {
+			out[i] = ivec2 { xy[2u * i], xy[2u * i + 1u] };
+		}
+		return out;
+	}
 };
 
 } // namespace SuperTerrainPlus

@@ -30,7 +30,7 @@ __all__ = [
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
     "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch", "Layer", "LayerBiomes",
     "layer_chain_demo", "STPLayerChainBuilder", "AltitudeRule", "GradientRule", "SplatChunk", "splat_rules_demo",
-    "STPSplatmapGenerator",
+    "STPSplatmapGenerator", "STPChunk",
 ]
 
 BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
@@ -40,6 +40,11 @@ BIOME_DTYPE = np.dtype([("Scale", "<f4"), ("Octave", "<u4"), ("Persistence", "<f
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def _data(a):
+    """Host address of a numpy array, or NULL for None (a request the call skips)."""
+    return a.ctypes.data if a is not None else None
 
 
 # ------------------------------------------------------------ host tables
@@ -68,6 +73,65 @@ def erosion_brush(dimension_x, radius):
 
 def lifetime_min_water_volume(init_water_volume, evaporate_speed, lifetime):
     return float(lib().stpgb_lifetime_min_water_volume(init_water_volume, evaporate_speed, lifetime))
+
+
+# ------------------------------------------------------ chunk coordinates
+
+
+def _vec(values, ctype):
+    return (ctype * 2)(*values)
+
+
+class STPChunk:
+    """The static coordinate functions of STPChunk (SuperTerrain+/World/Chunk/STPChunk.h:110-157) over
+    the C ABI.  Vectors are (x, y) pairs; a chunk coordinate is in world units (a multiple of the chunk
+    size).  Arguments the reference leaves undefined (zero sizes, int32 overflow) raise
+    STPNumericDomainError."""
+
+    @staticmethod
+    def calcWorldChunkCoordinate(point_pos, chunk_size, scale):
+        """point_pos is (x, y, z); the chunk holding (x, z)."""
+        out = (C.c_int32 * 2)()
+        check(lib().stpgb_chunk_world_coordinate(float(point_pos[0]), float(point_pos[2]),
+                                                 _vec(chunk_size, C.c_uint32), _vec(scale, C.c_double), out))
+        return tuple(out)
+
+    @staticmethod
+    def calcLocalChunkCoordinate(chunk_id, chunk_range):
+        out = (C.c_uint32 * 2)()
+        check(lib().stpgb_chunk_local_coordinate(chunk_id, _vec(chunk_range, C.c_uint32), out))
+        return tuple(out)
+
+    @staticmethod
+    def calcLocalChunkOrigin(centre, chunk_size, neighbour_size):
+        out = (C.c_int32 * 2)()
+        check(lib().stpgb_chunk_local_origin(_vec(centre, C.c_int32), _vec(chunk_size, C.c_uint32),
+                                             _vec(neighbour_size, C.c_uint32), out))
+        return tuple(out)
+
+    @staticmethod
+    def calcChunkMapOffset(chunk_coord, chunk_size, map_size, map_offset):
+        out = (C.c_double * 2)()
+        check(lib().stpgb_chunk_map_offset(_vec(chunk_coord, C.c_int32), _vec(chunk_size, C.c_uint32),
+                                           _vec(map_size, C.c_uint32), _vec(map_offset, C.c_double), out))
+        return tuple(out)
+
+    @staticmethod
+    def offsetChunk(chunk_coord, chunk_size, offset):
+        out = (C.c_int32 * 2)()
+        check(lib().stpgb_chunk_offset(_vec(chunk_coord, C.c_int32), _vec(chunk_size, C.c_uint32),
+                                       _vec(offset, C.c_int32), out))
+        return tuple(out)
+
+    @staticmethod
+    def calcChunkNeighbourOffset(chunk_size, region_size):
+        """List of (x, y) offsets from the centre chunk, in chunk-index order."""
+        n = C.c_uint32(0)
+        cs, rs = _vec(chunk_size, C.c_uint32), _vec(region_size, C.c_uint32)
+        count = int(region_size[0]) * int(region_size[1])
+        out = (C.c_int32 * (2 * max(count, 1)))()
+        check(lib().stpgb_chunk_neighbour_offset(cs, rs, out, count, C.byref(n)))
+        return [(out[2 * i], out[2 * i + 1]) for i in range(n.value)]
 
 
 # ------------------------------------------------- single histogram filter
@@ -327,15 +391,15 @@ class Batch:
 
     def download(self, heights=None, fixed=None, residual=None, stream=None):
         n = len(self.requests)
-        hp = (C.c_void_p * n)(*[a.ctypes.data for a in heights]) if heights is not None else None
-        fp = (C.c_void_p * n)(*[a.ctypes.data for a in fixed]) if fixed is not None else None
+        hp = (C.c_void_p * n)(*[_data(a) for a in heights]) if heights is not None else None
+        fp = (C.c_void_p * n)(*[_data(a) for a in fixed]) if fixed is not None else None
         rp = residual.ctypes.data_as(C.c_void_p) if residual is not None else None
         check(lib().stpgb_batch_download(self._h, hp, fp, rp, self._s(stream)))
 
     def download_inputs(self, biome_regions=None, starts=None, stream=None):
         n = len(self.requests)
-        bp = (C.c_void_p * n)(*[a.ctypes.data for a in biome_regions]) if biome_regions is not None else None
-        sp = (C.c_void_p * n)(*[a.ctypes.data for a in starts]) if starts is not None else None
+        bp = (C.c_void_p * n)(*[_data(a) for a in biome_regions]) if biome_regions is not None else None
+        sp = (C.c_void_p * n)(*[_data(a) for a in starts]) if starts is not None else None
         check(lib().stpgb_batch_download_inputs(self._h, bp, sp, self._s(stream)))
 
     def status(self, stream=None):

@@ -160,6 +160,12 @@ PROTOTYPES = {
     "stpgb_permutation_generate": (C.c_int, [C.POINTER(SimplexSetting), vp, vp, u32]),
     "stpgb_erosion_brush_generate": (C.c_int, [u32, u32, vp, vp, u32, C.POINTER(u32)]),
     "stpgb_lifetime_min_water_volume": (f32, [f32, f32, u32]),
+    "stpgb_chunk_world_coordinate": (C.c_int, [f64, f64, vp, vp, vp]),
+    "stpgb_chunk_local_coordinate": (C.c_int, [u32, vp, vp]),
+    "stpgb_chunk_local_origin": (C.c_int, [vp, vp, vp, vp]),
+    "stpgb_chunk_map_offset": (C.c_int, [vp, vp, vp, vp, vp]),
+    "stpgb_chunk_offset": (C.c_int, [vp, vp, vp, vp]),
+    "stpgb_chunk_neighbour_offset": (C.c_int, [vp, vp, vp, u32, C.POINTER(u32)]),
     "stpgb_shf_workspace_size": (C.c_int, [C.POINTER(NNInfo), u32, u32, C.POINTER(sz)]),
     "stpgb_shf_filter": (C.c_int, [vp, C.POINTER(NNInfo), u32, u32, vp, sz, vp, vp, u64, vp, vp]),
     "stpgb_shf_filter_host": (C.c_int, [vp, C.POINTER(NNInfo), u32, vp, vp, u64, C.POINTER(u64)]),

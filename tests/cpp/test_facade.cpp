@@ -2,7 +2,8 @@
 // against the C++ façade (include/stpgb.hpp) the way a SuperTerrain+ caller
 // would: SuperTest+/SuperAlgorithm+/STPTestHistogram.cpp (known-answer
 // histograms and error cases), STPTestPermutation.cpp (gradients,
-// repetition, seeds, invalid setting), a generate/erode round trip, and the
+// repetition, seeds, invalid setting), STPTest2DChunk.cpp (chunk coordinate
+// known answers), a generate/erode round trip, and the
 // demo's biome layer chain against maps of the compiled reference.
 // `--cpu` runs the parts that fail before any device work.
 #include "stpgb.hpp"
@@ -218,6 +219,10 @@ void generator_round_trip() {
 
 struct ivec2 {
 	int x, y;
+	ivec2(int a, int b) : x(a), y(b) {}
+	bool operator==(const ivec2& o) const {
+		return x == o.x && y == o.y;
+	}
 };
 
 uint64_t fnv1a(const std::vector<STPSample_t>& v) {
@@ -233,6 +238,44 @@ uint64_t fnv1a(const std::vector<STPSample_t>& v) {
 
 void biome_factory_errors() {
 	CHECK(throws<STPException::STPNumericDomainError>([] { STPDemo::STPLayerChainBuilder f(ivec2 { 0, 4 }, 1u); }));
+}
+
+// SuperTest+/SuperTerrain+/STPTest2DChunk.cpp:30-89, with the test's own vector types
+struct dvec2 {
+	double x, y;
+	dvec2(double a, double b) : x(a), y(b) {}
+	bool operator==(const dvec2& o) const {
+		return x == o.x && y == o.y;
+	}
+};
+struct dvec3 {
+	double x, y, z;
+};
+
+void chunk_coordinates() {
+	const dvec3 camera { -573.74, 679.5, 845.982 };
+	const uvec2 chunk_size { 8u, 5u };
+	const dvec2 scale(2.5, 4.0);
+	const ivec2 position = STPChunk::calcWorldChunkCoordinate(camera, chunk_size, scale);
+	CHECK(position == ivec2(-232, 210));
+	const dvec2 map_offset = STPChunk::calcChunkMapOffset(position, chunk_size, uvec2 { 512u, 256u }, dvec2(25.5, -57.5));
+	CHECK(map_offset == dvec2(-14822.5, 10694.5));
+	CHECK(static_cast<ivec2>(STPChunk::offsetChunk(ivec2(30, -30), chunk_size, ivec2(3, -2))) == ivec2(54, -40));
+	const uvec2 region { 5u, 7u };
+	const uvec2 l7 = STPChunk::calcLocalChunkCoordinate(7u, region), l12 = STPChunk::calcLocalChunkCoordinate(12u, region),
+		l20 = STPChunk::calcLocalChunkCoordinate(20u, region);
+	CHECK(l7.x == 2u && l7.y == 1u);
+	CHECK(l12.x == 2u && l12.y == 2u);
+	CHECK(l20.x == 0u && l20.y == 4u);
+	CHECK(static_cast<ivec2>(STPChunk::calcLocalChunkOrigin(ivec2(-24, 50), chunk_size, region)) == ivec2(-40, 35));
+	const auto offsets = STPChunk::calcChunkNeighbourOffset(chunk_size, region);
+	CHECK(offsets.size() == 35u);
+	CHECK(static_cast<ivec2>(offsets[0]) == ivec2(-16, -15));
+	CHECK(static_cast<ivec2>(offsets[9]) == ivec2(16, -10));
+	CHECK(static_cast<ivec2>(offsets[17]) == ivec2(0, 0));
+	CHECK(static_cast<ivec2>(offsets[23]) == ivec2(8, 5));
+	CHECK(static_cast<ivec2>(offsets[34]) == ivec2(16, 15));
+	CHECK(throws<STPException::STPNumericDomainError>([&] { STPChunk::calcLocalChunkCoordinate(1u, uvec2 { 0u, 3u }); }));
 }
 
 void splat_generator_errors() {
@@ -274,6 +317,7 @@ int main(int argc, char** argv) {
 	generator_errors();
 	biome_factory_errors();
 	splat_generator_errors();
+	chunk_coordinates();
 	if (!cpu_only) {
 		histogram_known_answer();
 		generator_round_trip();
