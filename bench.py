@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--batch", type=int, default=16)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-large-field", action="store_true",
-                   help="skip the 4096^2 large-field section")
+                   help="skip the 4096^2 large-field and the uneven-batch sections")
     p.add_argument("--serve-requests", type=int, default=600,
                    help="camera-walk requests replayed through the server (0 skips the serving section)")
     return p.parse_args()
@@ -356,10 +356,11 @@ def run_ours(args):
         serving["at_120_per_s"] = serve_section(m, np, torch, args.serve_requests, rate=120.0, plain=False)
         serving["layer_chain_biomes"] = serve_section(m, np, torch, args.serve_requests, layer=True, plain=False)
 
-    biomemap = splatmap = large = None
+    biomemap = splatmap = large = uneven = None
     if rank == 0:
         if not args.no_large_field:
             large = large_field_section(m, np, torch)
+            uneven = uneven_batch_section(m, np, torch)
         biomemap = biomemap_section(m, np, torch, B, cpu=world == 1 and not args.no_cpu_baseline)
         splatmap = splatmap_section(m, np, torch, batch, reqs, cpu=world == 1 and not args.no_cpu_baseline)
 
@@ -390,6 +391,7 @@ def run_ours(args):
             "biomemap": biomemap,
             "splatmap": splatmap,
             "large_field": large,
+            "uneven_batch": uneven,
             "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
@@ -442,6 +444,94 @@ def biomemap_section(m, np, torch, batch, cpu=True, reps=3):
         out["cpu_baseline"] = {"value": 1.0 / dt, "unit": f"{S}^2 biomemap chunks/s", "cores": 1, "kind": "port",
                                "sample": f"one {S}^2 chunk through the CPU restatement of the layer chain"}
     return out
+
+
+def uneven_requests(np, seed=31, count=64, table_biomes=16):
+    """64 independent eroded chunks: sides log-uniform 128-1024 (multiples of 32), an even filter
+    radius of 8-48, 2.3 droplets/px, brush radius 2-5, lifetime 30, 1-16 biomes each."""
+    rng = np.random.default_rng(seed)
+    reqs, biomes = [], []
+    for n in range(count):
+        side = int(np.exp(rng.uniform(np.log(128.0), np.log(1024.0))))
+        side = min(1024, max(128, 32 * int(round(side / 32.0))))
+        reqs.append(dict(MapSize=side, ChunkX=40 * n - 1000, ChunkY=7 * n - 200,
+                         InterpolationRadius=2 * int(rng.integers(4, 25)),
+                         DropletCount=int(round(2.3 * side * side)), BrushRadius=int(rng.integers(2, 6)),
+                         Lifetime=30))
+        biomes.append(int(rng.integers(1, table_biomes + 1)))
+    return reqs, biomes
+
+
+def uneven_batch_section(m, np, torch, reps=3):
+    """The uneven batch: 64 chunks of the shapes above in one autotuned CUDA graph of batched
+    launches, against the 64 plain per-chunk call sequences on the same resident data."""
+
+    class Ptr:
+        def __init__(self, p):
+            self.p = p
+
+        def data_ptr(self):
+            return self.p
+
+    reqs, biomes = uneven_requests(np)
+    rng = np.random.default_rng(31)
+    table = np.zeros(16, m.BIOME_DTYPE)
+    table["Scale"] = np.exp(rng.uniform(np.log(64.0), np.log(512.0), 16)).astype(np.float32)
+    table["Octave"] = rng.integers(4, 9, 16)
+    table["Persistence"] = 0.5
+    table["Lacunarity"] = 2.0
+    table["Variation"] = rng.uniform(0.2, 1.0, 16).astype(np.float32)
+    evap = 0.01
+    base = m.RaindropSetting(Seed=31, RainDropCount=1000, Inertia=0.05, SedimentCapacityFactor=4.0,
+                             minSedimentCapacity=0.01, initWaterVolume=1.0,
+                             minWaterVolume=m.lifetime_min_water_volume(1.0, evap, 30), Friction=0.1, initSpeed=1.0,
+                             ErodeSpeed=0.3, DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0, ErosionBrushRadius=3)
+    b = m.Batch(reqs, base, m.SimplexSetting(31, 8, 0.2181661565), table, graph=True)
+    b.synthesize(96, 31)
+    dev = m.DeviceOps()
+    for n, r in enumerate(reqs):
+        S = r["MapSize"]
+        dev.voronoi_biomemap(Ptr(b.buffers(n)[0]), 5 * S, 5 * S, 5 * S,
+                             ((r["ChunkX"] - 2) * S, (r["ChunkY"] - 2) * S), 96, biomes[n], 31)
+    torch.cuda.synchronize()
+    b.tune()
+    choice, tune_ms = b.tuning()
+    st = torch.cuda.current_stream()
+    for _ in range(3):
+        b.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        b.run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / reps
+    stage_ms = []
+    for stage in range(4):
+        b.run_stage(stage)
+        e0.record(st)
+        b.run_stage(stage)
+        e1.record(st)
+        torch.cuda.synchronize()
+        stage_ms.append(e0.elapsed_time(e1))
+    b.run_plain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run_plain()
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t0) * 1000.0
+    b.status()
+    px = sum(r["MapSize"] ** 2 for r in reqs)
+    return {"workload": "64 chunks, sides log-uniform 128-1024 (x32), 1-16 biomes, filter radius 8-48, "
+                        "2.3 droplets/px, brush 2-5, lifetime 30; %.1f M centre-chunk pixels, %.1f M droplets"
+                        % (px / 1e6, sum(r["DropletCount"] for r in reqs) / 1e6),
+            "batched_ms": batched_ms, "plain_ms": plain_ms, "batched_vs_plain": plain_ms / batched_ms,
+            "chunks_per_s": 64 * 1000.0 / batched_ms, "plain_chunks_per_s": 64 * 1000.0 / plain_ms,
+            "stage_ms": dict(zip(["single_histogram_filter", "multibiome_noise", "hydraulic_erosion", "format"],
+                                 stage_ms)),
+            "autotune_dominant_group": {"lanes_per_droplet": choice[0], "droplets_per_group": choice[1],
+                                        "brush_rows": bool(choice[2])}}
 
 
 def large_field_section(m, np, torch, reps=3):

@@ -48,6 +48,60 @@ struct RequestLayout {
 	size_t end;
 };
 
+// Erosion variant groups: requests that may take several lanes per droplet
+// (erosion_variant_stable) and whose brush takes the row kernel
+// (rows_max_lanes() >= 2); requests that may take several lanes but whose
+// brush is too small for rows (radius 2); and requests too densely packed for
+// anything but the one-lane reference kernel.  Each group has its own job
+// array, kernel variant and autotuning, and the erosion stage launches the
+// groups side by side.  One variant for the whole batch would hold every
+// request to the most restricted one: a single radius-2 brush, or one small
+// chunk with all of its droplets in flight, would put them all on the
+// point-wise kernels.
+struct ErosionGroup {
+	std::vector<uint32_t> members; // request indices
+	std::vector<ErosionJob> h;
+	ErosionJob* jobs = nullptr;    // device copy of h
+	uint32_t max_count = 0u, max_brush = 0u;
+	uint32_t lane_limit = 32u;     // max_lanes() of the smallest brush
+	uint32_t rows_limit = 4u;      // rows_max_lanes() of the smallest brush
+	uint32_t min_radius = 0xFFFFFFFFu;
+	// largest droplet density (droplets per centre-chunk pixel); the
+	// autotuner only tries the variants stable at this density
+	double density = 0.0;
+	double in_flight = 0.0; // largest droplets in flight per pixel
+	uint64_t droplets = 0u;
+	uint32_t lanes = 8u; // lanes per droplet
+	uint32_t dpg = 1u;   // droplets per lane group
+	bool rows = true;    // brush rows in 16-byte blocks
+	// autotuner's erosion time per candidate, [rows 0, 1][lanes 1..32][droplets 1, 2, 4] (0 = not tried)
+	float tune_ms[36] = {};
+
+	void add(const uint32_t n, const ErosionJob& e, const uint32_t radius, const double d, const double f) {
+		members.push_back(n);
+		h.push_back(e);
+		max_count = std::max(max_count, e.count);
+		max_brush = std::max(max_brush, e.brush_size);
+		lane_limit = std::min(lane_limit, max_lanes(e.brush_size));
+		rows_limit = std::min(rows_limit, rows_max_lanes(radius));
+		min_radius = std::min(min_radius, radius);
+		density = std::max(density, d);
+		in_flight = std::max(in_flight, f);
+		droplets += e.count;
+		// the default until the autotuner runs: brush rows with two lanes where
+		// stable, else several lanes point by point, else the reference kernel
+		const bool multi = erosion_variant_stable(2u, 1u, true, density, in_flight);
+		rows = multi && rows_limit != 0u;
+		lanes = rows ? 2u : multi ? std::min(8u, lane_limit) : 1u;
+		dpg = 1u;
+	}
+
+	int launch(cudaStream_t s) const {
+		return erosion_launch(jobs, h[0], static_cast<uint32_t>(h.size()), max_count, max_brush, s, lanes, false, dpg,
+			rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes));
+	}
+};
+
 } // namespace
 
 struct stpgb_batch {
@@ -68,27 +122,22 @@ struct stpgb_batch {
 	// job arrays (device) and launch bounds
 	ShfJob* shf_jobs = nullptr;
 	NoiseJob* noise_jobs = nullptr;
-	ErosionJob* ero_jobs = nullptr;
 	FormatJob* fmt_jobs = nullptr;
 	std::vector<ShfJob> shf_h;
 	std::vector<NoiseJob> noise_h;
-	std::vector<ErosionJob> ero_h;
+	std::vector<ErosionJob> ero_h; // per request, request order (the plain sequence)
 	std::vector<FormatJob> fmt_h;
-	uint32_t max_S = 0u, max_r = 0u, max_count = 0u, max_brush = 0u, kcap_v = 0u, kcap_h = 0u;
-	uint32_t lanes = 8u;       // lanes per droplet of the erosion kernel
-	uint32_t lane_limit = 32u; // max_lanes() of the smallest brush in the batch
-	uint32_t dpg = 1u;         // droplets per lane group
-	// brush rows in 16-byte blocks (every merged map of a batch is 256-byte
-	// aligned with a pitch of 3 * MapSize, a multiple of 24 floats), with at
-	// most rows_limit lanes: rows_max_lanes() of the smallest brush
-	bool rows = true;
-	uint32_t rows_limit = 4u;
-	uint32_t min_radius = 0xFFFFFFFFu; // smallest brush radius of the batch
-	// largest droplet density (droplets per centre-chunk pixel) of the batch;
-	// the autotuner only tries the variants stable at this density
-	double density = 0.0;
-	// autotuner's erosion time per candidate, [rows 0, 1][lanes 1..32][droplets 1, 2, 4] (0 = not tried)
-	float tune_ms[36] = {};
+	uint32_t max_S = 0u, max_r = 0u, kcap_v = 0u, kcap_h = 0u;
+	// erosion variant groups (brush rows in 16-byte blocks need aligned maps:
+	// every merged map of a batch is 512-byte aligned with a pitch of
+	// 3 * MapSize, a multiple of 24 floats); group_of[n] is request n's group
+	ErosionGroup grp[3];
+	uint32_t ngroups = 0u;
+	std::vector<uint32_t> group_of;
+	// launch streams of the second and third group, and the events that fork
+	// them from the batch's stream and join them back
+	cudaStream_t aux[2] = { nullptr, nullptr };
+	cudaEvent_t fork = nullptr, join[2] = { nullptr, nullptr };
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	bool use_graph = false;
@@ -132,12 +181,54 @@ struct stpgb_batch {
 		for (void* p : { static_cast<void*>(mem), static_cast<void*>(perm), static_cast<void*>(grad),
 				 static_cast<void*>(table), static_cast<void*>(residual), static_cast<void*>(status),
 				 static_cast<void*>(counters),
-				 static_cast<void*>(shf_jobs), static_cast<void*>(noise_jobs), static_cast<void*>(ero_jobs),
-				 static_cast<void*>(fmt_jobs) }) {
+				 static_cast<void*>(shf_jobs), static_cast<void*>(noise_jobs), static_cast<void*>(grp[0].jobs),
+				 static_cast<void*>(grp[1].jobs), static_cast<void*>(grp[2].jobs), static_cast<void*>(fmt_jobs) }) {
 			if (p) {
 				cudaFree(p);
 			}
 		}
+		if (fork) {
+			cudaEventDestroy(fork);
+		}
+		for (int k = 0; k < 2; k++) {
+			if (join[k]) {
+				cudaEventDestroy(join[k]);
+			}
+			if (aux[k]) {
+				cudaStreamDestroy(aux[k]);
+			}
+		}
+	}
+
+	// the erosion stage: one launch per group, the later groups on their own
+	// streams so that the groups run side by side
+	int erode(cudaStream_t s) {
+		if (ngroups == 1u) {
+			return grp[0].launch(s);
+		}
+		STPGB_CUDA_TRY(cudaEventRecord(fork, s));
+		for (uint32_t g = 1u; g < ngroups; g++) {
+			STPGB_CUDA_TRY(cudaStreamWaitEvent(aux[g - 1u], fork, 0));
+		}
+		int rc = grp[0].launch(s);
+		for (uint32_t g = 1u; g < ngroups; g++) {
+			const int rg = grp[g].launch(aux[g - 1u]);
+			rc = rc != STPGB_OK ? rc : rg;
+			STPGB_CUDA_TRY(cudaEventRecord(join[g - 1u], aux[g - 1u]));
+			STPGB_CUDA_TRY(cudaStreamWaitEvent(s, join[g - 1u], 0));
+		}
+		return rc;
+	}
+
+	// the group the tuning report describes: the one with the most droplets
+	const ErosionGroup& dominant() const {
+		uint32_t best = 0u;
+		for (uint32_t g = 1u; g < ngroups; g++) {
+			if (grp[g].droplets > grp[best].droplets) {
+				best = g;
+			}
+		}
+		return grp[best];
 	}
 
 	// the whole pipeline as a fixed launch sequence
@@ -160,8 +251,7 @@ struct stpgb_batch {
 			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
 				table, biome_count, s);
 		case 2u:
-			return erosion_launch(ero_jobs, ero_h[0], static_cast<uint32_t>(req.size()), max_count, max_brush, s, lanes,
-				false, dpg, rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes));
+			return erode(s);
 		case 3u:
 			return format_batch_launch(fmt_jobs, static_cast<uint32_t>(req.size()), 3u * max_S, 3u * max_S, s);
 		default:
@@ -169,9 +259,9 @@ struct stpgb_batch {
 		}
 	}
 
-	// Autotuner: times the erosion stage of this batch with every candidate
-	// lane count (noise regenerates the heights before each trial, so every
-	// trial erodes the same map) and keeps the fastest.
+	// Autotuner: times each group's erosion launch with every candidate
+	// variant (noise regenerates the heights before each trial, so every
+	// trial erodes the same map) and keeps the fastest per group.
 	int autotune() {
 		cudaStream_t s;
 		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
@@ -179,55 +269,58 @@ struct stpgb_batch {
 		STPGB_CUDA_TRY(cudaEventCreate(&e0));
 		STPGB_CUDA_TRY(cudaEventCreate(&e1));
 		int rc = stage(0u, s);
-		float best = 0.0f;
-		uint32_t best_lanes = lanes, best_dpg = dpg;
-		bool best_rows = rows;
 		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
 		const uint32_t dcands[3] = { 1u, 2u, 4u };
-		for (int c = 0; c < 36 && rc == STPGB_OK; c++) {
-			const bool cr = c >= 18;
-			const uint32_t cl = cands[(c % 18) / 3], cd = dcands[c % 3];
-			// lane counts above the brush limit, and several droplets per group
-			// below four lanes or above sixteen, are not candidates; brush rows
-			// run with 2 or 4 lanes (up to rows_limit) and 1 or 2 droplets
-			if (!cr && (cl > lane_limit || (cd > 1u && (cl < 4u || cl > 16u)))) {
-				continue;
-			}
-			if (cr && (cl < 2u || cl > rows_limit || cd > 2u)) {
-				continue;
-			}
-			if (!erosion_variant_stable(cl, cd, cr, density)) {
-				continue;
-			}
-			lanes = cl;
-			dpg = cd;
-			rows = cr;
-			float t = 0.0f;
-			for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
-				rc = stage(1u, s);
-				if (rc == STPGB_OK) {
-					cudaEventRecord(e0, s);
-					rc = stage(2u, s);
-					cudaEventRecord(e1, s);
+		for (uint32_t gi = 0u; gi < ngroups && rc == STPGB_OK; gi++) {
+			ErosionGroup& G = grp[gi];
+			float best = 0.0f;
+			uint32_t best_lanes = G.lanes, best_dpg = G.dpg;
+			bool best_rows = G.rows;
+			for (int c = 0; c < 36 && rc == STPGB_OK; c++) {
+				const bool cr = c >= 18;
+				const uint32_t cl = cands[(c % 18) / 3], cd = dcands[c % 3];
+				// lane counts above the brush limit, and several droplets per group
+				// below four lanes or above sixteen, are not candidates; brush rows
+				// run with 2 or 4 lanes (up to rows_limit) and 1 or 2 droplets
+				if (!cr && (cl > G.lane_limit || (cd > 1u && (cl < 4u || cl > 16u)))) {
+					continue;
 				}
-				if (cudaStreamSynchronize(s) != cudaSuccess) {
-					rc = cuda_fail(cudaGetLastError(), "autotune");
+				if (cr && (cl < 2u || cl > G.rows_limit || cd > 2u)) {
+					continue;
 				}
-				float ms = 0.0f;
-				cudaEventElapsedTime(&ms, e0, e1);
-				t = rep == 0 ? ms : std::min(t, ms);
+				if (!erosion_variant_stable(cl, cd, cr, G.density, G.in_flight)) {
+					continue;
+				}
+				G.lanes = cl;
+				G.dpg = cd;
+				G.rows = cr;
+				float t = 0.0f;
+				for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
+					rc = stage(1u, s);
+					if (rc == STPGB_OK) {
+						cudaEventRecord(e0, s);
+						rc = G.launch(s);
+						cudaEventRecord(e1, s);
+					}
+					if (cudaStreamSynchronize(s) != cudaSuccess) {
+						rc = cuda_fail(cudaGetLastError(), "autotune");
+					}
+					float ms = 0.0f;
+					cudaEventElapsedTime(&ms, e0, e1);
+					t = rep == 0 ? ms : std::min(t, ms);
+				}
+				G.tune_ms[c] = t;
+				if (rc == STPGB_OK && (best == 0.0f || t < best)) {
+					best = t;
+					best_lanes = cl;
+					best_dpg = cd;
+					best_rows = cr;
+				}
 			}
-			tune_ms[c] = t;
-			if (rc == STPGB_OK && (best == 0.0f || t < best)) {
-				best = t;
-				best_lanes = cl;
-				best_dpg = cd;
-				best_rows = cr;
-			}
+			G.lanes = best_lanes;
+			G.dpg = best_dpg;
+			G.rows = best_rows;
 		}
-		lanes = best_lanes;
-		dpg = best_dpg;
-		rows = best_rows;
 		cudaEventDestroy(e0);
 		cudaEventDestroy(e1);
 		cudaStreamDestroy(s);
@@ -248,9 +341,10 @@ struct stpgb_batch {
 				STPGB_CUDA_TRY(cudaStreamSynchronize(s));
 			}
 			const ErosionJob& e = ero_h[n];
+			const ErosionGroup& G = grp[group_of[n]];
 			STPGB_CUDA_TRY(cudaMemsetAsync(e.residual, 0, sizeof(double), s));
-			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, lanes, false, dpg, rows,
-				erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes)));
+			STPGB_TRY(erosion_launch(nullptr, e, 1u, e.count, e.brush_size, s, G.lanes, false, G.dpg, G.rows,
+				erosion_rows_wide(G.min_radius), erosion_rows_atomic(G.min_radius, G.lanes)));
 			const FormatJob& f = fmt_h[n];
 			STPGB_TRY(format_launch(f.in, f.in_pitch, f.out, f.out_pitch, f.W, f.H, s));
 			STPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -302,7 +396,6 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		STPGB_TRY(check_request(r));
 		b->max_S = std::max(b->max_S, r.MapSize);
 		b->max_r = std::max(b->max_r, r.InterpolationRadius);
-		b->max_count = std::max(b->max_count, r.DropletCount);
 	}
 	b->kcap_v = shf_kcap_v(b->max_r, b->max_items);
 	b->kcap_h = shf_kcap_h(b->max_r, b->max_items);
@@ -328,16 +421,6 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		brush_i[n].resize(bs);
 		brush_w[n].resize(bs);
 		STPGB_TRY(stpgb_erosion_brush_generate(3u * r.MapSize, r.BrushRadius, brush_i[n].data(), brush_w[n].data(), bs, &bs));
-		b->max_brush = std::max(b->max_brush, bs);
-		b->lane_limit = std::min(b->lane_limit, max_lanes(bs));
-		b->rows_limit = std::min(b->rows_limit, rows_max_lanes(r.BrushRadius));
-		b->min_radius = std::min(b->min_radius, r.BrushRadius);
-		b->density = std::max(b->density, static_cast<double>(r.DropletCount) / (static_cast<double>(S) * S));
-		// the default until the autotuner runs: brush rows where stable, else
-		// several lanes point by point, above kDenseRows the reference kernel
-		b->rows = b->rows_limit != 0u && b->density <= kDenseRows;
-		b->lanes = b->rows ? 2u : b->density <= kDenseRows ? std::min(8u, b->lane_limit) : 1u;
-		b->dpg = 1u;
 		L.brush_idx = off;
 		off += al(bs * sizeof(int32_t));
 		L.brush_w = off;
@@ -450,11 +533,45 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		e.fixed = reinterpret_cast<uint16_t*>(m + L.fixed);
 		b->ero_h.push_back(e);
 		b->fmt_h.push_back(FormatJob { height, 3ull * S, e.fixed, 3ull * S, 3u * S, 3u * S });
+		const double area = static_cast<double>(S) * S;
+		const double density = r.DropletCount / area, in_flight = erosion_in_flight(r.DropletCount, area);
+		const uint32_t cls = !erosion_variant_stable(2u, 1u, true, density, in_flight) ? 2u
+			: rows_max_lanes(r.BrushRadius) != 0u                                        ? 0u
+																						  : 1u;
+		b->group_of.push_back(cls);
+		b->grp[cls].add(n, e, r.BrushRadius, density, in_flight);
+	}
+	{
+		// the non-empty groups first, in their order
+		uint32_t remap[3] = { 0u, 0u, 0u }, k = 0u;
+		ErosionGroup packed[3];
+		for (uint32_t g = 0u; g < 3u; g++) {
+			if (!b->grp[g].h.empty()) {
+				remap[g] = k;
+				packed[k++] = std::move(b->grp[g]);
+			}
+		}
+		for (uint32_t g = 0u; g < 3u; g++) {
+			b->grp[g] = std::move(packed[g]);
+		}
+		for (auto& g : b->group_of) {
+			g = remap[g];
+		}
+		b->ngroups = k;
 	}
 	STPGB_TRY(upload(b->shf_jobs, b->shf_h));
 	STPGB_TRY(upload(b->noise_jobs, b->noise_h));
-	STPGB_TRY(upload(b->ero_jobs, b->ero_h));
+	for (uint32_t g = 0u; g < b->ngroups; g++) {
+		STPGB_TRY(upload(b->grp[g].jobs, b->grp[g].h));
+	}
 	STPGB_TRY(upload(b->fmt_jobs, b->fmt_h));
+	if (b->ngroups > 1u) {
+		STPGB_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+		for (uint32_t g = 1u; g < b->ngroups; g++) {
+			STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&b->aux[g - 1u], cudaStreamNonBlocking));
+			STPGB_CUDA_TRY(cudaEventCreateWithFlags(&b->join[g - 1u], cudaEventDisableTiming));
+		}
+	}
 
 	if (flags & STPGB_BATCH_AUTOTUNE) {
 		STPGB_TRY(b->autotune());
@@ -615,18 +732,19 @@ int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32
 	if (!b) {
 		return inval("stpgb_batch_tuning: null batch");
 	}
+	const ErosionGroup& G = b->dominant();
 	if (lanes_per_droplet) {
-		*lanes_per_droplet = b->lanes;
+		*lanes_per_droplet = G.lanes;
 	}
 	if (droplets_per_group) {
-		*droplets_per_group = b->dpg;
+		*droplets_per_group = G.dpg;
 	}
 	if (vector_rows) {
-		*vector_rows = b->rows ? 1u : 0u;
+		*vector_rows = G.rows ? 1u : 0u;
 	}
 	if (erosion_ms) {
 		for (int c = 0; c < 36; c++) {
-			erosion_ms[c] = b->tune_ms[c];
+			erosion_ms[c] = G.tune_ms[c];
 		}
 	}
 	return STPGB_OK;

@@ -1013,12 +1013,17 @@ uint32_t rows_max_lanes(uint32_t radius) {
 // and falls up to 0.1 below it at 7 (brush 3, four lanes); without the clamp
 // brush 3 ran away to -10^5 at 2.7 to 3.  Four lanes point by point went out
 // of range at 4.9 in some runs; one lane per droplet (the reference kernel)
-// holds at 7.  Above kDenseRows only the reference kernel is used.
+// holds at 7.  Above kDenseRows, or kDenseInFlight droplets in flight per
+// pixel, only the reference kernel is used.
 bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_group, const bool rows,
-	const double density) {
+	const double density, const double in_flight) {
 	(void)droplets_per_group;
 	(void)rows;
-	return lanes == 1u || density <= kDenseRows;
+	return lanes == 1u || (density <= kDenseRows && in_flight <= kDenseInFlight);
+}
+
+double erosion_in_flight(const uint32_t count, const double area) {
+	return area > 0.0 ? std::min<double>(count, erosion_resident_droplets(2u, 1u)) / area : 0.0;
 }
 
 uint32_t erosion_resident_droplets(const uint32_t lanes, const uint32_t dpg) {
@@ -1042,8 +1047,8 @@ bool erosion_rows_atomic(const uint32_t min_radius, const uint32_t lanes) {
 }
 
 ErosionChoice erosion_choice(const uint32_t radius, const uint32_t brush_size, const double density,
-	const bool rows_allowed) {
-	if (density > kDenseRows) {
+	const double in_flight, const bool rows_allowed) {
+	if (!erosion_variant_stable(2u, 1u, true, density, in_flight)) {
 		return ErosionChoice { 1u, 1u, false };
 	}
 	// brush rows with two lanes per droplet where the brush allows rows: with
@@ -1269,7 +1274,8 @@ int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn, const 
 	const double area = static_cast<double>(nn->MapSize[0]) * nn->MapSize[1];
 	const double density = static_cast<double>(count) / area;
 	if (lanes == 0u) {
-		const ErosionChoice c = erosion_choice(setting->ErosionBrushRadius, brush_size, density, rows);
+		const ErosionChoice c = erosion_choice(setting->ErosionBrushRadius, brush_size, density,
+			erosion_in_flight(count, area), rows);
 		lanes = c.lanes;
 		rows = c.rows;
 	}
@@ -1285,7 +1291,8 @@ int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area
 	}
 	uint32_t bs = 0u;
 	stpgb_erosion_brush_generate(4u * brush_radius + 4u, brush_radius, nullptr, nullptr, 0u, &bs);
-	const ErosionChoice c = erosion_choice(brush_radius, bs, static_cast<double>(droplets) / area, true);
+	const ErosionChoice c = erosion_choice(brush_radius, bs, static_cast<double>(droplets) / area,
+		erosion_in_flight(droplets, area), true);
 	*lanes_per_droplet = c.lanes;
 	if (vector_rows) {
 		*vector_rows = c.rows ? 1u : 0u;

@@ -66,11 +66,22 @@ uint32_t rows_max_lanes(uint32_t radius);
 
 // Racing droplets that share cells can dig a channel below its neighbours
 // once they are packed densely enough; how densely depends on how compressed
-// in time a droplet's brush update is.  Up to kDenseRows droplets per pixel
-// of the start area every variant stays in range; beyond it only one lane per
-// droplet (the reference kernel) is used.
+// in time a droplet's brush update is.  Variants with several lanes per
+// droplet are taken up to kDenseRows droplets per pixel of the start area and
+// up to kDenseInFlight droplets in flight at once per pixel (min(droplets,
+// resident droplets of the two-lane row kernel) / area); beyond either only
+// one lane per droplet (the reference kernel) is used.  Ten-run tests on
+// 64^2 chunks kept every variant in range up to 3 droplets per pixel, all in
+// flight, but across many runs the two-lane row kernel fell below range
+// twice with every droplet in flight: once at 3 per pixel (brush 4), once
+// at 2.3 (a 128^2 chunk in a batch); the reference kernel never has, up to 7.
+// The production chunk keeps 0.33 in flight per pixel, a 256^2 chunk at
+// 2.3 per pixel 1.34.
 constexpr double kDenseRows = 3.0;
-bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density);
+constexpr double kDenseInFlight = 1.5;
+// Droplets in flight per pixel of `area` for `count` droplets.
+double erosion_in_flight(uint32_t count, double area);
+bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density, double in_flight);
 
 // Several brush blocks per round trip compress a droplet's brush update
 // further, which moves the racy result away from the serial one where many
@@ -109,8 +120,10 @@ struct ErosionChoice {
 	uint32_t lanes, droplets_per_group;
 	bool rows;
 };
-// Default kernel for a brush of `radius` (`brush_size` points) at `density`.
-ErosionChoice erosion_choice(uint32_t radius, uint32_t brush_size, double density, bool rows_allowed);
+// Default kernel for a brush of `radius` (`brush_size` points) at `density`
+// droplets per pixel of the start area, `in_flight` of them at once.
+ErosionChoice erosion_choice(uint32_t radius, uint32_t brush_size, double density, double in_flight,
+	bool rows_allowed);
 
 int format_launch(const float* in, uint64_t in_pitch, uint16_t* out, uint64_t out_pitch, uint32_t W, uint32_t H,
 	cudaStream_t stream);

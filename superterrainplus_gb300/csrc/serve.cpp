@@ -501,7 +501,7 @@ struct stpgb_server {
 
 		uint32_t maxS = 0u, maxR = 0u, maxRS = 0u, maxCount = 0u, maxBrush = 0u, minBrush = 0xFFFFFFFFu,
 			minRadius = 0xFFFFFFFFu;
-		double maxDensity = 0.0;
+		double maxDensity = 0.0, maxInFlight = 0.0;
 		size_t so = it.scratch_off;
 		for (size_t j = 0; j < ng; j++) {
 			const ChunkKey& k = it.generated[j];
@@ -599,6 +599,7 @@ struct stpgb_server {
 			minBrush = std::min(minBrush, bsize);
 			minRadius = std::min(minRadius, r.req.BrushRadius);
 			maxDensity = std::max(maxDensity, static_cast<double>(r.droplets) / (static_cast<double>(S) * S));
+			maxInFlight = std::max(maxInFlight, erosion_in_flight(r.droplets, static_cast<double>(S) * S));
 		}
 		std::fill(it.residual_host, it.residual_host + nr, 0.0);
 		*it.status_host = 0u;
@@ -627,8 +628,11 @@ struct stpgb_server {
 		// group; each job reads several blocks per round trip where few of its
 		// droplets are in flight per pixel.  The stable point-wise variant with
 		// two droplets per group where rows are not allowed
-		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, true);
-		const uint32_t dpg = !ec.rows && ec.lanes >= 4u && erosion_variant_stable(ec.lanes, 2u, false, maxDensity) ? 2u : 1u;
+		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, maxInFlight, true);
+		const uint32_t dpg = !ec.rows && ec.lanes >= 4u
+				&& erosion_variant_stable(ec.lanes, 2u, false, maxDensity, maxInFlight)
+			? 2u
+			: 1u;
 		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
 			maxBrush, s, ec.lanes, false, dpg, ec.rows, erosion_rows_wide(minRadius),
 			erosion_rows_atomic(minRadius, ec.lanes)));

@@ -141,19 +141,23 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
         _capi.lib()
 
 
-@pytest.mark.parametrize("radius,density,lanes,rows", [
-    (4, 600000 / 512**2, 2, 1),  # the production chunk: brush rows, two lanes
-    (5, 2.3, 2, 1),
-    (3, 2.3, 2, 1),
-    (2, 2.3, 2, 0),              # brush 2 is too small for row blocks
-    (4, 4.0, 1, 0),              # above 3 droplets per pixel: one lane per droplet, the reference kernel
-    (3, 4.9, 1, 0),
-    (4, 7.0, 1, 0),
+@pytest.mark.parametrize("radius,droplets,side,lanes,rows", [
+    (4, 600000, 512, 2, 1),          # the production chunk (0.33 in flight per pixel): brush rows, two lanes
+    (5, 150733, 256, 2, 1),          # 2.3 per pixel of a 256^2 chunk, 1.34 in flight
+    (3, 150733, 256, 2, 1),
+    (2, 150733, 256, 2, 0),          # brush 2 is too small for row blocks
+    (4, 9421, 64, 1, 0),             # 2.3 per pixel of a 64^2 chunk, all in flight: the reference kernel
+    (3, 6144, 64, 2, 1),             # 1.5 in flight per pixel, the limit of the several-lane variants
+    (4, 1048576, 512, 1, 0),         # above 3 droplets per pixel: one lane per droplet, the reference kernel
+    (3, 20070, 64, 1, 0),
+    (4, 28672, 64, 1, 0),
 ])
-def test_erosion_choice_follows_density(stpgb, radius, density, lanes, rows):
+def test_erosion_choice_follows_density(stpgb, radius, droplets, side, lanes, rows):
+    """Several lanes per droplet up to 3 droplets per pixel of the start area and 1.5 in flight at once
+    (the two-lane row kernel keeps 152 SMs x 9 blocks x 64 droplets resident; no GPU here, so the SM
+    count of the GB300 is taken)."""
     import ctypes as C
-    area = 64 * 64
+    area = side * side
     got_lanes, got_rows = C.c_uint32(0), C.c_uint32(0)
-    stpgb.check(stpgb.lib().stpgb_erosion_choice(radius, int(round(density * area)), area, C.byref(got_lanes),
-                                                 C.byref(got_rows)))
+    stpgb.check(stpgb.lib().stpgb_erosion_choice(radius, droplets, area, C.byref(got_lanes), C.byref(got_rows)))
     assert (got_lanes.value, got_rows.value) == (lanes, rows)

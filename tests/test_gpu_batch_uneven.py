@@ -105,14 +105,23 @@ def test_uneven_batch_full_size(stpgb, dev, oracle):
     choice, ms = b.tuning()
     assert choice in ms
     print(f"uneven batch: autotuner chose {choice} from {ms}")
+    failures = []
     for run in (b.run, b.run_plain):
         run()
         after, fixed, res = heights()
-        for n in range(COUNT):
+        for n, r in enumerate(reqs):
             t0 = before[n].astype(np.float64).sum()
             bal = (t0 - after[n].astype(np.float64).sum()) - res[n]
-            assert abs(bal) <= 1e-5 * t0, (run.__name__, n, bal)
-            assert np.isfinite(after[n]).all()
-            assert after[n].min() >= before[n].min() - 1e-3 and after[n].max() <= before[n].max() + 1e-3
-            assert not np.array_equal(before[n], after[n])
-            assert np.array_equal(fixed[n], oracle.format(after[n])), (run.__name__, n)
+            what = (run.__name__, n, r["MapSize"], r["BrushRadius"])
+            if not abs(bal) <= 1e-5 * t0:
+                failures.append(what + ("mass balance", bal))
+            if not np.isfinite(after[n]).all():
+                failures.append(what + ("not finite",))
+            elif not (after[n].min() >= before[n].min() - 1e-3 and after[n].max() <= before[n].max() + 1e-3):
+                failures.append(what + ("out of range", float(after[n].min() - before[n].min()),
+                                        float(after[n].max() - before[n].max())))
+            if np.array_equal(before[n], after[n]):
+                failures.append(what + ("not eroded",))
+            if not np.array_equal(fixed[n], oracle.format(after[n])):
+                failures.append(what + ("format",))
+    assert not failures, failures
