@@ -59,7 +59,6 @@ struct RequestLayout {
 // chunk with all of its droplets in flight, would put them all on the
 // point-wise kernels.
 struct ErosionGroup {
-	std::vector<uint32_t> members; // request indices
 	std::vector<ErosionJob> h;
 	ErosionJob* jobs = nullptr;    // device copy of h
 	uint32_t max_count = 0u, max_brush = 0u;
@@ -77,8 +76,7 @@ struct ErosionGroup {
 	// autotuner's erosion time per candidate, [rows 0, 1][lanes 1..32][droplets 1, 2, 4] (0 = not tried)
 	float tune_ms[36] = {};
 
-	void add(const uint32_t n, const ErosionJob& e, const uint32_t radius, const double d, const double f) {
-		members.push_back(n);
+	void add(const ErosionJob& e, const uint32_t radius, const double d, const double f) {
 		h.push_back(e);
 		max_count = std::max(max_count, e.count);
 		max_brush = std::max(max_brush, e.brush_size);
@@ -539,7 +537,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 			: rows_max_lanes(r.BrushRadius) != 0u                                        ? 0u
 																						  : 1u;
 		b->group_of.push_back(cls);
-		b->grp[cls].add(n, e, r.BrushRadius, density, in_flight);
+		b->grp[cls].add(e, r.BrushRadius, density, in_flight);
 	}
 	{
 		// the non-empty groups first, in their order
