@@ -308,7 +308,11 @@ STPGB_API int stpgb_hydraulic_erosion(float* heightmap, const stpgb_nn_info* nn,
  * 3/4), a lane reads up to three blocks of a run per round trip.  The default
  * runs brush rows with two lanes per droplet (row blocks need at least four
  * points or blocks per lane; with fewer a step's reads happen nearly together
- * and densely packed droplets can run the map away).
+ * and densely packed droplets can run the map away), and, where few droplets
+ * are in flight per pixel, the warp-cooperative row kernel: one droplet per
+ * lane, the brush runs of a warp's eroding droplets shared out over all 32
+ * lanes, each run's blocks taken by returning atomics (lanes_per_droplet = 1
+ * without STPGB_EROSION_POINTWISE selects it explicitly).
  * STPGB_EROSION_POINTWISE keeps the point-by-point kernels.
  * STPGB_EROSION_EXACT_CLAMP erodes each point by compare-and-swap instead, so
  * racing droplets never remove more than a cell holds (closer to the serial
@@ -320,9 +324,11 @@ enum { STPGB_EROSION_EXACT_CLAMP = 1, STPGB_EROSION_POINTWISE = 2 };
  * `droplets` over `area` pixels (the chunk the starts cover).  Racing
  * droplets packed densely enough dig channels without bound, and the faster
  * a droplet's brush update completes, the lower that density: up to 3
- * droplets per pixel brush rows are taken (lanes keeping four 16-byte blocks
- * each; point by point for brushes too small for that), beyond it one lane
- * per droplet (the reference kernel).  No counterpart in the reference. */
+ * droplets per pixel and 1.5 in flight at once brush rows are taken (the
+ * warp-cooperative kernel up to 0.2 in flight, reported as 1 lane with
+ * rows; else lanes keeping four 16-byte blocks each; point by point for
+ * brushes too small for that), beyond it one lane per droplet (the reference
+ * kernel).  No counterpart in the reference. */
 STPGB_API int stpgb_erosion_choice(uint32_t brush_radius, uint32_t droplets, uint32_t area,
 	uint32_t* lanes_per_droplet, uint32_t* vector_rows);
 STPGB_API int stpgb_hydraulic_erosion_ex(float* heightmap, const stpgb_nn_info* nn,

@@ -86,11 +86,16 @@ struct ErosionGroup {
 		density = std::max(density, d);
 		in_flight = std::max(in_flight, f);
 		droplets += e.count;
-		// the default until the autotuner runs: brush rows with two lanes where
-		// stable, else several lanes point by point, else the reference kernel
+		// the default until the autotuner runs: brush rows (the warp-cooperative
+		// kernel where it is stable, else two lanes per droplet), else several
+		// lanes point by point, else the reference kernel
 		const bool multi = erosion_variant_stable(2u, 1u, true, density, in_flight);
 		rows = multi && rows_limit != 0u;
-		lanes = rows ? 2u : multi ? std::min(8u, lane_limit) : 1u;
+		lanes = rows ? (erosion_variant_stable(1u, 1u, true, density, in_flight) && in_flight <= kCoopDefaultInFlight
+							   ? 1u
+							   : 2u)
+			: multi  ? std::min(8u, lane_limit)
+					 : 1u;
 		dpg = 1u;
 	}
 
@@ -279,11 +284,13 @@ struct stpgb_batch {
 				const uint32_t cl = cands[(c % 18) / 3], cd = dcands[c % 3];
 				// lane counts above the brush limit, and several droplets per group
 				// below four lanes or above sixteen, are not candidates; brush rows
-				// run with 2 or 4 lanes (up to rows_limit) and 1 or 2 droplets
+				// run with 2 or 4 lanes (up to rows_limit) and 1 or 2 droplets, or
+				// warp-cooperatively (1 lane, 1 droplet) where the brush allows rows
 				if (!cr && (cl > G.lane_limit || (cd > 1u && (cl < 4u || cl > 16u)))) {
 					continue;
 				}
-				if (cr && (cl < 2u || cl > G.rows_limit || cd > 2u)) {
+				if (cr && !(G.rows_limit != 0u
+							   && ((cl == 1u && cd == 1u) || (cl >= 2u && cl <= G.rows_limit && cd <= 2u)))) {
 					continue;
 				}
 				if (!erosion_variant_stable(cl, cd, cr, G.density, G.in_flight)) {

@@ -915,6 +915,274 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 	}
 }
 
+// One droplet per lane, the brush of every eroding droplet of a warp shared
+// out over all 32 lanes.  Phases 1 and 2 (the corners of the current and of
+// the new cell) are each lane's own four reads and twice as many droplets are
+// in flight per SM as with two lanes per droplet.  In phase 3 the runs of the
+// warp's eroding droplets form one task list -- (droplet, run) in the order
+// of the droplets' lanes, then of the runs -- that the lanes take 32 at a
+// time, so the lanes of depositing and finished droplets help and a step
+// costs ceil(tasks / 32) round trips instead of one per run of a lane.  A
+// run's 16-byte blocks are taken by returning vector atomics (the cells'
+// values at that moment, w subtracted, the part of w a cell lacked given
+// back): for the droplet this is c - min(max(c, 0), w) on the exact current
+// value whichever lane takes the run and in whatever order.  Each run's
+// eroded amount goes to a shared slot and the droplet's lane adds its runs up
+// in run order, so the droplet's sediment does not depend on which lane took
+// which run.  Every run of a droplet is in flight at once -- the brush update
+// is more compressed in time than with two lanes per droplet -- so the
+// default takes this kernel only where few droplets are in flight per pixel
+// (erosion_variant_stable).  Needs what the row kernel needs: a 16-byte
+// aligned map whose pitch is a multiple of four floats.
+constexpr int32_t kCoopTrip = 3; // blocks of a run per round trip
+
+__global__ void __launch_bounds__(kErodeBlock, 9) erosion_coop_kernel(const ErosionJob* __restrict__ jobs,
+	const ErosionJob single, const uint32_t runcap) {
+	constexpr uint32_t kWarps = kErodeBlock / 32u;
+	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
+	extern __shared__ __align__(16) unsigned char esm[];
+	int32_t* const bidx = reinterpret_cast<int32_t*>(esm);
+	float* const bw = reinterpret_cast<float*>(esm) + J.brush_size;
+	int2* const runs = reinterpret_cast<int2*>(esm + ((8u * J.brush_size + 7u) & ~7u)); // (first point, length)
+	float* const parts = reinterpret_cast<float*>(runs + runcap);                         // [warp][32 * runcap]
+	__shared__ uint32_t slot_cell[kWarps][32];
+	__shared__ float slot_ero[kWarps][32];
+	__shared__ uint32_t nruns;
+	for (uint32_t k = threadIdx.x; k < J.brush_size; k += kErodeBlock) {
+		bidx[k] = J.brush_index[k];
+		bw[k] = J.brush_weight[k];
+	}
+	__syncthreads();
+	if (threadIdx.x == 0u) {
+		uint32_t n = 0u;
+		for (uint32_t p = 0u; p < J.brush_size; p++) {
+			if (p == 0u || bidx[p] != bidx[p - 1u] + 1) {
+				if (n < runcap) {
+					runs[n] = make_int2(static_cast<int32_t>(p), 0);
+				}
+				n++;
+			}
+			if (n <= runcap) {
+				runs[n - 1u].y++;
+			}
+		}
+		nruns = n;
+	}
+	__syncthreads();
+	if (nruns > runcap) {
+		// a brush of more runs than the shared slots were sized for (never one
+		// made by stpgb_erosion_brush_generate): refused through the status word
+		if (threadIdx.x == 0u && J.status) {
+			atomicOr(J.status, STATUS_CAPACITY);
+		}
+		return;
+	}
+
+	const RainParams& P = J.p;
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	const uint32_t d = blockIdx.x * kErodeBlock + threadIdx.x;
+	const uint32_t nrun = nruns;
+	float* const wparts = parts + static_cast<size_t>(warp) * 32u * runcap;
+	float* const map = J.map;
+	// cell offsets in 32 bits: a map holds fewer than 2^32 cells (checked at launch)
+	const uint32_t pitch = static_cast<uint32_t>(J.pitch);
+	const float lo = static_cast<float>(P.BrushRadius);
+	const float hi_x = 1.0f * J.dim_x - P.BrushRadius, hi_y = 1.0f * J.dim_y - P.BrushRadius;
+	// cells whose brush (reach BrushRadius - 1) and deposit corners stay inside the map
+	const uint32_t safe_lo = P.BrushRadius - 1u, safe_hx = J.dim_x - max(P.BrushRadius, 2u),
+		safe_hy = J.dim_y - max(P.BrushRadius, 2u);
+
+	bool alive = d < J.count;
+	float px = alive ? J.starts[2u * d] : 0.0f, py = alive ? J.starts[2u * d + 1u] : 0.0f;
+	alive = alive && px >= 0.0f && px < J.dim_x - 1.0f && py >= 0.0f && py < J.dim_y - 1.0f;
+	float dirx = 0.0f, diry = 0.0f, speed = P.initSpeed, vol = P.initWaterVolume, sed = 0.0f;
+	uint32_t step = 0u;
+	float residual = 0.0f;
+	bool capped = false;
+	uint32_t steps_done = 0u, erode_steps = 0u;
+	auto corners = [&](const uint32_t cell) {
+		const float* const c = map + cell;
+		return make_float4(__ldcg(c), __ldcg(c + 1), __ldcg(c + pitch), __ldcg(c + pitch + 1));
+	};
+
+	while (true) {
+		if (alive && !(vol >= P.minWaterVolume)) {
+			alive = false;
+			residual += sed;
+		} else if (alive && step++ >= P.MaxSteps) {
+			alive = false;
+			capped = true;
+			residual += sed;
+		}
+		// the lanes of finished droplets stay for the shared brush phase
+		if (!__any_sync(0xFFFFFFFFu, alive)) {
+			break;
+		}
+		bool erode = false;
+		uint32_t mi = 0u;
+		float ero = 0.0f, dh = 0.0f;
+		if (alive) {
+			// phase 1: corners of the current cell (STPRainDrop.cu:23-51)
+			const uint32_t cx = static_cast<uint32_t>(px), cy = static_cast<uint32_t>(py);
+			const bool safe = cx >= safe_lo && cx <= safe_hx && cy >= safe_lo && cy <= safe_hy;
+			mi = cy * pitch + cx;
+			const float ox = px - static_cast<float>(cx), oy = py - static_cast<float>(cy);
+			const float4 q = corners(mi);
+			HG hg;
+			hg.h = q.x * (1.0f - ox) * (1.0f - oy) + q.y * ox * (1.0f - oy) + q.z * (1.0f - ox) * oy + q.w * ox * oy;
+			hg.gx = (q.y - q.x) * (1.0f - oy) + (q.w - q.z) * oy;
+			hg.gy = (q.z - q.x) * (1.0f - ox) + (q.w - q.y) * ox;
+			dirx = (-hg.gx) * (1.0f - P.Inertia) + dirx * P.Inertia;
+			diry = (-hg.gy) * (1.0f - P.Inertia) + diry * P.Inertia;
+			const float len = sqrtf(dirx * dirx + diry * diry);
+			if (len != 0.0f) {
+				dirx /= len;
+				diry /= len;
+			}
+			px += dirx;
+			py += diry;
+			// the reference's border test (a NaN position also dies); `safe`
+			// also covers a direction that rounded above unit length
+			if ((dirx == 0.0f && diry == 0.0f) || !(px >= lo && px < hi_x && py >= lo && py < hi_y) || !safe) {
+				alive = false; // the carried sediment leaves with the droplet
+				residual += sed;
+			} else {
+				// phase 2: corners of the new cell, capacity, deposit or erode
+				const uint32_t nx = static_cast<uint32_t>(px), ny = static_cast<uint32_t>(py);
+				const float4 q2 = corners(ny * pitch + nx);
+				const float cx2 = px - static_cast<float>(nx), cy2 = py - static_cast<float>(ny);
+				const float h2 = q2.x * (1.0f - cx2) * (1.0f - cy2) + q2.y * cx2 * (1.0f - cy2)
+					+ q2.z * (1.0f - cx2) * cy2 + q2.w * cx2 * cy2;
+				dh = h2 - hg.h;
+				const float cap = fmaxf(-dh * speed * vol * P.SedimentCapacityFactor, P.minSedimentCapacity);
+				if (sed > cap || dh > 0.0f) {
+					const float dep = (dh > 0.0f) ? fminf(dh, sed) : (sed - cap) * P.DepositSpeed;
+					sed -= dep;
+#pragma unroll
+					for (uint32_t c = 0u; c < 4u; c++) {
+						const float wx = (c & 1u) ? ox : 1.0f - ox, wy = (c & 2u) ? oy : 1.0f - oy;
+						atomicAdd(map + mi + ((c & 2u) ? pitch : 0u) + (c & 1u), dep * wx * wy);
+					}
+				} else {
+					erode = true;
+					erode_steps++;
+					ero = fminf((cap - sed) * P.ErodeSpeed, -dh);
+				}
+			}
+		}
+		// phase 3: the brush runs of the warp's eroding droplets over all lanes
+		const uint32_t emask = __ballot_sync(0xFFFFFFFFu, erode);
+		if (emask != 0u) {
+			const uint32_t rank = __popc(emask & ((1u << lane) - 1u));
+			if (erode) {
+				slot_cell[warp][rank] = mi;
+				slot_ero[warp][rank] = ero;
+			}
+			__syncwarp();
+			const uint32_t ntask = static_cast<uint32_t>(__popc(emask)) * nrun;
+#pragma unroll 1
+			for (uint32_t t = lane; t < ntask; t += 32u) {
+				const uint32_t di = t / nrun, r = t - di * nrun;
+				const uint32_t cell = slot_cell[warp][di];
+				const float e = slot_ero[warp][di];
+				const int2 R = runs[r];
+				float* const first = map + (static_cast<int64_t>(cell) + bidx[R.x]);
+				const int32_t lead = static_cast<int32_t>((reinterpret_cast<uintptr_t>(first) >> 2) & 3u);
+				float4* const blk = reinterpret_cast<float4*>(first - lead);
+				const int32_t nb = (lead + R.y + 3) >> 2;
+				float part = 0.0f;
+#pragma unroll 1
+				for (int32_t b0 = 0; b0 < nb; b0 += kCoopTrip) {
+					float4 cur[kCoopTrip];
+#pragma unroll
+					for (int32_t u = 0; u < kCoopTrip; u++) {
+						const int32_t b = b0 + u;
+						if (b < nb) {
+							float dd[4];
+#pragma unroll
+							for (int i = 0; i < 4; i++) {
+								const int32_t j = 4 * b + i - lead;
+								dd[i] = (j >= 0 && j < R.y) ? -(e * bw[R.x + j]) : -0.0f;
+							}
+							cur[u] = atom_add_v4(blk + b, dd[0], dd[1], dd[2], dd[3]);
+						}
+					}
+#pragma unroll
+					for (int32_t u = 0; u < kCoopTrip; u++) {
+						const int32_t b = b0 + u;
+						if (b < nb) {
+							const float c[4] = { cur[u].x, cur[u].y, cur[u].z, cur[u].w };
+							float dd[4];
+							bool back = false;
+#pragma unroll
+							for (int i = 0; i < 4; i++) {
+								const int32_t j = 4 * b + i - lead;
+								dd[i] = -0.0f;
+								if (j >= 0 && j < R.y) {
+									const float we = e * bw[R.x + j];
+									const float ds = fminf(fmaxf(c[i], 0.0f), we);
+									part += ds;
+									// w was taken; give back what the cell lacked
+									if (ds < we) {
+										dd[i] = we - ds;
+										back = true;
+									}
+								}
+							}
+							if (back) {
+								red_add_v4(blk + b, dd[0], dd[1], dd[2], dd[3]);
+							}
+						}
+					}
+				}
+				wparts[t] = part;
+			}
+			__syncwarp();
+			if (erode) {
+				float sum = 0.0f;
+				for (uint32_t r = 0u; r < nrun; r++) {
+					sum += wparts[rank * nrun + r];
+				}
+				sed += sum;
+			}
+			__syncwarp();
+		}
+		if (alive) {
+			speed = sqrtf(fmaxf(0.0f, speed * speed + dh * P.Gravity));
+			speed *= 1.0f - P.Friction;
+			vol *= 1.0f - P.EvaporateSpeed;
+			steps_done++;
+		}
+	}
+	if (J.counters) {
+		unsigned long long s = steps_done, e = erode_steps;
+		for (int o = 16; o > 0; o >>= 1) {
+			s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+			e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		}
+		if (lane == 0u) {
+			atomicAdd(J.counters, s);
+			atomicAdd(J.counters + 1, e);
+		}
+	}
+	if (J.residual) {
+		// the warp's 32 droplet residuals, gathered on lane 0 and summed in double
+		double total = 0.0;
+		for (uint32_t l = 0u; l < 32u; l++) {
+			const float r = __shfl_sync(0xFFFFFFFFu, residual, static_cast<int>(l));
+			if (lane == 0u) {
+				total += static_cast<double>(r);
+			}
+		}
+		if (lane == 0u && total != 0.0) {
+			atomicAdd(J.residual, total);
+		}
+	}
+	if (capped && J.status) {
+		atomicOr(J.status, STATUS_TIMEOUT);
+	}
+}
+
 // STPHeightfieldKernel.cu:112-122, eight pixels per thread where rows allow.
 __device__ __forceinline__ uint32_t fmt1(const float h) {
 	return static_cast<uint32_t>(rintf(__saturatef(h) * 65535.0f));
@@ -1018,7 +1286,9 @@ uint32_t rows_max_lanes(uint32_t radius) {
 bool erosion_variant_stable(const uint32_t lanes, const uint32_t droplets_per_group, const bool rows,
 	const double density, const double in_flight) {
 	(void)droplets_per_group;
-	(void)rows;
+	if (lanes == 1u && rows) {
+		return density <= kDenseRows && in_flight <= kCoopInFlight;
+	}
 	return lanes == 1u || (density <= kDenseRows && in_flight <= kDenseInFlight);
 }
 
@@ -1051,12 +1321,15 @@ ErosionChoice erosion_choice(const uint32_t radius, const uint32_t brush_size, c
 	if (!erosion_variant_stable(2u, 1u, true, density, in_flight)) {
 		return ErosionChoice { 1u, 1u, false };
 	}
-	// brush rows with two lanes per droplet where the brush allows rows: with
-	// the brush taken by returning atomics the fastest row variant on the
-	// production chunk (69 ms per 16 chunks against 76 ms with four lanes),
-	// inside the one-thread kernel's band around the serial result everywhere
-	// measured
+	// brush rows where the brush allows them: the warp-cooperative kernel
+	// where few droplets are in flight per pixel, else two lanes per droplet
+	// (with the brush taken by returning atomics the fastest lane-group row
+	// variant on the production chunk, 69 ms per 16 chunks against 76 ms with
+	// four lanes, inside the one-thread kernel's band everywhere measured)
 	if (rows_allowed && rows_max_lanes(radius) != 0u) {
+		if (erosion_variant_stable(1u, 1u, true, density, in_flight) && in_flight <= kCoopDefaultInFlight) {
+			return ErosionChoice { 1u, 1u, true };
+		}
 		return ErosionChoice { 2u, 1u, true };
 	}
 	return ErosionChoice { default_lanes(brush_size), 1u, false };
@@ -1096,6 +1369,30 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 		return STPGB_OK;
 	}
 	const size_t smem = static_cast<size_t>(max_brush) * (sizeof(int32_t) + sizeof(float));
+	if (vector_rows && !exact_clamp && lanes_per_droplet == 1u && droplets_per_group == 1u) {
+		// the warp-cooperative kernel: brush, runs and one eroded-amount slot per
+		// (lane, run) of every warp; the reference's circular brush of radius r
+		// has 2r - 1 runs, fewer than 2 * ceil(sqrt(size)) + 3
+		uint32_t sq = 0u;
+		while (sq * sq < max_brush) {
+			sq++;
+		}
+		const uint32_t runcap = std::min(max_brush, 2u * sq + 3u);
+		const size_t csmem = smem + static_cast<size_t>(runcap) * sizeof(int2)
+			+ static_cast<size_t>(kErodeBlock) * runcap * sizeof(float);
+		const uint64_t cblocks = (static_cast<uint64_t>(max_count) + kErodeBlock - 1u) / kErodeBlock;
+		if (cblocks > 0x7FFFFFFFull) {
+			return inval("erosion: too many droplets for one launch");
+		}
+		if (csmem > 48u * 1024u) {
+			STPGB_CUDA_TRY(cudaFuncSetAttribute(erosion_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				static_cast<int>(csmem)));
+		}
+		erosion_coop_kernel<<<dim3(static_cast<uint32_t>(cblocks), njobs), kErodeBlock, csmem, stream>>>(jobs, single,
+			runcap);
+		STPGB_CUDA_TRY(cudaGetLastError());
+		return STPGB_OK;
+	}
 	if (vector_rows && !exact_clamp && (droplets_per_group == 1u || droplets_per_group == 2u)
 		&& (lanes_per_droplet == 2u || lanes_per_droplet == 4u)) {
 		const size_t rsmem = smem + static_cast<size_t>(max_brush) * sizeof(BrushRun);

@@ -79,6 +79,19 @@ uint32_t rows_max_lanes(uint32_t radius);
 // 2.3 per pixel 1.34.
 constexpr double kDenseRows = 3.0;
 constexpr double kDenseInFlight = 1.5;
+// The warp-cooperative kernel (one droplet per lane, the warp's brush runs
+// shared out over all lanes: lanes = 1 with rows) takes every run of a
+// droplet's brush at once and keeps twice the droplets in flight; it is
+// taken up to kCoopInFlight droplets in flight per pixel counted as for two
+// lanes (0.75 of its own), where several blocks of a run per round trip were
+// measured inside the reference kernel's RMS band.  The default prefers it
+// to two lanes per droplet up to kCoopDefaultInFlight: brush 4 at 2.3
+// droplets per pixel took 3.73 against 3.91 ms on one 3x3 x 512^2 map (0.33
+// in flight), 13.1 against 14.9 on 3x3 x 1024^2 (0.08), 173 against 229 on a
+// 4096^2 field, but 71.1 against 69.4 ms on the production batch of 16
+// multi-biome 512^2 neighbourhoods, where the autotuner decides.
+constexpr double kCoopInFlight = 0.375;
+constexpr double kCoopDefaultInFlight = 0.2;
 // Droplets in flight per pixel of `area` for `count` droplets.
 double erosion_in_flight(uint32_t count, double area);
 bool erosion_variant_stable(uint32_t lanes, uint32_t droplets_per_group, bool rows, double density, double in_flight);
@@ -116,6 +129,7 @@ bool erosion_rows_wide(uint32_t min_radius);
 constexpr uint32_t kAtomicMinRadius = 4u;
 bool erosion_rows_atomic(uint32_t min_radius, uint32_t lanes);
 
+// lanes == 1 with rows: the warp-cooperative kernel
 struct ErosionChoice {
 	uint32_t lanes, droplets_per_group;
 	bool rows;

@@ -499,9 +499,7 @@ struct stpgb_server {
 		double* res_dev = reinterpret_cast<double*>(sl.dev + o_res);
 		uint32_t* status_dev = reinterpret_cast<uint32_t*>(sl.dev + o_status);
 
-		uint32_t maxS = 0u, maxR = 0u, maxRS = 0u, maxCount = 0u, maxBrush = 0u, minBrush = 0xFFFFFFFFu,
-			minRadius = 0xFFFFFFFFu;
-		double maxDensity = 0.0, maxInFlight = 0.0;
+		uint32_t maxS = 0u, maxR = 0u, maxRS = 0u, maxCount = 0u;
 		size_t so = it.scratch_off;
 		for (size_t j = 0; j < ng; j++) {
 			const ChunkKey& k = it.generated[j];
@@ -595,11 +593,48 @@ struct stpgb_server {
 			fmt[i] = FormatJob { e.map, 3ull * S, reinterpret_cast<uint16_t*>(at(r.fixed)), 3ull * S, 3u * S, 3u * S };
 			maxRS = std::max(maxRS, S);
 			maxCount = std::max(maxCount, r.droplets);
-			maxBrush = std::max(maxBrush, bsize);
-			minBrush = std::min(minBrush, bsize);
-			minRadius = std::min(minRadius, r.req.BrushRadius);
-			maxDensity = std::max(maxDensity, static_cast<double>(r.droplets) / (static_cast<double>(S) * S));
-			maxInFlight = std::max(maxInFlight, erosion_in_flight(r.droplets, static_cast<double>(S) * S));
+		}
+		// Erosion variant groups: every request takes its own default kernel
+		// (erosion_choice on its brush, its droplet density and its droplets in
+		// flight per pixel), the jobs of one variant are made contiguous and
+		// eroded by one launch.  One variant for the whole sequence would hold
+		// every request to what its densest one allows.
+		struct ErosionGroup {
+			ErosionChoice ec;
+			uint32_t dpg, first, n, maxCount, maxBrush, minRadius;
+		};
+		std::vector<ErosionGroup> egroups;
+		{
+			std::vector<ErosionJob> by_request(ero, ero + nr);
+			std::vector<std::pair<uint32_t, uint32_t>> keyed(nr); // (variant key, request)
+			std::vector<ErosionChoice> choice(nr);
+			std::vector<uint32_t> dpgs(nr);
+			for (size_t i = 0; i < nr; i++) {
+				const Request& r = requests[it.tickets[i]];
+				const double area = static_cast<double>(r.req.MapSize) * r.req.MapSize;
+				const double density = r.droplets / area, in_flight = erosion_in_flight(r.droplets, area);
+				choice[i] = erosion_choice(r.req.BrushRadius, by_request[i].brush_size, density, in_flight, true);
+				// the stable point-wise variant with two droplets per group where rows are not allowed
+				dpgs[i] = !choice[i].rows && choice[i].lanes >= 4u
+						&& erosion_variant_stable(choice[i].lanes, 2u, false, density, in_flight)
+					? 2u
+					: 1u;
+				keyed[i] = { choice[i].lanes * 8u + dpgs[i] * 2u + (choice[i].rows ? 1u : 0u), static_cast<uint32_t>(i) };
+			}
+			std::stable_sort(keyed.begin(), keyed.end(),
+				[](const auto& a, const auto& b) { return a.first < b.first; });
+			for (size_t pos = 0; pos < nr; pos++) {
+				const uint32_t i = keyed[pos].second;
+				ero[pos] = by_request[i];
+				if (pos == 0u || keyed[pos].first != keyed[pos - 1u].first) {
+					egroups.push_back(ErosionGroup { choice[i], dpgs[i], static_cast<uint32_t>(pos), 0u, 0u, 0u, 0xFFFFFFFFu });
+				}
+				ErosionGroup& g = egroups.back();
+				g.n++;
+				g.maxCount = std::max(g.maxCount, ero[pos].count);
+				g.maxBrush = std::max(g.maxBrush, ero[pos].brush_size);
+				g.minRadius = std::min(g.minRadius, requests[it.tickets[i]].req.BrushRadius);
+			}
 		}
 		std::fill(it.residual_host, it.residual_host + nr, 0.0);
 		*it.status_host = 0u;
@@ -624,18 +659,13 @@ struct stpgb_server {
 		STPGB_TRY(starts_jobs_launch(reinterpret_cast<StartsJob*>(sl.dev + o_starts), static_cast<uint32_t>(nr), maxCount,
 			this->base.Seed, s));
 		// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
-		// pitches 3 * MapSize), the default two lanes and one droplet per
-		// group; each job reads several blocks per round trip where few of its
-		// droplets are in flight per pixel.  The stable point-wise variant with
-		// two droplets per group where rows are not allowed
-		const ErosionChoice ec = erosion_choice(minRadius, minBrush, maxDensity, maxInFlight, true);
-		const uint32_t dpg = !ec.rows && ec.lanes >= 4u
-				&& erosion_variant_stable(ec.lanes, 2u, false, maxDensity, maxInFlight)
-			? 2u
-			: 1u;
-		STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero), ero[0], static_cast<uint32_t>(nr), maxCount,
-			maxBrush, s, ec.lanes, false, dpg, ec.rows, erosion_rows_wide(minRadius),
-			erosion_rows_atomic(minRadius, ec.lanes)));
+		// pitches 3 * MapSize); each job reads several blocks per round trip
+		// where few of its droplets are in flight per pixel
+		for (const ErosionGroup& g : egroups) {
+			STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero) + g.first, ero[g.first], g.n,
+				g.maxCount, g.maxBrush, s, g.ec.lanes, false, g.dpg, g.ec.rows, erosion_rows_wide(g.minRadius),
+				erosion_rows_atomic(g.minRadius, g.ec.lanes)));
+		}
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
 		STPGB_CUDA_TRY(cudaMemcpyAsync(it.residual_host, res_dev, nr * sizeof(double), cudaMemcpyDeviceToHost, s));

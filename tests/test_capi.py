@@ -143,7 +143,8 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
 
 @pytest.mark.parametrize("radius,droplets,side,lanes,rows", [
     (4, 600000, 512, 2, 1),          # the production chunk (0.33 in flight per pixel): brush rows, two lanes
-    (5, 150733, 256, 2, 1),          # 2.3 per pixel of a 256^2 chunk, 1.34 in flight
+    (5, 2411725, 1024, 1, 1),        # 2.3 per pixel of a 1024^2 chunk, 0.08 in flight: warp-cooperative rows
+    (5, 150733, 256, 2, 1),          # 2.3 per pixel of a 256^2 chunk, 1.34 in flight: rows, two lanes
     (3, 150733, 256, 2, 1),
     (2, 150733, 256, 2, 0),          # brush 2 is too small for row blocks
     (4, 9421, 64, 1, 0),             # 2.3 per pixel of a 64^2 chunk, all in flight: the reference kernel
@@ -155,7 +156,7 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
 def test_erosion_choice_follows_density(stpgb, radius, droplets, side, lanes, rows):
     """Several lanes per droplet up to 3 droplets per pixel of the start area and 1.5 in flight at once
     (the two-lane row kernel keeps 152 SMs x 9 blocks x 64 droplets resident; no GPU here, so the SM
-    count of the GB300 is taken)."""
+    count of the GB300 is taken); by default the warp-cooperative kernel (1 lane with rows) up to 0.2."""
     import ctypes as C
     area = side * side
     got_lanes, got_rows = C.c_uint32(0), C.c_uint32(0)

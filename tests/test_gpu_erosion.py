@@ -221,16 +221,20 @@ def test_erosion_rms_within_reference_spread(dev, oracle, stpgb, case, variant):
     erosion_rms_within_reference_spread(dev, oracle, stpgb, EROSION_CASES[case], variant, case)
 
 
-@pytest.mark.parametrize("params", [(512, 600000, 4, 50), (256, 150000, 4, 50)], ids=["512", "256"])
-def test_production_brush_rms_within_reference_spread(dev, oracle, stpgb, params):
+@pytest.mark.parametrize("params,variant", [((512, 600000, 4, 50), "default"), ((256, 150000, 4, 50), "default"),
+                                            ((512, 600000, 4, 50), "warp-cooperative")],
+                         ids=["512", "256", "512-warp-cooperative"])
+def test_production_brush_rms_within_reference_spread(dev, oracle, stpgb, params, variant):
     """The production chunk (3x3 x 512^2, 600,000 droplets, brush 4, lifetime 50) and the same
-    density on 256^2 chunks: the default choice (brush rows, the brush taken by returning atomics,
-    several blocks per round trip on the production chunk) stays within the reference kernel's
-    band around the FP64 serial result."""
-    erosion_rms_within_reference_spread(dev, oracle, stpgb, params, "default", f"brush4-{params[0]}")
+    density on 256^2 chunks: the default choice (brush rows with two lanes, the brush taken by
+    returning atomics, several blocks per round trip on the production chunk) and, on the production
+    chunk, the warp-cooperative kernel (one droplet per lane, every run of the brush in flight at
+    once) stay within the reference kernel's band around the FP64 serial result."""
+    erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, f"brush4-{params[0]}",
+                                        {"warp-cooperative": {"lanes": 1}}.get(variant))
 
 
-def erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, case):
+def erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, case, kw=None):
     """Per-pixel RMS against the FP64 serial oracle stays within the reference kernel's own band.
 
     The reference kernel is one thread per droplet reading and updating the brush point by point
@@ -247,7 +251,7 @@ def erosion_rms_within_reference_spread(dev, oracle, stpgb, params, variant, cas
     ref_runs = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 5, lanes=1, pointwise=True)
     ref_rms = [rms(r, ref) for r, _ in ref_runs]
     spread = max(rms(a, b) for i, (a, _) in enumerate(ref_runs) for b, _ in ref_runs[i + 1:])
-    kw = dict(VARIANTS[variant])
+    kw = dict(VARIANTS[variant] if kw is None else kw)
     if kw.get("droplets_per_group", 1) > 1:
         kw.setdefault("lanes", 4)  # several droplets per group need >= 4 lanes; every brush here allows 4
     prod = erode_runs(dev, stpgb, h, (S, S), nn, s, starts, 3, **kw)
