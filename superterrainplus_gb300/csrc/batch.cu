@@ -48,11 +48,12 @@ struct RequestLayout {
 	size_t end;
 };
 
-// Erosion variant groups: requests that may take several lanes per droplet
-// (erosion_variant_stable) and whose brush takes the row kernel
-// (rows_max_lanes() >= 2); requests that may take several lanes but whose
-// brush is too small for rows (radius 2); and requests too densely packed for
-// anything but the one-lane reference kernel.  Each group has its own job
+// Erosion variant groups: requests whose brush takes the row kernels
+// (rows_max_lanes() >= 2) with few enough droplets in flight per pixel for the
+// warp-cooperative kernel; the other requests that may take several lanes per
+// droplet (erosion_variant_stable) with row blocks; those whose brush is too
+// small for rows (radius 2); and requests too densely packed for anything but
+// the one-lane reference kernel.  Each group has its own job
 // array, kernel variant and autotuning, and the erosion stage launches the
 // groups side by side.  One variant for the whole batch would hold every
 // request to the most restricted one: a single radius-2 brush, or one small
@@ -134,13 +135,14 @@ struct stpgb_batch {
 	// erosion variant groups (brush rows in 16-byte blocks need aligned maps:
 	// every merged map of a batch is 512-byte aligned with a pitch of
 	// 3 * MapSize, a multiple of 24 floats); group_of[n] is request n's group
-	ErosionGroup grp[3];
+	static constexpr uint32_t kGroups = 4u;
+	ErosionGroup grp[kGroups];
 	uint32_t ngroups = 0u;
 	std::vector<uint32_t> group_of;
-	// launch streams of the second and third group, and the events that fork
+	// launch streams of the groups after the first, and the events that fork
 	// them from the batch's stream and join them back
-	cudaStream_t aux[2] = { nullptr, nullptr };
-	cudaEvent_t fork = nullptr, join[2] = { nullptr, nullptr };
+	cudaStream_t aux[kGroups - 1u] = {};
+	cudaEvent_t fork = nullptr, join[kGroups - 1u] = {};
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	bool use_graph = false;
@@ -185,7 +187,8 @@ struct stpgb_batch {
 				 static_cast<void*>(table), static_cast<void*>(residual), static_cast<void*>(status),
 				 static_cast<void*>(counters),
 				 static_cast<void*>(shf_jobs), static_cast<void*>(noise_jobs), static_cast<void*>(grp[0].jobs),
-				 static_cast<void*>(grp[1].jobs), static_cast<void*>(grp[2].jobs), static_cast<void*>(fmt_jobs) }) {
+				 static_cast<void*>(grp[1].jobs), static_cast<void*>(grp[2].jobs), static_cast<void*>(grp[3].jobs),
+				 static_cast<void*>(fmt_jobs) }) {
 			if (p) {
 				cudaFree(p);
 			}
@@ -193,7 +196,7 @@ struct stpgb_batch {
 		if (fork) {
 			cudaEventDestroy(fork);
 		}
-		for (int k = 0; k < 2; k++) {
+		for (uint32_t k = 0u; k + 1u < kGroups; k++) {
 			if (join[k]) {
 				cudaEventDestroy(join[k]);
 			}
@@ -540,23 +543,24 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		b->fmt_h.push_back(FormatJob { height, 3ull * S, e.fixed, 3ull * S, 3u * S, 3u * S });
 		const double area = static_cast<double>(S) * S;
 		const double density = r.DropletCount / area, in_flight = erosion_in_flight(r.DropletCount, area);
-		const uint32_t cls = !erosion_variant_stable(2u, 1u, true, density, in_flight) ? 2u
-			: rows_max_lanes(r.BrushRadius) != 0u                                        ? 0u
+		const uint32_t cls = !erosion_variant_stable(2u, 1u, true, density, in_flight) ? 3u
+			: rows_max_lanes(r.BrushRadius) == 0u                                        ? 2u
+			: erosion_variant_stable(1u, 1u, true, density, in_flight)                   ? 0u
 																						  : 1u;
 		b->group_of.push_back(cls);
 		b->grp[cls].add(e, r.BrushRadius, density, in_flight);
 	}
 	{
 		// the non-empty groups first, in their order
-		uint32_t remap[3] = { 0u, 0u, 0u }, k = 0u;
-		ErosionGroup packed[3];
-		for (uint32_t g = 0u; g < 3u; g++) {
+		uint32_t remap[stpgb_batch::kGroups] = {}, k = 0u;
+		ErosionGroup packed[stpgb_batch::kGroups];
+		for (uint32_t g = 0u; g < stpgb_batch::kGroups; g++) {
 			if (!b->grp[g].h.empty()) {
 				remap[g] = k;
 				packed[k++] = std::move(b->grp[g]);
 			}
 		}
-		for (uint32_t g = 0u; g < 3u; g++) {
+		for (uint32_t g = 0u; g < stpgb_batch::kGroups; g++) {
 			b->grp[g] = std::move(packed[g]);
 		}
 		for (auto& g : b->group_of) {
