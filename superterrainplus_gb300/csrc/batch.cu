@@ -102,7 +102,8 @@ struct ErosionGroup {
 
 	int launch(cudaStream_t s) const {
 		return erosion_launch(jobs, h[0], static_cast<uint32_t>(h.size()), max_count, max_brush, s, lanes, false, dpg,
-			rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes));
+			rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes),
+			erosion_coop_interleave(h.data(), static_cast<uint32_t>(h.size())));
 	}
 };
 

@@ -16,6 +16,7 @@
 //    Volume >= minWaterVolume); reaching it sets STATUS_TIMEOUT.
 #include "erosion.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
 
@@ -934,12 +935,25 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 // default takes this kernel only where few droplets are in flight per pixel
 // (erosion_variant_stable).  Needs what the row kernel needs: a 16-byte
 // aligned map whose pitch is a multiple of four floats.
+// The grid is one-dimensional, `blocks_per_job` blocks per job; with
+// `interleave` > 1 the blocks of that many consecutive jobs alternate, so
+// that several jobs share the droplets in flight and each keeps fewer of its
+// own in flight per pixel (the blocks of a job still go out in order).
 constexpr int32_t kCoopTrip = 3; // blocks of a run per round trip
 
 __global__ void __launch_bounds__(kErodeBlock, 9) erosion_coop_kernel(const ErosionJob* __restrict__ jobs,
-	const ErosionJob single, const uint32_t runcap) {
+	const ErosionJob single, const uint32_t runcap, const uint32_t njobs, const uint32_t interleave,
+	const uint32_t blocks_per_job) {
 	constexpr uint32_t kWarps = kErodeBlock / 32u;
-	const ErosionJob& J = jobs ? jobs[blockIdx.y] : single;
+	uint32_t job = 0u, bx = blockIdx.x;
+	if (jobs) {
+		const uint32_t span = interleave * blocks_per_job;
+		const uint32_t chunk = blockIdx.x / span, within = blockIdx.x - chunk * span;
+		const uint32_t qn = min(interleave, njobs - chunk * interleave);
+		job = chunk * interleave + within % qn;
+		bx = within / qn;
+	}
+	const ErosionJob& J = jobs ? jobs[job] : single;
 	extern __shared__ __align__(16) unsigned char esm[];
 	int32_t* const bidx = reinterpret_cast<int32_t*>(esm);
 	float* const bw = reinterpret_cast<float*>(esm) + J.brush_size;
@@ -980,7 +994,7 @@ __global__ void __launch_bounds__(kErodeBlock, 9) erosion_coop_kernel(const Eros
 
 	const RainParams& P = J.p;
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-	const uint32_t d = blockIdx.x * kErodeBlock + threadIdx.x;
+	const uint32_t d = bx * kErodeBlock + threadIdx.x;
 	const uint32_t nrun = nruns;
 	float* const wparts = parts + static_cast<size_t>(warp) * 32u * runcap;
 	float* const map = J.map;
@@ -1308,6 +1322,27 @@ uint32_t erosion_resident_droplets(const uint32_t lanes, const uint32_t dpg) {
 	return static_cast<uint32_t>(sms) * blocks * kErodeBlock / std::max(lanes, 1u) * std::max(dpg, 1u);
 }
 
+uint32_t erosion_coop_interleave(const ErosionJob* jobs, const uint32_t njobs) {
+	int dev = 0, l2 = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess
+		|| l2 <= 0) {
+		cudaGetLastError();
+		l2 = 126 * 1024 * 1024;
+	}
+	const double resident = erosion_resident_droplets(1u, 1u);
+	double worst = 0.0, map_bytes = 1.0;
+	for (uint32_t j = 0u; j < njobs; j++) {
+		const ErosionJob& J = jobs[j];
+		if (J.start_area != 0u) {
+			worst = std::max(worst, std::min<double>(J.count, resident) / J.start_area);
+		}
+		map_bytes = std::max(map_bytes, static_cast<double>(J.pitch) * J.dim_y * sizeof(float));
+	}
+	const double want = std::ceil(worst / kCoopInterleaveInFlight);
+	const double fit = std::floor(0.5 * l2 / map_bytes);
+	return static_cast<uint32_t>(std::max(1.0, std::min({ want, fit, static_cast<double>(njobs) })));
+}
+
 bool erosion_rows_wide(const uint32_t min_radius) {
 	return min_radius >= kWideMinRadius;
 }
@@ -1364,7 +1399,7 @@ RainParams rain_params(const stpgb_raindrop_setting& s) {
 
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp,
-	uint32_t droplets_per_group, bool vector_rows, bool wide_trips, bool atomic_brush) {
+	uint32_t droplets_per_group, bool vector_rows, bool wide_trips, bool atomic_brush, uint32_t interleave) {
 	if (max_count == 0u || njobs == 0u) {
 		return STPGB_OK;
 	}
@@ -1380,16 +1415,17 @@ int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t nj
 		const uint32_t runcap = std::min(max_brush, 2u * sq + 3u);
 		const size_t csmem = smem + static_cast<size_t>(runcap) * sizeof(int2)
 			+ static_cast<size_t>(kErodeBlock) * runcap * sizeof(float);
-		const uint64_t cblocks = (static_cast<uint64_t>(max_count) + kErodeBlock - 1u) / kErodeBlock;
-		if (cblocks > 0x7FFFFFFFull) {
+		const uint64_t per_job = (static_cast<uint64_t>(max_count) + kErodeBlock - 1u) / kErodeBlock;
+		if (per_job * njobs > 0x7FFFFFFFull) {
 			return inval("erosion: too many droplets for one launch");
 		}
 		if (csmem > 48u * 1024u) {
 			STPGB_CUDA_TRY(cudaFuncSetAttribute(erosion_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 				static_cast<int>(csmem)));
 		}
-		erosion_coop_kernel<<<dim3(static_cast<uint32_t>(cblocks), njobs), kErodeBlock, csmem, stream>>>(jobs, single,
-			runcap);
+		const uint32_t q = jobs ? std::max(1u, std::min(interleave, njobs)) : 1u;
+		erosion_coop_kernel<<<static_cast<uint32_t>(per_job * njobs), kErodeBlock, csmem, stream>>>(jobs, single,
+			runcap, njobs, q, static_cast<uint32_t>(per_job));
 		STPGB_CUDA_TRY(cudaGetLastError());
 		return STPGB_OK;
 	}

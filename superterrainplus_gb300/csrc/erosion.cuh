@@ -50,10 +50,18 @@ RainParams rain_params(const stpgb_raindrop_setting& s);
 // three blocks of a run per round trip (one droplet per group) or two (two
 // droplets);
 // atomic_brush: with vector_rows, take each block's brush amounts with one
-// returning vector atomic and give back what a cell lacked
+// returning vector atomic and give back what a cell lacked;
+// interleave: the warp-cooperative kernel (lanes_per_droplet 1 with
+// vector_rows) alternates the blocks of that many consecutive jobs
 int erosion_launch(const ErosionJob* jobs, const ErosionJob& single, uint32_t njobs, uint32_t max_count,
 	uint32_t max_brush, cudaStream_t stream, uint32_t lanes_per_droplet, bool exact_clamp = false,
-	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool wide_trips = false, bool atomic_brush = false);
+	uint32_t droplets_per_group = 1u, bool vector_rows = false, bool wide_trips = false, bool atomic_brush = false,
+	uint32_t interleave = 1u);
+// Jobs a warp-cooperative launch interleaves: enough that each keeps at most
+// kCoopInterleaveInFlight droplets in flight per pixel, with the maps of the
+// interleaved jobs together in half of the L2.
+constexpr double kCoopInterleaveInFlight = 0.2;
+uint32_t erosion_coop_interleave(const ErosionJob* jobs, uint32_t njobs);
 
 // Largest lanes-per-droplet that keeps at least four brush points per lane,
 // and the per-call default, min(8, max_lanes).

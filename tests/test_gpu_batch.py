@@ -131,3 +131,42 @@ def test_batch_with_layer_chain_biomes(stpgb, dev, oracle):
     for n in range(len(REQS)):
         t0 = before[n].astype(np.float64).sum()
         assert abs((t0 - after[n].astype(np.float64).sum()) - res[n]) <= 1e-5 * t0
+
+
+def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
+    """The headline path: four production requests (3x3 x 512^2, 8 biomes, filter radius 32, 600,000
+    droplets, brush 4, lifetime 50) through the autotuned graph, whatever erosion variant and job
+    interleaving the tuner settles on.  Request 0's eroded neighbourhood stays within the reference
+    kernel's band around the FP64 serial result (the one-lane kernel run five times on the same map
+    and starts: its worst RMS plus its run-to-run spread)."""
+    import torch
+    from test_gpu_erosion import erode_runs, rms
+    S, count = 512, 600000
+    reqs = [dict(MapSize=S, ChunkX=4 * n, ChunkY=0, InterpolationRadius=32, DropletCount=count, BrushRadius=4,
+                 Lifetime=50) for n in range(4)]
+    base = stpgb.RaindropSetting(**helpers.raindrop_dict(count, radius=4, lifetime=50, seed=42))
+    b = stpgb.Batch(reqs, base, stpgb.SimplexSetting(42, 8, 0.2181661565), helpers.biome_table(8, 42), graph=True)
+    b.synthesize(192, 42)
+    b.tune()
+    b.run_stage(0)
+    b.run_stage(1)
+    before = [np.zeros((3 * S, 3 * S), np.float32) for _ in reqs]
+    b.download(before)
+    starts = [np.zeros(2 * count, np.float32) if n == 0 else None for n in range(4)]
+    b.download_inputs(starts=starts)
+    b.status()
+    b.run()
+    after = [np.zeros((3 * S, 3 * S), np.float32) for _ in reqs]
+    b.download(after)
+    b.status()
+    s = helpers.raindrop_dict(count, radius=4, lifetime=50, seed=42)
+    idx, w = oracle.brush(3 * S, 4)
+    h0 = before[0]
+    ref, _, _ = oracle.erode(h0, s, starts[0], idx, w, fp64=True)
+    ref_runs = erode_runs(dev, stpgb, h0, (S, S), (3, 3), s, starts[0], 5, lanes=1, pointwise=True)
+    ref_rms = [rms(r, ref) for r, _ in ref_runs]
+    spread = max(rms(a, c) for i, (a, _) in enumerate(ref_runs) for c, _ in ref_runs[i + 1:])
+    got = rms(after[0].astype(np.float64), ref)
+    print(f"production batch ({b.tuning()[0]}): RMS {got:.3g}; reference kernel {min(ref_rms):.3g}..{max(ref_rms):.3g}, "
+          f"spread {spread:.3g}")
+    assert got <= max(ref_rms) + spread
