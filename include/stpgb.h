@@ -606,10 +606,14 @@ STPGB_API int stpgb_batch_run_stage(stpgb_batch* batch, uint32_t stage, void* st
  * re-captures the graph of a batch created with STPGB_BATCH_GRAPH. */
 STPGB_API int stpgb_batch_tune(stpgb_batch* batch);
 
-/* Erosion lanes per droplet, droplets per lane group and brush update (1 =
- * brush rows in 16-byte blocks, 0 = point by point) in use, and the
- * autotuner's erosion time in ms per candidate: 36 floats, index
- * 18*rows + 3*log2(lanes) + {0, 1, 2} for 1, 2, 4 droplets per group
+/* A batch erodes its requests in up to four variant groups (requests that may
+ * take the warp-cooperative kernel, other row requests, radius-2 brushes,
+ * requests too densely packed for more than one lane per droplet), each tuned
+ * on its own.  Reports the group with the most droplets: its erosion lanes per
+ * droplet, droplets per lane group and brush update (1 = brush rows in 16-byte
+ * blocks, 0 = point by point; 1 lane with rows = the warp-cooperative kernel)
+ * in use, and the autotuner's erosion time in ms per candidate: 36 floats,
+ * index 18*rows + 3*log2(lanes) + {0, 1, 2} for 1, 2, 4 droplets per group
  * (0 = not tried).  Any output pointer may be NULL. */
 STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_droplet,
 	uint32_t* droplets_per_group, uint32_t* vector_rows, float* erosion_ms);
