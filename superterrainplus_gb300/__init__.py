@@ -478,6 +478,10 @@ class DeviceOps:
     def hydraulic_erosion(self, heightmap, map_size, nn, setting, starts, count, brush_index, brush_weight,
                           residual=None, status=None, lanes=0, exact_clamp=False, droplets_per_group=1,
                           pointwise=False):
+        """stpgb_hydraulic_erosion_ex on a merged map tensor.  lanes=0 takes the default kernel for the
+        brush and the droplet density; lanes=1 with row blocks allowed (pointwise=False, an aligned
+        map) runs the warp-cooperative kernel, lanes=1 with pointwise=True the one-lane reference
+        kernel, lanes=2/4 the lane-group kernels."""
         info = NNInfo.make(map_size, nn)
         check(lib().stpgb_hydraulic_erosion_ex(
             C.c_void_p(heightmap.data_ptr()), C.byref(info), C.byref(setting), C.c_void_p(starts.data_ptr()), count,
