@@ -1,7 +1,7 @@
 """ctypes front end of the oracle (test infrastructure only).
 
 Only the tests, the smoke check and bench.py's CPU-baseline leg use this
-module; it is the checker, never the product.  `Oracle` wraps the CPU
+module; it is what the product is compared with, never the product.  `Oracle` wraps the CPU
 restatement (oracle/liboracle.so), `Reference` wraps the reference's own
 compiled host sources (oracle/_ref/libstpref.so) where they could be built.
 """

@@ -1,6 +1,6 @@
 /*
  * oracle/stp_oracle.cpp — CPU restatement of the SuperTerrain+ heightfield
- * path.  TEST INFRASTRUCTURE ONLY: it is the checker the parity tests, the
+ * path.  TEST INFRASTRUCTURE ONLY: it is what the parity tests, the
  * smoke test and the CPU-baseline leg of bench.py compare the CUDA path
  * against.  The product never links or calls it.
  *
