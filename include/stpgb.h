@@ -191,6 +191,18 @@ STPGB_API int stpgb_chunk_offset(const int32_t* chunk_coord, const uint32_t* chu
 STPGB_API int stpgb_chunk_neighbour_offset(const uint32_t* chunk_size, const uint32_t* region_size,
 	int32_t* offsets_xy, uint32_t capacity, uint32_t* count);
 
+/* Host memory mode of STPNearestNeighbourTextureBuffer::STPMergedBuffer
+ * (SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPNearestNeighbourTextureBuffer.cpp:18-113):
+ * pack the ChunkNearestNeighbour.x * .y host chunk maps (MapSize pixels of
+ * `element_size` bytes each, row-major, chunk index order) into one merged
+ * TotalMapSize map, chunk i at local chunk coordinate (i % nx, i / nx), and
+ * unpack it back.  The device path merges on the GPU inside the generator,
+ * the batch and the server. */
+STPGB_API int stpgb_nn_merge_host(const void* const* chunks, uint32_t element_size, const stpgb_nn_info* nn,
+	void* merged);
+STPGB_API int stpgb_nn_unmerge_host(const void* merged, uint32_t element_size, const stpgb_nn_info* nn,
+	void* const* chunks);
+
 /* ----------------------------------------------- single histogram filter -- */
 
 /* Workspace bytes stpgb_shf_filter needs for a chunk of `nn`, `radius`, and

@@ -30,7 +30,7 @@ __all__ = [
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
     "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch", "Layer", "LayerBiomes",
     "layer_chain_demo", "STPLayerChainBuilder", "AltitudeRule", "GradientRule", "SplatChunk", "splat_rules_demo",
-    "STPSplatmapGenerator", "STPChunk",
+    "STPSplatmapGenerator", "STPChunk", "nn_merge_host", "nn_unmerge_host",
 ]
 
 BIN_DTYPE = np.dtype([("Item", "<u2"), ("_pad", "<u2"), ("Weight", "<f4")])
@@ -132,6 +132,23 @@ class STPChunk:
         out = (C.c_int32 * (2 * max(count, 1)))()
         check(lib().stpgb_chunk_neighbour_offset(cs, rs, out, count, C.byref(n)))
         return [(out[2 * i], out[2 * i + 1]) for i in range(n.value)]
+
+
+def nn_merge_host(chunks, nn_info):
+    """Pack the ChunkNearestNeighbour.x * .y chunk maps (numpy arrays of MapSize, one dtype, chunk
+    index order) into one merged TotalMapSize map (STPNearestNeighbourTextureBuffer host mode)."""
+    chunks = [np.ascontiguousarray(c) for c in chunks]
+    merged = np.empty((nn_info.TotalMapSize[1], nn_info.TotalMapSize[0]), chunks[0].dtype)
+    ptrs = (C.c_void_p * len(chunks))(*[c.ctypes.data for c in chunks])
+    check(lib().stpgb_nn_merge_host(ptrs, chunks[0].dtype.itemsize, C.byref(nn_info), _p(merged)))
+    return merged
+
+
+def nn_unmerge_host(merged, nn_info, chunks):
+    """Unpack a merged map back into the chunk maps `chunks` (contiguous numpy arrays, written in place)."""
+    merged = np.ascontiguousarray(merged)
+    ptrs = (C.c_void_p * len(chunks))(*[c.ctypes.data for c in chunks])
+    check(lib().stpgb_nn_unmerge_host(_p(merged), merged.dtype.itemsize, C.byref(nn_info), ptrs))
 
 
 # ------------------------------------------------- single histogram filter

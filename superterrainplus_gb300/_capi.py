@@ -166,6 +166,8 @@ PROTOTYPES = {
     "stpgb_chunk_map_offset": (C.c_int, [vp, vp, vp, vp, vp]),
     "stpgb_chunk_offset": (C.c_int, [vp, vp, vp, vp]),
     "stpgb_chunk_neighbour_offset": (C.c_int, [vp, vp, vp, u32, C.POINTER(u32)]),
+    "stpgb_nn_merge_host": (C.c_int, [vp, u32, C.POINTER(NNInfo), vp]),
+    "stpgb_nn_unmerge_host": (C.c_int, [vp, u32, C.POINTER(NNInfo), vp]),
     "stpgb_shf_workspace_size": (C.c_int, [C.POINTER(NNInfo), u32, u32, C.POINTER(sz)]),
     "stpgb_shf_filter": (C.c_int, [vp, C.POINTER(NNInfo), u32, u32, vp, sz, vp, vp, u64, vp, vp]),
     "stpgb_shf_filter_host": (C.c_int, [vp, C.POINTER(NNInfo), u32, vp, vp, u64, C.POINTER(u64)]),

@@ -13,6 +13,8 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <string>
 
 namespace {
 
@@ -145,6 +147,74 @@ int stpgb_chunk_neighbour_offset(const uint32_t* chunk_size, const uint32_t* reg
 		}
 	}
 	return STPGB_OK;
+}
+
+} // extern "C"
+
+// Host half of STPNearestNeighbourTextureBuffer::STPMergedBuffer
+// (SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPNearestNeighbourTextureBuffer.cpp:18-113):
+// the chunk maps of a neighbourhood packed into one row-major merged map,
+// chunk i at its local chunk coordinate (i % nx, i / nx), and back.
+namespace {
+
+int check_nn(const stpgb_nn_info* nn, const uint32_t element_size, const char* what) {
+	if (!nn || element_size == 0u) {
+		return inval(std::string(what) + ": null neighbour information or zero element size");
+	}
+	for (int k = 0; k < 2; k++) {
+		if (nn->MapSize[k] == 0u || nn->ChunkNearestNeighbour[k] == 0u
+			|| static_cast<uint64_t>(nn->MapSize[k]) * nn->ChunkNearestNeighbour[k] != nn->TotalMapSize[k]) {
+			return inval(std::string(what) + ": TotalMapSize must equal MapSize * ChunkNearestNeighbour, all positive");
+		}
+	}
+	return STPGB_OK;
+}
+
+template<bool Pack>
+int copy_neighbours(unsigned char* merged, unsigned char* const* chunks, const uint32_t es, const stpgb_nn_info& nn) {
+	const uint32_t count = nn.ChunkNearestNeighbour[0] * nn.ChunkNearestNeighbour[1];
+	const size_t row = static_cast<size_t>(nn.MapSize[0]) * es, total_row = static_cast<size_t>(nn.TotalMapSize[0]) * es;
+	for (uint32_t i = 0u; i < count; i++) {
+		if (!chunks[i]) {
+			return inval("stpgb_nn_merge_host / stpgb_nn_unmerge_host: null chunk pointer");
+		}
+	}
+	for (uint32_t i = 0u; i < count; i++) {
+		uint32_t local[2];
+		STPGB_TRY(stpgb_chunk_local_coordinate(i, nn.ChunkNearestNeighbour, local));
+		unsigned char* const corner = merged + static_cast<size_t>(local[1]) * nn.MapSize[1] * total_row
+			+ static_cast<size_t>(local[0]) * row;
+		for (uint32_t y = 0u; y < nn.MapSize[1]; y++) {
+			if (Pack) {
+				std::memcpy(corner + y * total_row, chunks[i] + y * row, row);
+			} else {
+				std::memcpy(chunks[i] + y * row, corner + y * total_row, row);
+			}
+		}
+	}
+	return STPGB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int stpgb_nn_merge_host(const void* const* chunks, uint32_t element_size, const stpgb_nn_info* nn, void* merged) {
+	STPGB_TRY(check_nn(nn, element_size, "stpgb_nn_merge_host"));
+	if (!chunks || !merged) {
+		return inval("stpgb_nn_merge_host: null pointer argument");
+	}
+	return copy_neighbours<true>(static_cast<unsigned char*>(merged),
+		const_cast<unsigned char* const*>(reinterpret_cast<const unsigned char* const*>(chunks)), element_size, *nn);
+}
+
+int stpgb_nn_unmerge_host(const void* merged, uint32_t element_size, const stpgb_nn_info* nn, void* const* chunks) {
+	STPGB_TRY(check_nn(nn, element_size, "stpgb_nn_unmerge_host"));
+	if (!chunks || !merged) {
+		return inval("stpgb_nn_unmerge_host: null pointer argument");
+	}
+	return copy_neighbours<false>(const_cast<unsigned char*>(static_cast<const unsigned char*>(merged)),
+		reinterpret_cast<unsigned char* const*>(chunks), element_size, *nn);
 }
 
 } // extern "C"

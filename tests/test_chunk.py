@@ -1,5 +1,7 @@
-"""Chunk coordinate arithmetic (STPChunk's static functions) through the C ABI:
-the reference's own known answers (SuperTest+/SuperTerrain+/STPTest2DChunk.cpp:30-89)
+"""Chunk coordinate arithmetic (STPChunk's static functions) and the host
+memory mode of the nearest-neighbour merge (STPNearestNeighbourTextureBuffer)
+through the C ABI: the reference's own known answers
+(SuperTest+/SuperTerrain+/STPTest2DChunk.cpp:30-89, STPTestNearestNeighbour.cpp:49-101)
 and properties over many inputs.  Host-only: no GPU needed."""
 import itertools
 import math
@@ -85,3 +87,37 @@ def test_undefined_arguments_are_refused(chunk, stpgb):
         chunk.calcChunkMapOffset((8, 5), (0, 5), (512, 256), (0.0, 0.0))
     with pytest.raises(stpgb.STPNumericDomainError):
         chunk.calcChunkNeighbourOffset((8, 5), (0, 3))
+
+
+@pytest.mark.parametrize("dtype", [np.uint16, np.float32])
+def test_nearest_neighbour_merge_reference_scenario(stpgb, dtype):
+    """STPTestNearestNeighbour.cpp:49-101: a 3x3 neighbourhood of 2x2 chunks, chunk i filled with i,
+    merges into the map whose pixel (x, y) holds its chunk's index (x / 2) + (y / 2) * 3, and the
+    merged map unmerges back into the chunks."""
+    info = stpgb.NNInfo.make((2, 2), (3, 3))
+    chunks = [np.full((2, 2), i, dtype) for i in range(9)]
+    y, x = np.mgrid[0:6, 0:6]
+    want = ((x // 2) + (y // 2) * 3).astype(dtype)
+    assert np.array_equal(stpgb.nn_merge_host(chunks, info), want)
+    back = [np.zeros((2, 2), dtype) for _ in range(9)]
+    stpgb.nn_unmerge_host(want, info, back)
+    assert all(np.array_equal(b, c) for b, c in zip(back, chunks))
+
+
+def test_nearest_neighbour_merge_round_trip(stpgb):
+    rng = np.random.default_rng(4)
+    for ms, nn in (((7, 4), (5, 3)), ((16, 16), (1, 1)), ((3, 9), (1, 5))):
+        info = stpgb.NNInfo.make(ms, nn)
+        chunks = [rng.random((ms[1], ms[0])).astype(np.float32) for _ in range(nn[0] * nn[1])]
+        merged = stpgb.nn_merge_host(chunks, info)
+        assert merged.shape == (ms[1] * nn[1], ms[0] * nn[0])
+        for i, c in enumerate(chunks):
+            lx, ly = i % nn[0], i // nn[0]
+            assert np.array_equal(merged[ly * ms[1]:(ly + 1) * ms[1], lx * ms[0]:(lx + 1) * ms[0]], c)
+        back = [np.zeros_like(c) for c in chunks]
+        stpgb.nn_unmerge_host(merged, info, back)
+        assert all(np.array_equal(b, c) for b, c in zip(back, chunks))
+    bad = stpgb.NNInfo.make((2, 2), (3, 3))
+    bad.TotalMapSize[0] = 5
+    with pytest.raises(stpgb.STPNumericDomainError):
+        stpgb.nn_merge_host([np.zeros((2, 2), np.float32)] * 9, bad)
