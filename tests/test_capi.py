@@ -162,3 +162,20 @@ def test_erosion_choice_follows_density(stpgb, radius, droplets, side, lanes, ro
     got_lanes, got_rows = C.c_uint32(0), C.c_uint32(0)
     stpgb.check(stpgb.lib().stpgb_erosion_choice(radius, droplets, area, C.byref(got_lanes), C.byref(got_rows)))
     assert (got_lanes.value, got_rows.value) == (lanes, rows)
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/stpgb.h is the C boundary: it compiles as C11 with every warning, and a C program can
+    call an entry point through it and link against the library."""
+    from superterrainplus_gb300 import _capi
+    src = tmp_path / "caller.c"
+    src.write_text('#include "stpgb.h"\n#include <stdio.h>\n'
+                   'int main(void) { uint32_t out[2]; const uint32_t range[2] = { 5u, 7u };\n'
+                   '  int rc = stpgb_chunk_local_coordinate(7u, range, out);\n'
+                   '  printf("%d %u %u %s\\n", rc, out[0], out[1], stpgb_version()); return rc; }\n')
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_capi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    str(src), "-L" + libdir, "-lstpgb", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out[:3] == ["0", "2", "1"]

@@ -13,7 +13,7 @@ def facade_binary(tmp_path_factory, stpgb):
     from superterrainplus_gb300 import _capi
     out = str(tmp_path_factory.mktemp("facade") / "test_facade")
     libdir = os.path.dirname(_capi.LIB_PATH)
-    subprocess.check_call(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+    subprocess.check_call(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-I" + os.path.join(ROOT, "include"),
                            os.path.join(ROOT, "tests", "cpp", "test_facade.cpp"), "-L" + libdir, "-lstpgb",
                            "-Wl,-rpath," + libdir, "-o", out])
     return out
