@@ -2,7 +2,10 @@
 // free-slip neighbourhood, chunks of uneven side, own filter radius, droplet
 // count and brush) generated, filtered and eroded by one fixed sequence of
 // batched kernel launches -- every launch covers every chunk of every
-// request (grid.y = job) -- captured once into a CUDA graph and replayed.
+// request (grid.y = job; the erosion is one launch per variant group, side by
+// side, and the warp-cooperative kernel interleaves the blocks of several
+// jobs in a one-dimensional grid) -- captured once into a CUDA graph and
+// replayed.
 //
 // Device layout per request (side S, all buffers resident, one allocation):
 //   biome region   (5S)^2 uint16   the 3x3 diversity neighbourhoods of all
