@@ -554,7 +554,8 @@ typedef struct stpgb_batch_request {
 
 enum {
 	STPGB_BATCH_GRAPH = 1,   /* capture the launch sequence into a CUDA graph */
-	STPGB_BATCH_AUTOTUNE = 2 /* time the erosion kernel's lanes-per-droplet on the batch, keep the fastest */
+	STPGB_BATCH_AUTOTUNE = 2 /* at the first stpgb_batch_run, time the erosion variants on the batch's inputs
+	                          * (uploaded or synthesized by then) and keep the fastest per group */
 };
 
 /* Lays out and allocates every buffer of the batch on the current device in

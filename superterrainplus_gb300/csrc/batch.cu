@@ -150,6 +150,9 @@ struct stpgb_batch {
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	bool use_graph = false;
+	// STPGB_BATCH_AUTOTUNE: the autotuner runs at the first stpgb_batch_run,
+	// on the inputs the caller has uploaded or synthesized by then
+	bool tune_pending = false;
 
 	// (re)captures the launch sequence into a graph
 	int capture() {
@@ -586,9 +589,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 		}
 	}
 
-	if (flags & STPGB_BATCH_AUTOTUNE) {
-		STPGB_TRY(b->autotune());
-	}
+	b->tune_pending = (flags & STPGB_BATCH_AUTOTUNE) != 0u;
 	b->use_graph = (flags & STPGB_BATCH_GRAPH) != 0u;
 	if (b->use_graph) {
 		STPGB_TRY(b->capture());
@@ -602,6 +603,7 @@ int stpgb_batch_tune(stpgb_batch* b) {
 		return inval("stpgb_batch_tune: null batch");
 	}
 	STPGB_CUDA_TRY(cudaDeviceSynchronize());
+	b->tune_pending = false;
 	STPGB_TRY(b->autotune());
 	return b->use_graph ? b->capture() : STPGB_OK;
 }
@@ -684,6 +686,15 @@ int stpgb_batch_run(stpgb_batch* b, void* stream) {
 		return inval("stpgb_batch_run: null batch");
 	}
 	const cudaStream_t s = as_stream(stream);
+	if (b->tune_pending) {
+		// the caller's uploads on `s` complete before the tuner reads the inputs
+		STPGB_CUDA_TRY(cudaStreamSynchronize(s));
+		b->tune_pending = false;
+		STPGB_TRY(b->autotune());
+		if (b->use_graph) {
+			STPGB_TRY(b->capture());
+		}
+	}
 	if (b->exec) {
 		STPGB_CUDA_TRY(cudaGraphLaunch(b->exec, s));
 		return STPGB_OK;
