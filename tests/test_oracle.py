@@ -130,3 +130,52 @@ def test_erosion_oracle_mass_balance(oracle):
     assert abs((h.astype(np.float64).sum() - m.sum()) - res) < 1e-9 * h.sum()
     m32, res32, _ = oracle.erode(h, s, starts, idx, w, fp64=False)
     assert abs((h.astype(np.float64).sum() - m32.astype(np.float64).sum()) - res32) < 1e-5 * h.sum()
+
+
+@pytest.fixture(scope="module")
+def reference():
+    """The reference's own filter and permutation sources compiled here (absent where the reference
+    tree is not available: then these tests skip)."""
+    from oracle.oracle import Reference
+    try:
+        return Reference()
+    except Exception as e:  # no reference tree, or it could not be compiled here
+        pytest.skip(f"reference build unavailable: {e}")
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_shf_oracle_matches_live_reference(oracle, reference, seed):
+    """Random neighbourhoods (sides 3-40, 1-40 IDs, clustered or scattered, every legal even radius
+    drawn at random): the oracle's filter equals the reference's serial and 4-thread parallel
+    buffers, offsets and (item, weight) bins bit for bit, in bin order."""
+    rng = np.random.default_rng(1000 + seed)
+    mx, my = (int(v) for v in rng.integers(3, 41, 2))
+    nx, ny = 3, 3
+    ids = int(rng.integers(1, 41))
+    if seed % 2:
+        sm = rng.integers(0, ids, (ny * my, nx * mx)).astype(np.uint16)
+    else:
+        cell = int(rng.integers(2, 12))
+        sm = oracle.voronoi(nx * mx, ny * my, (int(rng.integers(-500, 500)), int(rng.integers(-500, 500))), cell,
+                            ids, seed)
+    r = 2 * int(rng.integers(1, min(mx, my) // 2 + 1))
+    rc, off, bins = oracle.shf(sm, (mx, my), (nx, ny), r)
+    assert rc == 0
+    for parallel in (False, True):
+        rrc, roff, rbins = reference.shf(sm, (mx, my), (nx, ny), r, parallel=parallel)
+        assert rrc == 0
+        assert np.array_equal(off, roff), (mx, my, r, parallel)
+        assert np.array_equal(bins["Item"], rbins["Item"])
+        assert np.array_equal(bins["Weight"].view(np.uint32), rbins["Weight"].view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 42, 6666, 2**40 + 7, 2**64 - 1])
+def test_permutation_oracle_matches_live_reference(oracle, reference, seed):
+    """Distributions whose gradient loop stays inside the reference's table (for 6, 11, 13, ... the
+    reference writes one gradient past it, which the oracle reports instead of repeating)."""
+    for distribution, offset in ((8, 0.2181661565), (10, 0.11344640137963143), (16, 0.0), (32, 6.0), (7, 3.1)):
+        rc, perm, grad = oracle.permutation(seed, distribution, offset)
+        rrc, rperm, rgrad = reference.permutation(seed, distribution, offset)
+        assert rc == rrc == 0
+        assert np.array_equal(perm, rperm)
+        assert np.array_equal(grad.view(np.uint32), rgrad.view(np.uint32))
