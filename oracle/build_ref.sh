@@ -2,7 +2,10 @@
 # Compiles the reference's own host sources for the single histogram filter,
 # the permutation generator and the demo's biome layer chain, where they lie in the read-only reference
 # tree, against the builder-written shims in oracle/refshim, into
-# oracle/_ref/libstpref.so.  Run in the development container only (the
+# oracle/_ref/libstpref.so; and the reference's device code for simplex noise,
+# the droplet, the demo's multi-biome generator script, the erosion brush and
+# the format kernel, compiled as host C++ against oracle/refshim/device, into
+# oracle/_ref/libstpref_device.so.  Run in the development container only (the
 # reference tree is not present on GPU machines).  The reference's CMake
 # build is not used.
 set -e
@@ -41,3 +44,29 @@ g++ -std=c++20 -O3 $ARCHFLAGS -fPIC -shared -pthread \
 	"$HERE/refshim/ref_api.cpp" \
 	-o "$OUT/libstpref.so"
 echo "built $OUT/libstpref.so"
+# Device code as host C++: the CUDA language extensions come from
+# refshim/device/device_prelude.hpp (forced include), CUDA and libcu++ headers
+# from the stand-ins beside it; no contraction into fused multiply-adds, so
+# that every float operation rounds as written.  Two pieces are not whole
+# files: the erosion brush generator is a static template inside
+# STPHeightfieldGenerator.cpp and the format kernel closes
+# STPHeightfieldKernel.cu, whose other kernels need curand.  Their text is
+# copied into the git-ignored build folder and included by
+# refshim/device/ref_brush.cpp and ref_format.cpp.
+sed -n '/^static T generateErosionBrush/,/Populate Device Memory/p' \
+	"$CORE/Private/World/Chunk/STPHeightfieldGenerator.cpp" > "$OUT/src/brush_generator.inc"
+sed -n '/^#include <cuda\/std\/limits>/,$p' "$CORE/Private/GPGPU/STPHeightfieldKernel.cu" > "$OUT/src/format_kernel.inc"
+[ -s "$OUT/src/brush_generator.inc" ] && [ -s "$OUT/src/format_kernel.inc" ] || { echo "brush or format source not found" >&2; exit 4; }
+g++ -std=c++20 -O2 -ffp-contract=off -fPIC -shared -Wl,--no-undefined -Wno-unknown-pragmas \
+	-include "$HERE/refshim/device/device_prelude.hpp" -D__CUDACC__ -D__CUDACC_RTC__ -DSTP_IMPLEMENTATION -DNDEBUG \
+	-I"$HERE/refshim/device" -I"$HERE/refshim" -I"$CORE/Public" -I"$ALG/Device/Public" -I"$ALG/Host/Public" \
+	-I"$REF/SuperDemo+" -I"$OUT/src" \
+	-x c++ "$ALG/Device/Private/STPSimplexNoise.cu" \
+	"$CORE/Private/GPGPU/STPRainDrop.cu" \
+	"$REF/SuperDemo+/Script/STPCommonGenerator.cu" \
+	"$REF/SuperDemo+/Script/STPMultiHeightGenerator.cu" \
+	-x none "$HERE/refshim/device/ref_device_api.cpp" \
+	"$HERE/refshim/device/ref_brush.cpp" \
+	"$HERE/refshim/device/ref_format.cpp" \
+	-o "$OUT/libstpref_device.so"
+echo "built $OUT/libstpref_device.so"

@@ -3,7 +3,9 @@
 Only the tests, the smoke check and bench.py's CPU-baseline leg use this
 module; it is what the product is compared with, never the product.  `Oracle` wraps the CPU
 restatement (oracle/liboracle.so), `Reference` wraps the reference's own
-compiled host sources (oracle/_ref/libstpref.so) where they could be built.
+compiled host sources (oracle/_ref/libstpref.so) and `DeviceReference` its
+device code compiled as host C++ (oracle/_ref/libstpref_device.so), where
+they could be built.
 """
 import ctypes as C
 import os
@@ -272,3 +274,73 @@ class Reference:
 
     def local_seed(self, global_seed, salt, x, z):
         return self.lib.ref_local_seed(global_seed, salt, x, z)
+
+
+class DeviceReference:
+    """The reference's own device code compiled as host C++ (oracle/_ref/libstpref_device.so):
+    simplex2D / simplex2DFractal (STPSimplexNoise.cu), the droplet (STPRainDrop.cu), the demo's
+    multi-biome generator script (STPMultiHeightGenerator.cu, two biomes), the erosion brush
+    generator (STPHeightfieldGenerator.cpp:44-77) and the format kernel (STPHeightfieldKernel.cu:110-121).
+    Kernels run as serial host loops; every float operation rounds as written."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_ref(device=True)
+        if not path or not os.path.exists(path):
+            raise FileNotFoundError("reference device build unavailable")
+        self.lib = L = C.CDLL(path)
+        vp, u32, f32 = C.c_void_p, C.c_uint32, C.c_float
+        L.ref_simplex2d.argtypes = [vp, vp, u32, f32, f32]
+        L.ref_simplex2d.restype = f32
+        L.ref_fractal.argtypes = [vp, vp, u32, f32, f32, f32, f32, u32, f32, f32, f32, f32, f32]
+        L.ref_fractal.restype = f32
+        L.ref_multibiome.argtypes = [vp, vp, vp, vp, vp, vp, u32, u32, u32, f32, f32]
+        L.ref_multibiome.restype = C.c_int
+        L.ref_erode.argtypes = [vp, u32, u32, vp, vp, u32, vp, vp, u32]
+        L.ref_erode.restype = C.c_int
+        L.ref_brush.argtypes = [u32, u32, vp, vp]
+        L.ref_brush.restype = u32
+        L.ref_format.argtypes = [vp, vp, u32]
+        L.ref_format.restype = None
+
+    def simplex2d(self, perm, grad, x, y):
+        return self.lib.ref_simplex2d(_p(perm), _p(grad), len(grad) // 2, x, y)
+
+    def fractal(self, perm, grad, x, y, pers, lacu, oct, scale, off, half):
+        return self.lib.ref_fractal(_p(perm), _p(grad), len(grad) // 2, x, y, pers, lacu, oct, scale, off[0], off[1],
+                                    half[0], half[1])
+
+    def multibiome(self, offsets, bins, table, perm, grad, map_size, offset):
+        mx, my = map_size
+        out = np.zeros(mx * my, np.float32)
+        table = np.ascontiguousarray(table, BIOME_DTYPE)
+        assert len(table) == 2
+        rc = self.lib.ref_multibiome(_p(out), _p(np.ascontiguousarray(offsets, np.uint32)),
+                                     _p(np.ascontiguousarray(bins, BIN_DTYPE)), _p(table), _p(perm), _p(grad),
+                                     len(grad) // 2, mx, my, offset[0], offset[1])
+        assert rc == 0, "the generator script's biome table holds biomes 0 and 1 only"
+        return out.reshape(my, mx)
+
+    def erode(self, heightmap, setting, starts, brush_index, brush_weight):
+        """Droplets one after another in start order on a float32 copy of `heightmap`."""
+        dim_y, dim_x = heightmap.shape
+        m = np.ascontiguousarray(heightmap, np.float32).copy()
+        s = OrcRaindrop(**setting)
+        starts = np.ascontiguousarray(starts, np.float32)
+        rc = self.lib.ref_erode(_p(m), dim_x, dim_y, C.byref(s), _p(starts), len(starts) // 2,
+                                _p(np.ascontiguousarray(brush_index, np.int32)),
+                                _p(np.ascontiguousarray(brush_weight, np.float32)), len(brush_index))
+        assert rc == 0
+        return m
+
+    def brush(self, dim_x, radius):
+        cap = (2 * radius + 1) ** 2
+        idx = np.zeros(cap, np.int32)
+        w = np.zeros(cap, np.float32)
+        n = self.lib.ref_brush(dim_x, radius, _p(idx), _p(w))
+        return idx[:n], w[:n]
+
+    def format(self, heightmap):
+        h = np.ascontiguousarray(heightmap, np.float32).ravel()
+        out = np.zeros(h.shape, np.uint16)
+        self.lib.ref_format(_p(h), _p(out), h.size)
+        return out.reshape(np.shape(heightmap))

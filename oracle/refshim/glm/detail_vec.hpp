@@ -29,12 +29,20 @@ template<typename T> constexpr tvec2<T> operator/(const tvec2<T>& a, T s) { retu
 template<typename T> constexpr tvec2<T> operator&(const tvec2<T>& a, const tvec2<T>& b) { return tvec2<T>(a.x & b.x, a.y & b.y); }
 template<typename T> constexpr bool operator==(const tvec2<T>& a, const tvec2<T>& b) { return a.x == b.x && a.y == b.y; }
 template<typename T> constexpr bool operator!=(const tvec2<T>& a, const tvec2<T>& b) { return !(a == b); }
+template<typename T> constexpr tvec2<T> operator-(const tvec2<T>& a) { return tvec2<T>(-a.x, -a.y); }
 
 template<typename T> struct tvec3 {
 	T x, y, z;
 	constexpr tvec3() : x(0), y(0), z(0) {}
 	constexpr explicit tvec3(T s) : x(s), y(s), z(s) {}
 	constexpr tvec3(T a, T b, T c) : x(a), y(b), z(c) {}
+};
+
+template<typename T> struct tvec4 {
+	T x, y, z, w;
+	constexpr tvec4() : x(0), y(0), z(0), w(0) {}
+	constexpr explicit tvec4(T s) : x(s), y(s), z(s), w(s) {}
+	constexpr tvec4(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
 };
 
 typedef tvec2<float> vec2;
@@ -45,5 +53,6 @@ typedef tvec3<float> vec3;
 typedef tvec3<double> dvec3;
 typedef tvec3<unsigned int> uvec3;
 typedef tvec3<int> ivec3;
+typedef tvec4<float> vec4;
 
 } // namespace glm

@@ -11,10 +11,13 @@
  * against the reference's own host sources compiled in this container
  * (oracle/build_ref.sh -> oracle/_ref), through committed fixtures in
  * tests/golden/.  The biome layer chain is pinned the same way against the
- * reference's STPLayer / STPBiomeFactory / demo layer sources.  Noise,
- * erosion and the splatmap have no reference test or CPU path: their
- * restatement follows the device code line by line (cited per function) and
- * is "parity unpinned" by reference outputs.
+ * reference's STPLayer / STPBiomeFactory / demo layer sources.  Noise, the
+ * multi-biome blend, the erosion brush, the FP32 serial droplet loop and the
+ * format are pinned bit for bit against the reference's own device code
+ * compiled as host C++ (oracle/refshim/device, oracle/_ref/libstpref_device.so;
+ * fixtures in tests/golden/device_reference.npz).  The splatmap's rule
+ * lookups follow the device code line by line; its texture reads restate the
+ * texture unit.
  *
  * Build: g++ -O2 -std=c++17 -ffp-contract=off -shared -fPIC (oracle/build.py).
  * -ffp-contract=off keeps every float operation separately rounded.

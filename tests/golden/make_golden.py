@@ -20,8 +20,15 @@ Fixtures:
                        biome-ID assignments, stored in full; STPLayer seed
                        arithmetic (mixSeed, seedLayer, seedLocal) known answers
   layer_digests.json   SHA-256 of the layer chain's output for large maps
+  device_reference.npz the reference's device code compiled as host C++
+                       (oracle/_ref/libstpref_device.so): simplex2D and
+                       simplex2DFractal values, the demo's two-biome generator
+                       script over filtered sample maps, droplets run one after
+                       another (STPRainDrop), erosion brushes and the format
+                       kernel, with their inputs
 
-`python tests/golden/make_golden.py layers` rewrites only the layer fixtures.
+`python tests/golden/make_golden.py layers` rewrites only the layer fixtures,
+`python tests/golden/make_golden.py device` only device_reference.npz.
 """
 import hashlib
 import json
@@ -34,7 +41,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle.oracle import Oracle, Reference  # noqa: E402
+from oracle.oracle import RAINDROP_FIELDS, BIOME_DTYPE, DeviceReference, Oracle, Reference  # noqa: E402
 
 KAT_TEXTURE = np.array([
     2, 0, 2, 0, 1, 1, 0, 3, 3, 2, 1, 2,
@@ -144,8 +151,119 @@ def digest(offsets, bins):
     return m.hexdigest()
 
 
+# (seed, distribution, offset) of the permutation tables the noise fixtures use
+DEVICE_PERMS = [(42, 8, 0.2181661565), (6666, 16, 0.0), (2**63 + 5, 32, 6.0)]
+# fractal parameter sets: persistence, lacunarity, octaves, scale, offset, half dimension
+FRACTAL_SETS = [(0.5, 2.0, 8, 300.0, (0.0, 0.0), (256.0, 256.0)),
+                (0.4, 2.5, 6, 123.5, (12.5, -40.25), (64.0, 32.0)),
+                (0.7, 1.88, 3, 91.5, (-5120.0, 9216.0), (512.0, 512.0)),
+                (0.25, 3.1, 10, 2048.0, (1.0e5, -3.3e4), (16.0, 16.0)),
+                (0.6, 2.2, 1, 17.0, (0.5, 0.5), (0.0, 0.0))]
+# two-biome generator cases: map size, neighbourhood, filter radius, cell size, seed, map offset
+MULTIBIOME_CASES = [((32, 32), (3, 3), 8, (20, 17), 1, (512.25, -96.5)),
+                    ((48, 40), (3, 3), 16, (13, 29), 2, (-7168.0, 2048.0)),
+                    ((16, 24), (3, 3), 2, (5, 3), 3, (0.0, 0.0))]
+TWO_BIOMES = [(160.0, 8, 0.4, 2.5, 0.2, 0.1), (330.0, 6, 0.5, 2.0, 0.0, 0.6)]
+# droplet cases: merged map side, brush radius, droplets, lifetime, inertia, seed
+EROSION_CASES = [(96, 3, 3000, 30, 0.05, 7), (96, 5, 1500, 64, 0.3, 8), (72, 2, 4000, 20, 0.0, 9)]
+
+
+def raindrop_setting(count, radius, lifetime, inertia):
+    """The small workload's droplet setting; the lifetime is set through minWaterVolume."""
+    evap = np.float32(0.01)
+    v = np.float32(1.0)
+    for _ in range(lifetime):
+        v = np.float32(v * np.float32(np.float32(1.0) - evap))
+    d = dict(Seed=42, RainDropCount=count, Inertia=inertia, SedimentCapacityFactor=4.0, minSedimentCapacity=0.01,
+             initWaterVolume=1.0, minWaterVolume=float(np.nextafter(v, np.float32(np.inf))), Friction=0.1,
+             initSpeed=1.0, ErodeSpeed=0.3, DepositSpeed=0.3, EvaporateSpeed=float(evap), Gravity=4.0,
+             ErosionBrushRadius=radius)
+    return d
+
+
+def erosion_input(n, seed):
+    """A smooth seeded relief with fine noise, in [0.1, 0.95], rounded to float16 values so that the
+    stored input is half the size."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:n, 0:n].astype(np.float64)
+    h = 0.5 + 0.3 * np.sin(x / 9.0 + seed) * np.cos(y / 7.0) + 0.1 * np.sin((x + 2 * y) / 23.0) \
+        + 0.05 * rng.random((n, n))
+    return h.astype(np.float16)
+
+
+def two_id_samplemap(total, cell, seed):
+    """Checkerboard of two biome IDs with cell sides `cell`, shifted by the seed."""
+    y, x = np.mgrid[0:total[1], 0:total[0]]
+    return np.where(((x + 3 * seed) // cell[0] + (y + 5 * seed) // cell[1]) % 2 == 0, 0, 1).astype(np.uint16)
+
+
+def make_device(orc):
+    dev = DeviceReference()
+    out = {}
+    rng = np.random.default_rng(2024)
+    for t, (seed, n, off) in enumerate(DEVICE_PERMS):
+        rc, perm, grad = orc.permutation(seed, n, off)
+        assert rc == 0
+        out[f"t{t}_perm"], out[f"t{t}_grad"] = perm, grad
+        # large, negative, near-integer and zero coordinates
+        pts = np.concatenate([rng.uniform(-1e4, 1e4, (1024, 2)), rng.uniform(-8, 8, (1024, 2)),
+                              np.round(rng.uniform(-300, 300, (256, 2))) + rng.choice([0.0, 1e-4, -1e-4], (256, 2)),
+                              np.zeros((1, 2))]).astype(np.float32)
+        out[f"t{t}_simplex_xy"] = pts
+        out[f"t{t}_simplex"] = np.array([dev.simplex2d(perm, grad, x, y) for x, y in pts], np.float32)
+        fpts = rng.uniform(-2000, 2000, (256, 2)).astype(np.float32)
+        out[f"t{t}_fractal_xy"] = fpts
+        out[f"t{t}_fractal"] = np.array([[dev.fractal(perm, grad, x, y, *fs) for x, y in fpts]
+                                         for fs in FRACTAL_SETS], np.float32)
+    out["fractal_sets"] = np.array([(p, l, o, sc, ox, oy, hx, hy) for p, l, o, sc, (ox, oy), (hx, hy)
+                                    in FRACTAL_SETS], np.float64)
+    table = np.array(TWO_BIOMES, BIOME_DTYPE)
+    out["two_biomes"] = table
+    rc, perm, grad = orc.permutation(*DEVICE_PERMS[0])
+    for i, (ms, nn, r, cell, seed, off) in enumerate(MULTIBIOME_CASES):
+        sm = two_id_samplemap((ms[0] * nn[0], ms[1] * nn[1]), cell, seed)
+        rc, offsets, bins = orc.shf(sm, ms, nn, r)
+        assert rc == 0
+        out[f"m{i}_samplemap"] = sm
+        out[f"m{i}_meta"] = np.array([*ms, *nn, r], np.int64)
+        out[f"m{i}_offset"] = np.array(off, np.float32)
+        out[f"m{i}_height"] = dev.multibiome(offsets, bins, table, perm, grad, ms, off)
+    out["multibiome_count"] = np.array(len(MULTIBIOME_CASES))
+    for i, (n, radius, count, lifetime, inertia, seed) in enumerate(EROSION_CASES):
+        s = raindrop_setting(count, radius, lifetime, inertia)
+        h = erosion_input(n, seed)
+        # starts in the central chunk of a 3x3 neighbourhood, as the reference spawns them (the
+        # oracle's Philox stream, pinned by its known answers, regenerates them from the seed)
+        starts = orc.droplet_starts(count, seed, 0, (n // 3, n // 3), (3, 3))
+        idx, w = dev.brush(n, radius)
+        out[f"e{i}_setting"] = np.array([s[k] for k, _ in RAINDROP_FIELDS], np.float64)
+        out[f"e{i}_meta"] = np.array([n, radius, count, lifetime, seed], np.int64)
+        out[f"e{i}_input"] = h
+        out[f"e{i}_output"] = dev.erode(h.astype(np.float32), s, starts, idx, w)
+    out["erosion_count"] = np.array(len(EROSION_CASES))
+    brushes = []
+    for dim_x in (300, 1000):
+        for radius in range(1, 11):
+            idx, w = dev.brush(dim_x, radius)
+            brushes.append((dim_x, radius, idx, w))
+    out["brush_meta"] = np.array([(d, r, len(i)) for d, r, i, _ in brushes], np.int64)
+    out["brush_index"] = np.concatenate([i for _, _, i, _ in brushes])
+    out["brush_weight"] = np.concatenate([w for _, _, _, w in brushes])
+    vals = np.concatenate([rng.uniform(-0.5, 1.5, 2048),
+                           np.arange(0, 65536, 97) / 65535.0 + rng.choice([0.0, 3e-8, -3e-8, 7.6e-6], 676),
+                           [np.nan, np.inf, -np.inf, -0.0, 0.0, 1.0, 0.5 / 65535, 1.5 / 65535]]).astype(np.float32)
+    out["format_input"] = vals
+    out["format_output"] = dev.format(vals)
+    np.savez_compressed(os.path.join(HERE, "device_reference.npz"), **out)
+
+
 def main():
-    orc, ref = Oracle(), Reference()
+    orc = Oracle()
+    if sys.argv[1:] == ["device"]:
+        make_device(orc)
+        print("device fixtures written to", HERE)
+        return
+    ref = Reference()
     make_layers(ref)
     if sys.argv[1:] == ["layers"]:
         print("layer fixtures written to", HERE)
@@ -196,6 +314,7 @@ def main():
         perm[f"p{i}_grad"] = g
     perm["count"] = np.array(len(PERM_CASES))
     np.savez_compressed(os.path.join(HERE, "permutation.npz"), **perm)
+    make_device(orc)
     print("fixtures written to", HERE)
 
 
