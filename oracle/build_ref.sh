@@ -3,8 +3,9 @@
 # the permutation generator and the demo's biome layer chain, where they lie in the read-only reference
 # tree, against the builder-written shims in oracle/refshim, into
 # oracle/_ref/libstpref.so; and the reference's device code for simplex noise,
-# the droplet, the demo's multi-biome generator script, the erosion brush and
-# the format kernel, compiled as host C++ against oracle/refshim/device, into
+# the droplet, the demo's multi-biome and splatmap generator scripts with the
+# splat rule lookups, the erosion brush and the format kernel, compiled as
+# host C++ against oracle/refshim/device, into
 # oracle/_ref/libstpref_device.so.  Run in the development container only (the
 # reference tree is not present on GPU machines).  The reference's CMake
 # build is not used.
@@ -65,7 +66,10 @@ g++ -std=c++20 -O2 -ffp-contract=off -fPIC -shared -Wl,--no-undefined -Wno-unkno
 	"$CORE/Private/GPGPU/STPRainDrop.cu" \
 	"$REF/SuperDemo+/Script/STPCommonGenerator.cu" \
 	"$REF/SuperDemo+/Script/STPMultiHeightGenerator.cu" \
+	"$REF/SuperDemo+/Script/STPSplatmapGenerator.cu" \
+	"$ALG/Device/Private/STPTextureSplatRuleWrapper.cu" \
 	-x none "$HERE/refshim/device/ref_device_api.cpp" \
+	"$HERE/refshim/device/ref_splat_api.cpp" \
 	"$HERE/refshim/device/ref_brush.cpp" \
 	"$HERE/refshim/device/ref_format.cpp" \
 	-o "$OUT/libstpref_device.so"

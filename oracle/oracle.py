@@ -279,8 +279,10 @@ class Reference:
 class DeviceReference:
     """The reference's own device code compiled as host C++ (oracle/_ref/libstpref_device.so):
     simplex2D / simplex2DFractal (STPSimplexNoise.cu), the droplet (STPRainDrop.cu), the demo's
-    multi-biome generator script (STPMultiHeightGenerator.cu, two biomes), the erosion brush
-    generator (STPHeightfieldGenerator.cpp:44-77) and the format kernel (STPHeightfieldKernel.cu:110-121).
+    multi-biome generator script (STPMultiHeightGenerator.cu, two biomes), the demo's splatmap
+    script with the rule lookups (STPSplatmapGenerator.cu, STPTextureSplatRuleWrapper.cu; texture
+    fetches and rnormf are stand-ins), the erosion brush generator
+    (STPHeightfieldGenerator.cpp:44-77) and the format kernel (STPHeightfieldKernel.cu:110-121).
     Kernels run as serial host loops; every float operation rounds as written."""
 
     def __init__(self, path=None):
@@ -301,6 +303,8 @@ class DeviceReference:
         L.ref_brush.restype = u32
         L.ref_format.argtypes = [vp, vp, u32]
         L.ref_format.restype = None
+        L.ref_splatmap.argtypes = [vp, vp, u32, u32, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp, vp, vp, u32, vp, u32]
+        L.ref_splatmap.restype = C.c_int
 
     def simplex2d(self, perm, grad, x, y):
         return self.lib.ref_simplex2d(_p(perm), _p(grad), len(grad) // 2, x, y)
@@ -344,3 +348,16 @@ class DeviceReference:
         out = np.zeros(h.shape, np.uint16)
         self.lib.ref_format(_p(h), _p(out), h.size)
         return out.reshape(np.shape(heightmap))
+
+    def splatmap(self, biomemap, heightmap, chunks, map_size, altitude_rules, gradient_rules, perm, grad):
+        """Region map (uint8, 255 = none) of the requested chunks, as Oracle.splatmap."""
+        h, w = heightmap.shape
+        dict_, reg, alt, gra = splat_rule_tables(altitude_rules, gradient_rules)
+        ch = np.array([tuple(c) for c in chunks], SPLAT_CHUNK_DTYPE)
+        out = np.zeros((h, w), np.uint8)
+        rc = self.lib.ref_splatmap(_p(np.ascontiguousarray(biomemap, np.uint16)),
+                                   _p(np.ascontiguousarray(heightmap, np.uint16)), w, w, h, _p(ch), len(ch),
+                                   map_size[0], map_size[1], _p(dict_), len(dict_), _p(reg), _p(alt), _p(gra),
+                                   _p(perm), _p(grad), len(grad) // 2, _p(out), w)
+        assert rc == 0, "a write left the surface"
+        return out

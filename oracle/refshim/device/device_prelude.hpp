@@ -48,3 +48,18 @@ static inline float atomicAdd(float* const address, const float value) {
 static inline float __saturatef(const float v) {
 	return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f;
 }
+
+// Texture and surface objects of the splatmap script: handles to host
+// descriptors that the harness (refshim/device/ref_splat_api.cpp) fills in;
+// the fetches there restate the sampler the reference configures.
+struct int2 { int x, y; };
+typedef unsigned long long cudaTextureObject_t;
+typedef unsigned long long cudaSurfaceObject_t;
+enum cudaSurfaceBoundaryMode { cudaBoundaryModeZero = 0, cudaBoundaryModeClamp = 1, cudaBoundaryModeTrap = 2 };
+template<class T> T tex2D(cudaTextureObject_t, float, float);
+template<> float tex2D<float>(cudaTextureObject_t, float, float);
+template<> unsigned short tex2D<unsigned short>(cudaTextureObject_t, float, float);
+template<class T> void surf2Dwrite(T, cudaSurfaceObject_t, int, int, cudaSurfaceBoundaryMode);
+template<> void surf2Dwrite<unsigned char>(unsigned char, cudaSurfaceObject_t, int, int, cudaSurfaceBoundaryMode);
+// rnormf(n, a): 1 / sqrt(a[0]^2 + ... + a[n-1]^2), here the double-precision value rounded to float
+float rnormf(int, const float*);

@@ -15,9 +15,10 @@
  * multi-biome blend, the erosion brush, the FP32 serial droplet loop and the
  * format are pinned bit for bit against the reference's own device code
  * compiled as host C++ (oracle/refshim/device, oracle/_ref/libstpref_device.so;
- * fixtures in tests/golden/device_reference.npz).  The splatmap's rule
- * lookups follow the device code line by line; its texture reads restate the
- * texture unit.
+ * fixtures in tests/golden/device_reference.npz).  The splatmap's region
+ * maps equal the demo's script and rule lookups compiled the same way; its
+ * texture reads and rnormf restate the texture unit and the math function
+ * (the same stand-ins serve the compiled script).
  *
  * Build: g++ -O2 -std=c++17 -ffp-contract=off -shared -fPIC (oracle/build.py).
  * -ffp-contract=off keeps every float operation separately rounded.

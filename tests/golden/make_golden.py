@@ -24,8 +24,9 @@ Fixtures:
                        (oracle/_ref/libstpref_device.so): simplex2D and
                        simplex2DFractal values, the demo's two-biome generator
                        script over filtered sample maps, droplets run one after
-                       another (STPRainDrop), erosion brushes and the format
-                       kernel, with their inputs
+                       another (STPRainDrop), the demo's splatmap script with
+                       the rule lookups, erosion brushes and the format kernel,
+                       with their inputs
 
 `python tests/golden/make_golden.py layers` rewrites only the layer fixtures,
 `python tests/golden/make_golden.py device` only device_reference.npz.
@@ -41,7 +42,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle.oracle import RAINDROP_FIELDS, BIOME_DTYPE, DeviceReference, Oracle, Reference  # noqa: E402
+from oracle.oracle import (RAINDROP_FIELDS, BIOME_DTYPE, DeviceReference, Oracle, Reference,  # noqa: E402
+                           splat_rule_tables)
 
 KAT_TEXTURE = np.array([
     2, 0, 2, 0, 1, 1, 0, 3, 3, 2, 1, 2,
@@ -164,6 +166,24 @@ MULTIBIOME_CASES = [((32, 32), (3, 3), 8, (20, 17), 1, (512.25, -96.5)),
                     ((48, 40), (3, 3), 16, (13, 29), 2, (-7168.0, 2048.0)),
                     ((16, 24), (3, 3), 2, (5, 3), 3, (0.0, 0.0))]
 TWO_BIOMES = [(160.0, 8, 0.4, 2.5, 0.2, 0.1), (330.0, 6, 0.5, 2.0, 0.0, 0.6)]
+# the demo's splat rules (SuperDemo+/Script/STPBiomeSplatRule.tdl): (sample, upper bound, region) and
+# (sample, min gradient, max gradient, lower bound, upper bound, region)
+DEMO_ALTITUDE = [(0, 1.0, 4), (1, 0.5, 3), (1, 0.72, 2), (1, 1.0, 1)]
+DEMO_GRADIENT = [(0, 0.0, 0.2, 0.0, 0.27, 3), (1, 0.4, 0.65, 0.58, 0.8, 5), (1, 0.625, 1.0, 0.65, 1.0, 0)]
+
+
+def splat_random_rules(rng, samples):
+    alt, gra = [], []
+    for smp in samples:
+        for ub in sorted(rng.uniform(0.1, 1.0, int(rng.integers(1, 4)))):
+            alt.append((smp, float(ub), int(rng.integers(0, 8))))
+        for _ in range(int(rng.integers(0, 3))):
+            g0, g1 = sorted(rng.uniform(0, 1, 2))
+            a0, a1 = sorted(rng.uniform(0, 1, 2))
+            gra.append((smp, float(g0), float(g1), float(a0), float(a1), int(rng.integers(0, 8))))
+    return alt, gra
+
+
 # droplet cases: merged map side, brush radius, droplets, lifetime, inertia, seed
 EROSION_CASES = [(96, 3, 3000, 30, 0.05, 7), (96, 5, 1500, 64, 0.3, 8), (72, 2, 4000, 20, 0.0, 9)]
 
@@ -241,6 +261,30 @@ def make_device(orc):
         out[f"e{i}_input"] = h
         out[f"e{i}_output"] = dev.erode(h.astype(np.float32), s, starts, idx, w)
     out["erosion_count"] = np.array(len(EROSION_CASES))
+    # splatmaps of a 3x3 rendering buffer of 32^2 chunks: the demo's rules over all 9 chunks, then
+    # random rules for samples 0-4 (sample 5 has none) over 4 chunks
+    S = 32
+    y, x = np.mgrid[0:3 * S, 0:3 * S]
+    for i, seed in enumerate((11, 12)):
+        srng = np.random.default_rng(seed)
+        hm = ((0.5 + 0.4 * np.sin(x / srng.uniform(5, 15)) * np.cos(y / srng.uniform(5, 15))
+               + 0.05 * srng.random(x.shape)) * 65535).clip(0, 65535).astype(np.uint16)
+        if i == 0:
+            bm = ((x // 37 + y // 29) % 3).astype(np.uint16)
+            alt, gra = DEMO_ALTITUDE, DEMO_GRADIENT
+            chunks = [(c % 3, c // 3, float(c * 512.0 - 2048.0), float(1024.0 - c * 256.0)) for c in range(9)]
+        else:
+            bm = ((x // 11 + 2 * (y // 17)) % 6).astype(np.uint16)
+            alt, gra = splat_random_rules(srng, range(5))
+            chunks = [(c % 3, c // 3, float(srng.uniform(-1e4, 1e4)), float(srng.uniform(-1e4, 1e4)))
+                      for c in (0, 4, 5, 7)]
+        d, reg, an, gn = splat_rule_tables(alt, gra)
+        out[f"s{i}_biomemap"], out[f"s{i}_heightmap"] = bm, hm
+        out[f"s{i}_chunks"] = np.array(chunks, np.float64)
+        out[f"s{i}_altitude_rules"] = np.array(alt, np.float64).reshape(-1, 3)
+        out[f"s{i}_gradient_rules"] = np.array(gra, np.float64).reshape(-1, 6)
+        out[f"s{i}_regions"] = dev.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
+    out["splat_count"] = np.array(2)
     brushes = []
     for dim_x in (300, 1000):
         for radius in range(1, 11):

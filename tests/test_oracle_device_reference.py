@@ -1,9 +1,12 @@
-"""Pins the oracle's noise, multi-biome blend, droplet, brush and format
-restatements against the reference's own device code compiled as host C++
-(oracle/build_ref.sh: STPSimplexNoise.cu, STPRainDrop.cu, the demo's
-STPMultiHeightGenerator.cu script, the brush generator of
+"""Pins the oracle's noise, multi-biome blend, droplet, brush, format and
+splatmap restatements against the reference's own device code compiled as
+host C++ (oracle/build_ref.sh: STPSimplexNoise.cu, STPRainDrop.cu, the demo's
+STPMultiHeightGenerator.cu and STPSplatmapGenerator.cu scripts,
+STPTextureSplatRuleWrapper.cu, the brush generator of
 STPHeightfieldGenerator.cpp and the format kernel of STPHeightfieldKernel.cu),
-run one thread at a time with no fused multiply-adds.  The oracle must agree
+run one thread at a time with no fused multiply-adds.  For the splatmap the
+texture fetches and rnormf are host stand-ins, so that pin covers the
+script's sampling positions, noise, altitude and rule lookups.  The oracle must agree
 bit for bit: with the committed fixtures that build produced
 (tests/golden/device_reference.npz) everywhere, and with the live build on
 random inputs where the reference tree is present.  CPU only."""
@@ -104,6 +107,19 @@ def test_brush_and_format_match_reference_fixtures(oracle, fix):
     assert np.array_equal(oracle.format(fix["format_input"]), fix["format_output"])
 
 
+def test_splatmap_matches_reference_script_fixtures(oracle, fix):
+    """The demo's splatmap script: the demo's rules over the 9 chunks of a 3x3 buffer, and random
+    rules (a sample without rules, empty gradient lists) over 4 of them."""
+    rc, perm, grad = oracle.permutation(42, 8, 0.2181661565)
+    for i in range(int(fix["splat_count"])):
+        alt = [(int(a), float(b), int(c)) for a, b, c in fix[f"s{i}_altitude_rules"]]
+        gra = [(int(r[0]), *(float(v) for v in r[1:5]), int(r[5])) for r in fix[f"s{i}_gradient_rules"]]
+        chunks = [(int(a), int(b), float(c), float(d)) for a, b, c, d in fix[f"s{i}_chunks"]]
+        got, _, _ = oracle.splatmap(fix[f"s{i}_biomemap"], fix[f"s{i}_heightmap"], chunks, (32, 32), alt, gra,
+                                    perm, grad)
+        assert np.array_equal(got, fix[f"s{i}_regions"]), i
+
+
 # ------------------------------------------------------------ live builds
 
 SAFE_DISTRIBUTIONS = [(8, 0.2181661565), (10, 0.11344640137963143), (16, 0.0), (32, 6.0), (7, 3.1)]
@@ -183,3 +199,27 @@ def test_brush_and_format_match_live_reference(oracle, device_reference):
     v = np.concatenate([rng.uniform(-1, 2, 100000), rng.standard_normal(1000) * 1e-6,
                         np.arange(65536) / 65535.0 + 0.5 / 65535]).astype(np.float32)
     assert np.array_equal(oracle.format(v), device_reference.format(v))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_splatmap_matches_live_reference(oracle, device_reference, seed):
+    rng = np.random.default_rng(400 + seed)
+    S = int(rng.integers(2, 7)) * 8
+    y, x = np.mgrid[0:3 * S, 0:3 * S]
+    hm = ((0.5 + 0.45 * np.sin(x / rng.uniform(3, 12)) * np.cos(y / rng.uniform(3, 12))
+           + 0.05 * rng.random(x.shape)) * 65535).clip(0, 65535).astype(np.uint16)
+    bm = rng.integers(0, 6, x.shape).astype(np.uint16)
+    alt, gra = [], []
+    for smp in range(5):
+        for ub in sorted(rng.uniform(0.1, 1.0, int(rng.integers(1, 4)))):
+            alt.append((smp, float(ub), int(rng.integers(0, 8))))
+        for _ in range(int(rng.integers(0, 3))):
+            g0, g1 = sorted(rng.uniform(0, 1, 2))
+            a0, a1 = sorted(rng.uniform(0, 1, 2))
+            gra.append((smp, float(g0), float(g1), float(a0), float(a1), int(rng.integers(0, 8))))
+    chunks = [(c % 3, c // 3, float(rng.uniform(-1e5, 1e5)), float(rng.uniform(-1e5, 1e5))) for c in range(9)
+              if rng.random() < 0.7]
+    rc, perm, grad = oracle.permutation(seed, 8, 0.2181661565)
+    want = device_reference.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
+    got, _, _ = oracle.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
+    assert np.array_equal(got, want)
