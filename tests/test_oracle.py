@@ -179,3 +179,31 @@ def test_permutation_oracle_matches_live_reference(oracle, reference, seed):
         assert rc == rrc == 0
         assert np.array_equal(perm, rperm)
         assert np.array_equal(grad.view(np.uint32), rgrad.view(np.uint32))
+
+
+@pytest.mark.parametrize("params", [(64, 9400, 4, 50), (128, 37500, 3, 30)])
+def test_droplet_order_spread_exceeds_fp64_distance(oracle, params):
+    """The reference's droplet arithmetic (the FP32 serial oracle, equal to the reference's
+    STPRainDrop bit for bit) depends on the order the droplets run in: a shuffled order moves the
+    map by an RMS of about 1e-3 to 2e-3.  The FP64 oracle is closer to the index-order run than any
+    reordered run is, so an RMS band measured against it bounds order effects, not a bias of the
+    oracle."""
+    S, count, brush, life = params
+    rng = np.random.default_rng(S)
+    y, x = np.mgrid[0:3 * S, 0:3 * S]
+    h = (0.5 + 0.25 * np.sin(x / 23.0) * np.cos(y / 17.0) + 0.15 * np.sin((x + 2 * y) / 41.0)
+         + 0.02 * rng.random(x.shape)).astype(np.float32)
+    s = helpers.raindrop_dict(count, radius=brush, lifetime=life)
+    starts = oracle.droplet_starts(count, 9, 0, (S, S), (3, 3))
+    idx, w = oracle.brush(3 * S, brush)
+
+    def rms(a, b):
+        return float(np.sqrt(((a.astype(np.float64) - b.astype(np.float64)) ** 2).mean()))
+
+    f64, _, _ = oracle.erode(h, s, starts, idx, w, fp64=True)
+    f32, _, _ = oracle.erode(h, s, starts, idx, w, fp64=False)
+    shuffled = [oracle.erode(h, s, starts.reshape(-1, 2)[rng.permutation(count)].ravel(), idx, w, fp64=False)[0]
+                for _ in range(3)]
+    order_spread = [rms(f32, m) for m in shuffled]
+    assert min(order_spread) > 5e-4
+    assert rms(f32, f64) < min(order_spread)
