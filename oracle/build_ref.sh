@@ -50,14 +50,17 @@ echo "built $OUT/libstpref.so"
 # from the stand-ins beside it; no contraction into fused multiply-adds, so
 # that every float operation rounds as written.  Two pieces are not whole
 # files: the erosion brush generator is a static template inside
-# STPHeightfieldGenerator.cpp and the format kernel closes
-# STPHeightfieldKernel.cu, whose other kernels need curand.  Their text is
+# STPHeightfieldGenerator.cpp, and the erosion and format kernels sit in
+# STPHeightfieldKernel.cu beside the curand set-up kernel.  Their text is
 # copied into the git-ignored build folder and included by
-# refshim/device/ref_brush.cpp and ref_format.cpp.
+# refshim/device/ref_brush.cpp, ref_erosion_kernel.cpp and ref_format.cpp.
 sed -n '/^static T generateErosionBrush/,/Populate Device Memory/p' \
 	"$CORE/Private/World/Chunk/STPHeightfieldGenerator.cpp" > "$OUT/src/brush_generator.inc"
 sed -n '/^#include <cuda\/std\/limits>/,$p' "$CORE/Private/GPGPU/STPHeightfieldKernel.cu" > "$OUT/src/format_kernel.inc"
-[ -s "$OUT/src/brush_generator.inc" ] && [ -s "$OUT/src/format_kernel.inc" ] || { echo "brush or format source not found" >&2; exit 4; }
+sed -n '/^__global__ void hydraulicErosionKERNEL/,/^}/p' "$CORE/Private/GPGPU/STPHeightfieldKernel.cu" > "$OUT/src/erosion_kernel.inc"
+for f in brush_generator format_kernel erosion_kernel; do
+	[ -s "$OUT/src/$f.inc" ] || { echo "$f source not found" >&2; exit 4; }
+done
 g++ -std=c++20 -O2 -ffp-contract=off -fPIC -shared -Wl,--no-undefined -Wno-unknown-pragmas \
 	-include "$HERE/refshim/device/device_prelude.hpp" -D__CUDACC__ -D__CUDACC_RTC__ -DSTP_IMPLEMENTATION -DNDEBUG \
 	-I"$HERE/refshim/device" -I"$HERE/refshim" -I"$CORE/Public" -I"$ALG/Device/Public" -I"$ALG/Host/Public" \
@@ -72,5 +75,6 @@ g++ -std=c++20 -O2 -ffp-contract=off -fPIC -shared -Wl,--no-undefined -Wno-unkno
 	"$HERE/refshim/device/ref_splat_api.cpp" \
 	"$HERE/refshim/device/ref_brush.cpp" \
 	"$HERE/refshim/device/ref_format.cpp" \
+	"$HERE/refshim/device/ref_erosion_kernel.cpp" \
 	-o "$OUT/libstpref_device.so"
 echo "built $OUT/libstpref_device.so"

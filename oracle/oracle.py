@@ -281,7 +281,8 @@ class DeviceReference:
     simplex2D / simplex2DFractal (STPSimplexNoise.cu), the droplet (STPRainDrop.cu), the demo's
     multi-biome generator script (STPMultiHeightGenerator.cu, two biomes), the demo's splatmap
     script with the rule lookups (STPSplatmapGenerator.cu, STPTextureSplatRuleWrapper.cu; texture
-    fetches and rnormf are stand-ins), the erosion brush generator
+    fetches and rnormf are stand-ins), the erosion kernel with its droplet spawn
+    (STPHeightfieldKernel.cu:80-108; curand draws supplied by the caller), the erosion brush generator
     (STPHeightfieldGenerator.cpp:44-77) and the format kernel (STPHeightfieldKernel.cu:110-121).
     Kernels run as serial host loops; every float operation rounds as written."""
 
@@ -305,6 +306,8 @@ class DeviceReference:
         L.ref_format.restype = None
         L.ref_splatmap.argtypes = [vp, vp, u32, u32, u32, vp, u32, u32, u32, vp, u32, vp, vp, vp, vp, vp, u32, vp, u32]
         L.ref_splatmap.restype = C.c_int
+        L.ref_erosion_kernel.argtypes = [vp, vp, vp, vp, vp, u32, vp, vp, u32]
+        L.ref_erosion_kernel.restype = C.c_int
 
     def simplex2d(self, perm, grad, x, y):
         return self.lib.ref_simplex2d(_p(perm), _p(grad), len(grad) // 2, x, y)
@@ -361,3 +364,16 @@ class DeviceReference:
                                    _p(perm), _p(grad), len(grad) // 2, _p(out), w)
         assert rc == 0, "a write left the surface"
         return out
+
+    def erosion_kernel(self, heightmap, map_size, nn, setting, uniforms, brush_index, brush_weight):
+        """hydraulicErosionKERNEL over droplets 0..count-1 in index order on a float32 copy of the
+        merged map; `uniforms` holds each droplet's two curand_uniform draws."""
+        m = np.ascontiguousarray(heightmap, np.float32).copy()
+        s = OrcRaindrop(**setting)
+        u = np.ascontiguousarray(uniforms, np.float32)
+        ms, n = np.array(map_size, np.uint32), np.array(nn, np.uint32)
+        rc = self.lib.ref_erosion_kernel(_p(m), _p(ms), _p(n), C.byref(s), _p(u), len(u) // 2,
+                                         _p(np.ascontiguousarray(brush_index, np.int32)),
+                                         _p(np.ascontiguousarray(brush_weight, np.float32)), len(brush_index))
+        assert rc == 0
+        return m

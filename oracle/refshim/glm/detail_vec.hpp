@@ -18,6 +18,8 @@ template<typename T> struct tvec2 {
 	tvec2& operator-=(const tvec2& o) { x -= o.x; y -= o.y; return *this; }
 	tvec2& operator*=(T s) { x *= s; y *= s; return *this; }
 	tvec2& operator/=(T s) { x /= s; y /= s; return *this; }
+	template<typename U> tvec2& operator+=(const tvec2<U>& o) { x += static_cast<T>(o.x); y += static_cast<T>(o.y); return *this; }
+	template<typename U> tvec2& operator*=(const tvec2<U>& o) { x *= static_cast<T>(o.x); y *= static_cast<T>(o.y); return *this; }
 };
 template<typename T> constexpr tvec2<T> operator+(const tvec2<T>& a, const tvec2<T>& b) { return tvec2<T>(a.x + b.x, a.y + b.y); }
 template<typename T> constexpr tvec2<T> operator-(const tvec2<T>& a, const tvec2<T>& b) { return tvec2<T>(a.x - b.x, a.y - b.y); }
@@ -26,6 +28,7 @@ template<typename T> constexpr tvec2<T> operator/(const tvec2<T>& a, const tvec2
 template<typename T> constexpr tvec2<T> operator*(const tvec2<T>& a, T s) { return tvec2<T>(a.x * s, a.y * s); }
 template<typename T> constexpr tvec2<T> operator*(T s, const tvec2<T>& a) { return tvec2<T>(a.x * s, a.y * s); }
 template<typename T> constexpr tvec2<T> operator/(const tvec2<T>& a, T s) { return tvec2<T>(a.x / s, a.y / s); }
+template<typename T> constexpr tvec2<T> operator-(const tvec2<T>& a, T s) { return tvec2<T>(a.x - s, a.y - s); }
 template<typename T> constexpr tvec2<T> operator&(const tvec2<T>& a, const tvec2<T>& b) { return tvec2<T>(a.x & b.x, a.y & b.y); }
 template<typename T> constexpr bool operator==(const tvec2<T>& a, const tvec2<T>& b) { return a.x == b.x && a.y == b.y; }
 template<typename T> constexpr bool operator!=(const tvec2<T>& a, const tvec2<T>& b) { return !(a == b); }

@@ -190,6 +190,31 @@ def test_droplets_match_live_reference(oracle, device_reference, seed):
     assert np.array_equal(bits(got), bits(want))
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_erosion_kernel_spawn_matches_live_reference(oracle, device_reference, seed):
+    """The reference's hydraulicErosionKERNEL, spawn included: fed the oracle's Philox uniforms in
+    place of curand's (the oracle's starts for a 1x1 neighbourhood of 2^2 chunks are the uniforms
+    themselves: u * 1 + 0), it gives the map of the oracle's FP32 serial erosion from the oracle's
+    starts for the real neighbourhood, bit for bit: same spawn range, same arithmetic."""
+    rng = np.random.default_rng(500 + seed)
+    ms = (int(rng.integers(12, 40)), int(rng.integers(12, 40)))
+    nn = (3, 3) if seed < 2 else (5, 3)
+    count = int(rng.integers(500, 4000))
+    s = helpers.raindrop_dict(count, radius=int(rng.integers(1, 5)), lifetime=int(rng.integers(10, 60)))
+    total = (ms[0] * nn[0], ms[1] * nn[1])
+    y, x = np.mgrid[0:total[1], 0:total[0]]
+    h = (0.5 + 0.3 * np.sin(x / rng.uniform(4, 12)) * np.cos(y / rng.uniform(4, 12))
+         + 0.05 * rng.random(x.shape)).astype(np.float32)
+    uniforms = oracle.droplet_starts(count, seed, 0, (2, 2), (1, 1))
+    assert uniforms.min() > 0.0 and uniforms.max() <= 1.0
+    starts = oracle.droplet_starts(count, seed, 0, ms, nn)
+    idx, w = oracle.brush(total[0], s["ErosionBrushRadius"])
+    want = device_reference.erosion_kernel(h, ms, nn, s, uniforms, idx, w)
+    got, _, _ = oracle.erode(h, s, starts, idx, w, fp64=False)
+    assert not np.array_equal(want, h)
+    assert np.array_equal(bits(got), bits(want))
+
+
 def test_brush_and_format_match_live_reference(oracle, device_reference):
     for dim_x in (7, 64, 513, 4096):
         for radius in range(1, 16):
