@@ -34,7 +34,7 @@ constexpr uint32_t kErodeBlock = 128u;
 // the same cell before either update lands can take it below zero; the
 // reference's min() then returns the negative height, so each droplet that
 // read it adds its magnitude back, and with three or more such readers the
-// magnitude grows every round: measured on 64^2 chunks of multi-biome
+// magnitude grows with every such exchange: measured on 64^2 chunks of multi-biome
 // terrain, 2.7 to 3 droplets per pixel with brush radius 3 drove heights to
 // -10^5 and beyond in some runs.  With the clamp a negative cell is left to
 // the deposits, and no feedback remains.
