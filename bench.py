@@ -219,7 +219,9 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample": "1 eroded chunk per step", "impl": "CPU oracle restatement "
-                       "of the reference algorithm (filter, noise, serial erosion)"},
+                       "of the reference algorithm (filter, noise, serial FP32 erosion), each equal bit for bit to "
+                       "the reference's own code compiled for the host (filter sources; noise, generator script "
+                       "and droplet device code)"},
             "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": "port",
                              "sample": "1 eroded chunk per step"},
             "e2e": {"value": value, "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
