@@ -369,9 +369,16 @@ void put2(T* out, const V& v) {
  * world units.  Arguments the reference leaves undefined (zero sizes, int32
  * overflow, a non-finite position) throw STPNumericDomainError. */
 struct STPChunk {
+#ifdef GLM_VERSION
+	// glm included before this header: the reference's own result types
+	using ivec2 = glm::ivec2;
+	using uvec2 = glm::uvec2;
+	using dvec2 = glm::dvec2;
+#else
 	using ivec2 = detail::vec2_of<int32_t>;
 	using uvec2 = detail::vec2_of<uint32_t>;
 	using dvec2 = detail::vec2_of<double>;
+#endif
 	using STPChunkNeighbourOffset = std::vector<ivec2>;
 
 	template<class P, class U, class D>

@@ -4,6 +4,11 @@
 #include <cmath>
 #include <cstddef>
 
+// glm defines its version here; code that adapts to glm tests this macro
+#ifndef GLM_VERSION
+#define GLM_VERSION 0
+#endif
+
 namespace glm {
 
 template<typename T> struct tvec2 {

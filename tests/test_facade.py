@@ -28,3 +28,31 @@ def test_facade_error_paths_and_permutation(facade_binary):
 def test_facade_reference_scenarios(facade_binary):
     r = subprocess.run([facade_binary], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+REFERENCE_CHUNK_TEST = os.path.join(os.environ.get("STP_REFERENCE_ROOT", "/root/reference"), "SuperTest+",
+                                     "SuperTerrain+", "STPTest2DChunk.cpp")
+
+
+def test_reference_chunk_scenario_compiles_against_the_facade(tmp_path, stpgb):
+    """The reference's own STPChunk utility scenario (SuperTest+/SuperTerrain+/STPTest2DChunk.cpp, the
+    part before its chunk-storage tests, copied unchanged into a scratch folder) compiles against
+    the façade through the compatibility headers in tests/cpp/compat, with glm result types, and
+    passes.  Skips where the reference tree is absent."""
+    if not os.path.exists(REFERENCE_CHUNK_TEST):
+        pytest.skip("reference tree not present")
+    from superterrainplus_gb300 import _capi
+    with open(REFERENCE_CHUNK_TEST) as f:
+        text = f.read()
+    cut = text.index("class ChunkTester")
+    src = tmp_path / "chunk_scenario.cpp"
+    src.write_text(text[:cut])
+    libdir = os.path.dirname(_capi.LIB_PATH)
+    exe = str(tmp_path / "chunk_scenario")
+    subprocess.check_call(["g++", "-std=c++20", "-O1", "-DSTPGB_CATCH_MAIN",
+                           "-I" + os.path.join(ROOT, "tests", "cpp", "compat"), "-I" + os.path.join(ROOT, "include"),
+                           "-I" + os.path.join(ROOT, "oracle", "refshim"), str(src), "-L" + libdir, "-lstpgb",
+                           "-Wl,-rpath," + libdir, "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "1 scenarios, 0 failed checks" in r.stdout
