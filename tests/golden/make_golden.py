@@ -27,6 +27,8 @@ Fixtures:
                        another (STPRainDrop), the demo's splatmap script with
                        the rule lookups, erosion brushes and the format kernel,
                        with their inputs
+  device_digests.json  SHA-256 of that build's production-size outputs (a 512^2
+                       two-biome chunk, 600,000 droplets on a 1536^2 map)
 
 `python tests/golden/make_golden.py layers` rewrites only the layer fixtures,
 `python tests/golden/make_golden.py device` only device_reference.npz.
@@ -217,6 +219,10 @@ def two_id_samplemap(total, cell, seed):
     return np.where(((x + 3 * seed) // cell[0] + (y + 5 * seed) // cell[1]) % 2 == 0, 0, 1).astype(np.uint16)
 
 
+def float_digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+
 def make_device(orc):
     dev = DeviceReference()
     out = {}
@@ -285,6 +291,24 @@ def make_device(orc):
         out[f"s{i}_gradient_rules"] = np.array(gra, np.float64).reshape(-1, 6)
         out[f"s{i}_regions"] = dev.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
     out["splat_count"] = np.array(2)
+    # production size, stored as SHA-256 digests of the float32 bits: a 512^2 chunk of the two-biome
+    # script (filter radius 32 over its 3x3 neighbourhood), and 600,000 droplets (brush 5,
+    # lifetime 50) on a 1536^2 merged map
+    rc, perm, grad = orc.permutation(*DEVICE_PERMS[0])
+    sm = two_id_samplemap((1536, 1536), (97, 131), 4)
+    rc, offsets, bins = orc.shf(sm, (512, 512), (3, 3), 32)
+    assert rc == 0
+    hm = dev.multibiome(offsets, bins, table, perm, grad, (512, 512), (-1536.0, 2560.5))
+    h = erosion_input(1536, 5).astype(np.float32)
+    s = raindrop_setting(600000, 5, 50, 0.05)
+    starts = orc.droplet_starts(600000, 5, 0, (512, 512), (3, 3))
+    idx, w = dev.brush(1536, 5)
+    eroded = dev.erode(h, s, starts, idx, w)
+    with open(os.path.join(HERE, "device_digests.json"), "w") as f:
+        json.dump({"multibiome_512": {"samplemap_cell": [97, 131], "samplemap_seed": 4, "radius": 32,
+                                      "offset": [-1536.0, 2560.5], "sha256": float_digest(hm)},
+                   "erosion_1536": {"input_seed": 5, "droplets": 600000, "brush": 5, "lifetime": 50,
+                                    "inertia": 0.05, "start_seed": 5, "sha256": float_digest(eroded)}}, f, indent=1)
     brushes = []
     for dim_x in (300, 1000):
         for radius in range(1, 11):

@@ -248,3 +248,35 @@ def test_splatmap_matches_live_reference(oracle, device_reference, seed):
     want = device_reference.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
     got, _, _ = oracle.splatmap(bm, hm, chunks, (S, S), alt, gra, perm, grad)
     assert np.array_equal(got, want)
+
+
+def test_production_size_outputs_match_reference_digests(oracle):
+    """A 512^2 chunk of the two-biome script (filter radius 32) and 600,000 droplets (brush 5,
+    lifetime 50) on a 1536^2 merged map: the oracle reproduces the SHA-256 of the reference
+    build's float32 outputs (tests/golden/device_digests.json)."""
+    import hashlib
+    import json
+    import sys
+    sys.path.insert(0, helpers.GOLDEN)
+    import make_golden as g
+    with open(os.path.join(helpers.GOLDEN, "device_digests.json")) as f:
+        want = json.load(f)
+
+    def digest(a):
+        return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+    m = want["multibiome_512"]
+    rc, perm, grad = oracle.permutation(*g.DEVICE_PERMS[0])
+    sm = g.two_id_samplemap((1536, 1536), tuple(m["samplemap_cell"]), m["samplemap_seed"])
+    rc, offsets, bins = oracle.shf(sm, (512, 512), (3, 3), m["radius"])
+    assert rc == 0
+    table = np.array(g.TWO_BIOMES, g.BIOME_DTYPE)
+    assert digest(oracle.multibiome(offsets, bins, table, perm, grad, (512, 512), tuple(m["offset"]),
+                                    threads=4)) == m["sha256"]
+    e = want["erosion_1536"]
+    h = g.erosion_input(1536, e["input_seed"]).astype(np.float32)
+    s = g.raindrop_setting(e["droplets"], e["brush"], e["lifetime"], e["inertia"])
+    starts = oracle.droplet_starts(e["droplets"], e["start_seed"], 0, (512, 512), (3, 3))
+    idx, w = oracle.brush(1536, e["brush"])
+    out, _, _ = oracle.erode(h, s, starts, idx, w, fp64=False)
+    assert digest(out) == e["sha256"]
