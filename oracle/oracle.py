@@ -377,3 +377,73 @@ class DeviceReference:
                                          _p(np.ascontiguousarray(brush_weight, np.float32)), len(brush_index))
         assert rc == 0
         return m
+
+
+def spawn_draws(starts, map_size, nn, guess=None):
+    """Draws in (0, 1] for the reference kernel's own spawn (u * (MapSize - 1) + (NN / 2) * MapSize,
+    STPHeightfieldKernel.cu:93-104) that give exactly `starts` (x, y interleaved) whether the
+    compiler evaluates the multiply-add in two roundings or fuses it into one: per coordinate the
+    float nearest to `guess` (default (start - offset) / (MapSize - 1)) for which both evaluations
+    land on the start.  Returns (draws, the fraction of droplets whose two draws meet that)."""
+    starts = np.ascontiguousarray(starts, np.float32)
+    count = len(starts) // 2
+    base = np.tile(np.array([map_size[0] - 1, map_size[1] - 1], np.float32), count)
+    rng = np.tile(np.array([(nn[0] // 2) * map_size[0], (nn[1] // 2) * map_size[1]], np.float32), count)
+    if guess is None:
+        guess = ((starts.astype(np.float64) - rng) / base).astype(np.float32)
+    u = np.clip(np.asarray(guess, np.float32), np.float32(2.0 ** -24), np.float32(1.0))
+    # two roundings (float32 operations); one rounding (the product and sum are exact in float64)
+    plain = lambda v: v * base + rng
+    fused = lambda v: (v.astype(np.float64) * base.astype(np.float64) + rng.astype(np.float64)).astype(np.float32)
+    both = lambda v: (plain(v) == starts) & (fused(v) == starts)
+    out = u.copy()
+    done = both(u)
+    for k in (1, -1, 2, -2, 3, -3, 4, -4, 5, -5, 6, -6):
+        cand = (u.view(np.int32) + np.int32(k)).view(np.float32)
+        ok = ~done & (cand > 0.0) & (cand <= 1.0) & both(cand)
+        out[ok] = cand[ok]
+        done |= ok
+    pair = done.reshape(-1, 2).all(axis=1)
+    return out, float(pair.mean()) if count else 1.0
+
+
+def droplet_draws(oracle, count, seed, counter_base, map_size, nn):
+    """Draws for the reference kernel's spawn that place exactly the droplets
+    oracle.droplet_starts(count, seed, counter_base, map_size, nn) places: each droplet's Philox
+    draws (the starts of a 1x1 neighbourhood of 2^2 chunks, whose spawn maps u to u), or the nearest
+    floats to them that spawn_draws accepts.  Returns (draws, fraction spawned exactly)."""
+    u = oracle.droplet_starts(count, seed, counter_base, (2, 2), (1, 1))
+    return spawn_draws(oracle.droplet_starts(count, seed, counter_base, map_size, nn), map_size, nn, guess=u)
+
+
+class ReferenceGPU:
+    """The reference's erosion kernel (hydraulicErosionKERNEL with STPRainDrop, STPHeightfieldKernel.cu:80-108,
+    STPRainDrop.cu) compiled by nvcc for sm_103a with the reference's release flags
+    (oracle/_ref/libstpref_gpu.so, oracle/build_ref.sh).  Test infrastructure only: its run-to-run
+    spread is the erosion tolerance.  Arguments are device addresses (integers); each droplet's two
+    curand draws come from `uniforms` (2 floats per droplet in (0, 1]), so it erodes the same droplets
+    as a kernel fed the starts those draws map to."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_ref(gpu=True)
+        if not path or not os.path.exists(path):
+            raise FileNotFoundError("reference GPU build unavailable")
+        self.lib = L = C.CDLL(path)
+        vp, u32 = C.c_void_p, C.c_uint32
+        L.ref_gpu_erosion.argtypes = [vp, u32, u32, u32, u32, vp, vp, u32, vp, vp, u32, vp]
+        L.ref_gpu_erosion.restype = C.c_int
+        L.ref_gpu_erosion_block_size.argtypes = [u32]
+        L.ref_gpu_erosion_block_size.restype = C.c_int
+
+    def erode(self, map_ptr, map_size, nn, setting, uniforms_ptr, count, brush_index_ptr, brush_weight_ptr,
+              brush_size, stream=0):
+        """One launch on the device map at `map_ptr`; synchronises `stream`."""
+        s = OrcRaindrop(**setting)
+        rc = self.lib.ref_gpu_erosion(C.c_void_p(map_ptr), map_size[0], map_size[1], nn[0], nn[1], C.byref(s),
+                                      C.c_void_p(uniforms_ptr), count, C.c_void_p(brush_index_ptr),
+                                      C.c_void_p(brush_weight_ptr), brush_size, C.c_void_p(stream))
+        if rc != 0:
+            raise RuntimeError(f"reference erosion kernel: CUDA error {rc}")
+
+    def block_size(self, brush_size):
+        return self.lib.ref_gpu_erosion_block_size(brush_size)

@@ -106,3 +106,84 @@ def raindrop_dict(count, radius=3, lifetime=30, seed=42):
     return dict(Seed=seed, RainDropCount=count, Inertia=0.05, SedimentCapacityFactor=4.0, minSedimentCapacity=0.01,
                 initWaterVolume=1.0, minWaterVolume=minv, Friction=0.1, initSpeed=1.0, ErodeSpeed=0.3,
                 DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0, ErosionBrushRadius=radius)
+
+
+# ------------------------------------------------------------------ erosion tolerance
+
+BAND_FILE = os.path.join(GOLDEN, "erosion_band.json")
+
+
+def spawn_draws(starts, map_size, nn, guess=None):
+    from oracle.oracle import spawn_draws as f
+    return f(starts, map_size, nn, guess)
+
+
+def droplet_uniforms(oracle, count, seed, counter_base, map_size, nn):
+    from oracle.oracle import droplet_draws
+    return droplet_draws(oracle, count, seed, counter_base, map_size, nn)
+
+
+def _reference_gpu():
+    try:
+        from oracle.oracle import ReferenceGPU
+        return ReferenceGPU()
+    except (FileNotFoundError, OSError):
+        return None
+
+
+def reference_band(case, oracle, h, map_size, nn, setting, seed, counter_base, ref64, runs=5):
+    """The erosion tolerance of one case: the reference's own erosion kernel (hydraulicErosionKERNEL with
+    STPRainDrop, built for sm_103a by oracle/build_ref.sh) run `runs` times on `h` with the droplets of
+    (seed, counter_base); returns (RMS of each run against the FP64 serial result `ref64`, run-to-run
+    spread = the largest RMS between two runs, source).  Where the reference build is absent, the
+    figures recorded for `case` in tests/golden/erosion_band.json by the same runs on a GB300
+    (tests/golden/make_erosion_band.py).  With STPGB_RECORD_BAND set to a file name, live figures are
+    added to that file."""
+    import json
+
+    import pytest
+    ref = _reference_gpu()
+    if ref is None:
+        rec = None
+        if os.path.exists(BAND_FILE):
+            with open(BAND_FILE) as f:
+                rec = json.load(f).get(case)
+        if rec is None:
+            pytest.skip(f"reference GPU build absent and no recorded band for {case}")
+        return rec["rms"], rec["spread"], "recorded"
+    import torch
+    count = setting["RainDropCount"]
+    idx, w = oracle.brush(h.shape[1], setting["ErosionBrushRadius"])
+    # The reference kernel copies the brush into shared memory with the block's live droplet threads
+    # only (STPRainDrop.cu:63-71): a last block with fewer live droplets than brush points would erode
+    # with unwritten brush entries, so no tolerance case may have one.
+    block = ref.block_size(len(idx))
+    assert count % block == 0 or count % block >= len(idx), \
+        f"{case}: the reference kernel's last block would hold {count % block} droplets for {len(idx)} brush points"
+    draws, exact = droplet_uniforms(oracle, count, seed, counter_base, map_size, nn)
+    u = torch.from_numpy(draws).cuda()
+    d_idx, d_w = torch.from_numpy(idx).cuda(), torch.from_numpy(w).cuda()
+    outs = []
+    for _ in range(runs):
+        d = torch.from_numpy(np.ascontiguousarray(h, np.float32).copy()).cuda()
+        torch.cuda.synchronize()
+        ref.erode(d.data_ptr(), map_size, nn, setting, u.data_ptr(), count, d_idx.data_ptr(), d_w.data_ptr(),
+                  len(idx))
+        outs.append(d.cpu().numpy().astype(np.float64))
+    # a run that left the finite range has an unbounded distance
+    dist = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2))) if np.isfinite(a).all() and np.isfinite(b).all() \
+        else float("inf")
+    rms = [dist(o, ref64) for o in outs]
+    spread = max(dist(a, b) for i, a in enumerate(outs) for b in outs[i + 1:])
+    record = os.environ.get("STPGB_RECORD_BAND")
+    if record:
+        data = {}
+        if os.path.exists(record):
+            with open(record) as f:
+                data = json.load(f)
+        data[case] = {"rms": rms, "spread": spread, "runs": runs, "block": ref.block_size(len(idx)),
+                      "droplets_spawned_exactly": exact,
+                      "finite": bool(all(np.isfinite(o).all() for o in outs))}
+        with open(record, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+    return rms, spread, "live"

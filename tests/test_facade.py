@@ -30,19 +30,27 @@ def test_facade_reference_scenarios(facade_binary):
     assert r.returncode == 0, r.stdout + r.stderr
 
 
-REFERENCE_CHUNK_TEST = os.path.join(os.environ.get("STP_REFERENCE_ROOT", "/root/reference"), "SuperTest+",
-                                     "SuperTerrain+", "STPTest2DChunk.cpp")
+def reference_chunk_test():
+    """The reference's STPTest2DChunk.cpp: in the checkout named by STP_REFERENCE_ROOT, else in the copy
+    of the reference's sources that oracle/build_ref.sh keeps in oracle/_ref/tree; None without either."""
+    rel = os.path.join("SuperTest+", "SuperTerrain+", "STPTest2DChunk.cpp")
+    root = os.environ.get("STP_REFERENCE_ROOT")
+    for base in ([root] if root else []) + [os.path.join(ROOT, "oracle", "_ref", "tree")]:
+        if os.path.exists(os.path.join(base, rel)):
+            return os.path.join(base, rel)
+    return None
 
 
 def test_reference_chunk_scenario_compiles_against_the_facade(tmp_path, stpgb):
     """The reference's own STPChunk utility scenario (SuperTest+/SuperTerrain+/STPTest2DChunk.cpp, the
     part before its chunk-storage tests, copied unchanged into a scratch folder) compiles against
     the façade through the compatibility headers in tests/cpp/compat, with glm result types, and
-    passes.  Skips where the reference tree is absent."""
-    if not os.path.exists(REFERENCE_CHUNK_TEST):
-        pytest.skip("reference tree not present")
+    passes.  Skips where the reference's sources are absent."""
+    path = reference_chunk_test()
+    if path is None:
+        pytest.skip("reference sources not present")
     from superterrainplus_gb300 import _capi
-    with open(REFERENCE_CHUNK_TEST) as f:
+    with open(path) as f:
         text = f.read()
     cut = text.index("class ChunkTester")
     src = tmp_path / "chunk_scenario.cpp"

@@ -136,11 +136,10 @@ def test_batch_with_layer_chain_biomes(stpgb, dev, oracle):
 def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
     """The headline path: four production requests (3x3 x 512^2, 8 biomes, filter radius 32, 600,000
     droplets, brush 4, lifetime 50) through the autotuned graph, whatever erosion variant and job
-    interleaving the tuner settles on.  Request 0's eroded neighbourhood stays within the reference
-    kernel's band around the FP64 serial result (the one-lane kernel run five times on the same map
-    and starts: its worst RMS plus its run-to-run spread)."""
-    import torch
-    from test_gpu_erosion import erode_runs, rms
+    interleaving the tuner settles on.  Request 0's eroded neighbourhood stays within the band of the
+    reference's own erosion kernel built for sm_103a around the FP64 serial result (five runs on the
+    same map with the same droplets: its worst RMS plus its run-to-run spread)."""
+    from test_gpu_erosion import rms
     S, count = 512, 600000
     reqs = [dict(MapSize=S, ChunkX=4 * n, ChunkY=0, InterpolationRadius=32, DropletCount=count, BrushRadius=4,
                  Lifetime=50) for n in range(4)]
@@ -162,11 +161,11 @@ def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
     s = helpers.raindrop_dict(count, radius=4, lifetime=50, seed=42)
     idx, w = oracle.brush(3 * S, 4)
     h0 = before[0]
+    # request 0 (chunk 0, 0) draws its droplets from counter 0 of the batch's seed
+    assert np.array_equal(starts[0], oracle.droplet_starts(count, 42, 0, (S, S), (3, 3)))
     ref, _, _ = oracle.erode(h0, s, starts[0], idx, w, fp64=True)
-    ref_runs = erode_runs(dev, stpgb, h0, (S, S), (3, 3), s, starts[0], 5, lanes=1, pointwise=True)
-    ref_rms = [rms(r, ref) for r, _ in ref_runs]
-    spread = max(rms(a, c) for i, (a, _) in enumerate(ref_runs) for c, _ in ref_runs[i + 1:])
+    ref_rms, spread, source = helpers.reference_band("production-batch-512", oracle, h0, (S, S), (3, 3), s, 42, 0, ref)
     got = rms(after[0].astype(np.float64), ref)
-    print(f"production batch ({b.tuning()[0]}): RMS {got:.3g}; reference kernel {min(ref_rms):.3g}..{max(ref_rms):.3g}, "
-          f"spread {spread:.3g}")
+    print(f"production batch ({b.tuning()[0]}): RMS {got:.3g}; reference GPU build ({source}) "
+          f"{min(ref_rms):.3g}..{max(ref_rms):.3g}, spread {spread:.3g}")
     assert got <= max(ref_rms) + spread
