@@ -15,9 +15,11 @@ chunks (default 16) with inputs (biome regions, droplet starts) resident in
 HBM.  `value` = eroded chunks per second of the batched path (one CUDA graph
 of batched launches).  The plain per-chunk call sequence on the same data
 and the end-to-end rate through the C ABI with host buffers are reported
-beside it.  `--impl reference` times the reference algorithm on the host
-cores (the CPU oracle restatement; the reference's own build only exists on
-x86 development machines).
+beside it.  `--impl reference` times the path on the host cores through the
+reference's own CPU code where it has one (its filter, built for the host by
+oracle/build_ref.sh) and the CPU restatement elsewhere (noise, erosion,
+format: the reference runs them on the GPU only), without loading the
+library under test.
 """
 import argparse
 import json
@@ -61,12 +63,7 @@ def parse():
 
 
 def raindrop(m, count):
-    evap = 0.01
-    return m.RaindropSetting(Seed=SEED, RainDropCount=count, Inertia=0.05, SedimentCapacityFactor=4.0,
-                             minSedimentCapacity=0.01, initWaterVolume=1.0,
-                             minWaterVolume=m.lifetime_min_water_volume(1.0, evap, LIFETIME), Friction=0.1,
-                             initSpeed=1.0, ErodeSpeed=0.3, DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0,
-                             ErosionBrushRadius=BRUSH)
+    return m.RaindropSetting(**raindrop_dict(count))
 
 
 def biome_table(np, dtype):
@@ -96,6 +93,11 @@ EROSION_DRAM_BYTES_PER_REQUEST = 7.00e6 + 2.50e6
 def erosion_traffic(requests_per_launch):
     """DRAM bytes per erosion launch of `requests_per_launch` production requests."""
     return EROSION_DRAM_BYTES_PER_REQUEST * requests_per_launch
+
+
+def log(msg):
+    """Progress of the run on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
 def max_over_ranks(value, dist, device):
@@ -171,38 +173,83 @@ class ClockSampler:
 # ------------------------------------------------------------ CPU leg
 
 
-def cpu_eroded_chunk(threads, droplets=DROPLETS):
-    """One eroded chunk of the workload on the host cores with the oracle restatement:
-    9 filters (threaded), 9 noise chunks (rows threaded), serial FP32 erosion.
-    Returns (seconds, threads used, sample description)."""
+def raindrop_dict(count):
+    """The workload's droplet settings; the lifetime is expressed through minWaterVolume: the next
+    float above the volume left after LIFETIME evaporation steps in float32."""
+    import numpy as np
+    evap = 0.01
+    v = np.float32(1.0)
+    for _ in range(LIFETIME):
+        v = np.float32(v * np.float32(1.0 - np.float32(evap)))
+    return dict(Seed=SEED, RainDropCount=count, Inertia=0.05, SedimentCapacityFactor=4.0, minSedimentCapacity=0.01,
+                initWaterVolume=1.0, minWaterVolume=float(np.nextafter(v, np.float32(np.inf))), Friction=0.1,
+                initSpeed=1.0, ErodeSpeed=0.3, DepositSpeed=0.3, EvaporateSpeed=evap, Gravity=4.0,
+                ErosionBrushRadius=BRUSH)
+
+
+def reference_eroded_chunk(threads, droplets=DROPLETS):
+    """One eroded chunk of the workload on the host cores, each stage through the reference's own CPU
+    code where it has one:
+      * filter: the reference's STPSingleHistogramFilter built for this host by oracle/build_ref.sh,
+        with the shipped 4-thread Parallel buffer (STPSingleHistogramFilter.cpp:36, chosen by the demo
+        for chunks of 100,000 pixels and more), the nine calls shared out over threads // 4 workers,
+        as the reference's generator workers call one filter concurrently;
+      * noise, erosion, format: the reference runs these on the GPU only; the CPU restatement of the
+        multi-biome generator script (rows split over the threads), the serial FP32 droplet loop and
+        the format loop stand in.  Each equals the reference's own device code run on the host bit
+        for bit (the erosion on this very workload: 600,000 droplets on the 1536^2 map).
+    Without the reference build the filter is the restatement too.  Nothing here loads the library
+    under test.  Returns (seconds, threads, kind, sample, seconds per stage, kind per stage)."""
     import concurrent.futures as cf
 
     import numpy as np
 
-    from oracle.oracle import BIOME_DTYPE, Oracle
-    import superterrainplus_gb300 as m
+    from oracle.oracle import BIOME_DTYPE, Oracle, Reference
     orc = Oracle()
+    try:
+        ref = Reference()
+    except (FileNotFoundError, OSError):
+        ref = None
     S = MAP
     region = orc.voronoi(5 * S, 5 * S, (-2 * S, -2 * S), VORONOI_CELL, BIOMES, SEED)
     table = biome_table(np, BIOME_DTYPE)
-    rc, perm, grad = orc.permutation(*SIMPLEX)
-    rd = raindrop(m, droplets).as_dict()
+    rc, perm, grad = (ref or orc).permutation(*SIMPLEX)
+    rd = raindrop_dict(droplets)
     starts = orc.droplet_starts(droplets, SEED, 0, (S, S), (3, 3))
     idx, w = orc.brush(3 * S, BRUSH)
-    t0 = time.perf_counter()
     subs = [np.ascontiguousarray(region[(c // 3) * S:(c // 3) * S + 3 * S, (c % 3) * S:(c % 3) * S + 3 * S])
             for c in range(9)]
-    with cf.ThreadPoolExecutor(max_workers=min(threads, 9)) as ex:
-        hists = list(ex.map(lambda a: orc.shf(a, (S, S), (3, 3), RADIUS), subs))
+    t = [time.perf_counter()]
+    if ref:
+        with cf.ThreadPoolExecutor(max_workers=max(1, min(9, threads // 4))) as ex:
+            hists = list(ex.map(lambda a: ref.shf(a, (S, S), (3, 3), RADIUS, parallel=True, capacity=8 * S * S),
+                                subs))
+    else:
+        with cf.ThreadPoolExecutor(max_workers=min(threads, 9)) as ex:
+            hists = list(ex.map(lambda a: orc.shf(a, (S, S), (3, 3), RADIUS), subs))
+    t.append(time.perf_counter())
     merged = np.zeros((3 * S, 3 * S), np.float32)
     for c, (rc, off, bins) in enumerate(hists):
         h = orc.multibiome(off, bins, table, perm, grad, (S, S), (float((c % 3 - 1) * S), float((c // 3 - 1) * S)),
                            threads=threads)
         merged[(c // 3) * S:(c // 3 + 1) * S, (c % 3) * S:(c % 3 + 1) * S] = h
+    t.append(time.perf_counter())
     orc.erode(merged, rd, starts, idx, w, fp64=False)
+    t.append(time.perf_counter())
     orc.format(merged)
-    dt = time.perf_counter() - t0
-    return dt, threads, f"1 eroded chunk of the workload ({droplets} droplets), oracle port, {threads} threads"
+    t.append(time.perf_counter())
+    stages = dict(zip(["single_histogram_filter", "multibiome_noise", "hydraulic_erosion", "format"],
+                      [t[k + 1] - t[k] for k in range(4)]))
+    kinds = {k: "port" for k in stages}
+    if ref:
+        kinds["single_histogram_filter"] = "reference"
+        sample = (f"1 eroded chunk of the workload ({droplets} droplets): the reference's own filter built for the "
+                  f"host (4-thread buffer, {max(1, min(9, threads // 4))} concurrent calls); noise, serial FP32 "
+                  f"erosion and format through the CPU restatement (the reference has no CPU code for them), "
+                  f"{threads} threads")
+    else:
+        sample = f"1 eroded chunk of the workload ({droplets} droplets), CPU restatement, {threads} threads"
+    return t[-1] - t[0], threads, "reference" if ref else "port", sample, stages, kinds
 
 
 def run_reference(args):
@@ -211,19 +258,20 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_eroded_chunk(threads)
-    times = [cpu_eroded_chunk(threads)[0] for _ in range(args.steps)]
-    total = sum(times)
+        reference_eroded_chunk(threads)
+    runs = [reference_eroded_chunk(threads) for _ in range(args.steps)]
+    total = sum(r[0] for r in runs)
+    kind, sample = runs[0][2], runs[0][3]
     value = args.steps / total
+    stages = {k: statistics.median(r[4][k] for r in runs) * 1000.0 for k in runs[0][4]}
+    kinds = runs[0][5]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": "1 eroded chunk per step", "impl": "CPU oracle restatement "
-                       "of the reference algorithm (filter, noise, serial FP32 erosion), each equal bit for bit to "
-                       "the reference's own code compiled for the host (filter sources; noise, generator script "
-                       "and droplet device code)"},
-            "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": "port",
-                             "sample": "1 eroded chunk per step"},
+            "config": {"workload": WORKLOAD, "sample": "1 eroded chunk per step", "impl": sample},
+            "stage_ms": stages, "stage_kind": kinds,
+            "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": kind,
+                             "sample": "1 eroded chunk per step", "stage_kind": kinds},
             "e2e": {"value": value, "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -251,6 +299,7 @@ def run_ours(args):
     table = biome_table(np, m.BIOME_DTYPE)
     base = raindrop(m, DROPLETS)
     simplex = m.SimplexSetting(*SIMPLEX)
+    log("production batch: create, synthesize, tune")
     batch = m.Batch(reqs, base, simplex, table, graph=True)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
@@ -265,6 +314,7 @@ def run_ours(args):
         if dist:
             dist.barrier()
 
+    log("production batch: warm-up and timed steps")
     for _ in range(max(args.warmup, 3)):
         batch.run(sh)
     barrier()
@@ -303,6 +353,7 @@ def run_ours(args):
     brush_size = len(m.erosion_brush(3 * MAP, BRUSH)[0])
 
     # plain per-chunk call sequence on the same resident data
+    log("plain per-chunk calls")
     batch.run_plain(sh)
     t0 = time.perf_counter()
     batch.run_plain(sh)
@@ -310,6 +361,7 @@ def run_ours(args):
     plain_value = B / plain_s
 
     # end to end through the C ABI with host buffers: inputs H2D, outputs D2H, every step
+    log("end to end")
     S = MAP
     pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
     # host inputs of the same kind (Voronoi regions, central-chunk starts), made by the library's
@@ -400,6 +452,7 @@ def run_ours(args):
 
     serving = None
     if rank == 0 and args.serve_requests > 0:
+        log("serving")
         serving = serve_section(m, np, torch, args.serve_requests)
         serving["at_120_per_s"] = serve_section(m, np, torch, args.serve_requests, rate=120.0, plain=False)
         serving["layer_chain_biomes"] = serve_section(m, np, torch, args.serve_requests, layer=True, plain=False)
@@ -407,15 +460,21 @@ def run_ours(args):
     biomemap = splatmap = large = uneven = None
     if rank == 0:
         if not args.no_large_field:
+            log("large field")
             large = large_field_section(m, np, torch)
+            log("uneven batch")
             uneven = uneven_batch_section(m, np, torch)
+        log("biome layer chain")
         biomemap = biomemap_section(m, np, torch, B, cpu=world == 1 and not args.no_cpu_baseline)
+        log("splatmap")
         splatmap = splatmap_section(m, np, torch, batch, reqs, cpu=world == 1 and not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        dt, cores, sample = cpu_eroded_chunk(os.cpu_count() or 1)
-        cpu = {"value": 1.0 / dt, "unit": "chunks/s", "cores": cores, "kind": "port", "sample": sample}
+        log("CPU baseline")
+        dt, cores, kind, sample, stages, kinds = reference_eroded_chunk(os.cpu_count() or 1)
+        cpu = {"value": 1.0 / dt, "unit": "chunks/s", "cores": cores, "kind": kind, "sample": sample,
+               "stage_ms": {k: 1000.0 * v for k, v in stages.items()}, "stage_kind": kinds}
 
     if rank == 0:
         cs = clocks.summary()
