@@ -1311,15 +1311,9 @@ double erosion_in_flight(const uint32_t count, const double area) {
 }
 
 uint32_t erosion_resident_droplets(const uint32_t lanes, const uint32_t dpg) {
-	// SM count of the current device (a property query, no stream work)
-	int dev = 0, sms = 0;
-	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess
-		|| sms <= 0) {
-		cudaGetLastError();
-		sms = 152; // GB300
-	}
+	const uint32_t sms = current_sm_count();
 	const uint32_t blocks = dpg == 2u ? 8u : 9u; // the row kernel's launch bounds
-	return static_cast<uint32_t>(sms) * blocks * kErodeBlock / std::max(lanes, 1u) * std::max(dpg, 1u);
+	return sms * blocks * kErodeBlock / std::max(lanes, 1u) * std::max(dpg, 1u);
 }
 
 uint32_t erosion_coop_interleave(const ErosionJob* jobs, const uint32_t njobs) {

@@ -35,6 +35,16 @@ inline cudaStream_t as_stream(void* s) {
 	return static_cast<cudaStream_t>(s);
 }
 
+// SM count of the current device, queried once per device (152 if the query fails).
+uint32_t current_sm_count();
+
+// Keys of one-time per-device set-up steps (function attributes are per device).
+enum : unsigned { SETUP_SHF_SMEM = 0u };
+
+// Runs `setup` on the current device the first time `key` is asked for there and it succeeds;
+// serialised under a lock, so concurrent first calls from several host threads set up once.
+int once_per_device(unsigned key, int (*setup)());
+
 } // namespace stpgb
 
 #define STPGB_CUDA_TRY(expr)                                   \

@@ -44,7 +44,8 @@ namespace {
 
 constexpr uint32_t kLayerThreads = 256u;
 constexpr float kVoronoiGap = 1.0f / 131072.0f;
-constexpr uint32_t kTargetBlocks = 2u * 152u;
+// blocks a layer launch aims for per SM of the device
+constexpr uint32_t kTargetBlocksPerSM = 2u;
 constexpr size_t kSmemLimit = 48u * 1024u;
 constexpr int64_t kCoordLimit = int64_t(1) << 30;
 
@@ -524,13 +525,14 @@ int layer_chain_prepare(const stpgb_layer* chain, const uint32_t count, const ui
 }
 
 uint32_t layer_tile_for(const uint64_t pixels) {
-	if (pixels >= uint64_t(kTargetBlocks) * 128u * 128u) {
+	const uint64_t target_blocks = uint64_t { kTargetBlocksPerSM } * current_sm_count();
+	if (pixels >= target_blocks * 128u * 128u) {
 		return 128u;
 	}
-	if (pixels >= uint64_t(kTargetBlocks) * 64u * 64u) {
+	if (pixels >= target_blocks * 64u * 64u) {
 		return 64u;
 	}
-	if (pixels >= uint64_t(kTargetBlocks) * 32u * 32u) {
+	if (pixels >= target_blocks * 32u * 32u) {
 		return 32u;
 	}
 	return 16u;

@@ -37,8 +37,8 @@ namespace {
 constexpr uint32_t kVBlock = 64u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
-// threads the segmented passes aim for: 1024 per SM of the 152
-constexpr uint64_t kShfTargetThreads = 152u * 1024u;
+// threads per SM the segmented passes aim for
+constexpr uint64_t kShfThreadsPerSM = 1024u;
 
 size_t align256(size_t v) {
 	return (v + 255u) & ~static_cast<size_t>(255u);
@@ -404,7 +404,13 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 	}
 }
 
-bool g_attr_set = false;
+// the passes' dynamic shared memory above the default 48 KB (a per-device attribute)
+int shf_set_smem_attributes() {
+	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_vertical, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+	return STPGB_OK;
+}
 
 } // namespace
 
@@ -432,12 +438,8 @@ ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
 
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
 	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream) {
-	if (!g_attr_set) {
-		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_vertical, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-		STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_horizontal<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-		g_attr_set = true;
-	}
+	STPGB_TRY(once_per_device(SETUP_SHF_SMEM, shf_set_smem_attributes));
+	const uint64_t target_threads = uint64_t { current_sm_count() } * kShfThreadsPerSM;
 	// Segments per column / row: enough threads to fill the GPU when few
 	// chunks are filtered at once, none while the launch already has a
 	// quarter of that (a segment start sweeps back to the start of every run:
@@ -445,7 +447,7 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	// slower; on one chunk, 16 make it several times faster).
 	const uint64_t ncols = static_cast<uint64_t>(max_W) + 2u * max_r;
 	auto segments = [&](const uint64_t lanes, const uint32_t len) {
-		const uint64_t want = (kShfTargetThreads + lanes * njobs - 1u) / (lanes * njobs);
+		const uint64_t want = (target_threads + lanes * njobs - 1u) / (lanes * njobs);
 		if (want < 4u) {
 			return 1u;
 		}

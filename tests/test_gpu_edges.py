@@ -98,3 +98,29 @@ def test_smallest_batch_request(stpgb, oracle):
     t0 = before[0].astype(np.float64).sum()
     assert abs((t0 - after[0].astype(np.float64).sum()) - res[0]) <= 1e-5 * t0
     assert np.array_equal(fixed[0], oracle.format(after[0]))
+
+
+def test_droplets_that_never_dry_stop_at_the_step_cap(dev, stpgb):
+    """EvaporateSpeed 0 is a legal setting (the reference accepts [0, 1], STPEnvironment.cpp:62), and
+    with it the reference's loop (while Volume >= minWaterVolume) never ends for a droplet that stays
+    on the map.  Four droplets in a steep bowl whose lowest point lies inside a cell (no inertia, so
+    each step turns them back towards it; no erosion or deposition, so the bowl keeps its shape) roll
+    about its bottom for ever; the library's loop stops each at 2^20 steps and the call reports
+    STPGB_ETIMEOUT instead of hanging.  The map is unchanged."""
+    import torch
+    n = 64
+    y, x = np.mgrid[0:n, 0:n].astype(np.float32)
+    h = (((x - 31.3) ** 2 + (y - 31.7) ** 2) * 0.01).astype(np.float32)
+    s = helpers.raindrop_dict(4, radius=2, lifetime=30)
+    s.update(EvaporateSpeed=0.0, minWaterVolume=0.5, Inertia=0.0, ErodeSpeed=0.0, DepositSpeed=0.0)
+    starts = np.array([20.3, 22.7, 41.2, 25.1, 30.6, 44.4, 27.9, 31.2], np.float32)
+    d = torch.from_numpy(h.copy()).cuda()
+    st = torch.from_numpy(starts).cuda()
+    idx, w = stpgb.erosion_brush(n, 2)
+    res = torch.zeros(1, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dev.hydraulic_erosion(d, (n, n), (1, 1), stpgb.RaindropSetting(**s), st, 4, torch.from_numpy(idx).cuda(),
+                          torch.from_numpy(w).cuda(), res, status)
+    with pytest.raises(stpgb.STPTimeout):
+        dev.status_check(status)
+    assert np.array_equal(d.cpu().numpy(), h)

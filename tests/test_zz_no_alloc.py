@@ -10,7 +10,10 @@ process as well.
 
 Checks, through the C ABI: two calls in a row give output bit-identical to
 stpgb_shf_filter with a caller workspace (the filter's tolerance is
-exactness), and a chunk whose scratch exceeds the array is refused."""
+exactness), also when consecutive calls lay the shared scratch out
+differently; after the first call on the device, calls leave the device's
+free memory unchanged; and a chunk whose scratch exceeds the array is
+refused."""
 import ctypes as C
 
 import numpy as np
@@ -19,12 +22,20 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _filter(m, t, info, radius, max_items, cap, noalloc):
+def _outputs(info, cap):
     import torch
     npix = info.MapSize[0] * info.MapSize[1]
-    offsets = torch.full((npix + 1,), -1, dtype=torch.int32, device="cuda")
-    bins = torch.full((cap,), -1, dtype=torch.int64, device="cuda")
-    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    return (torch.full((npix + 1,), -1, dtype=torch.int32, device="cuda"),
+            torch.full((cap,), -1, dtype=torch.int64, device="cuda"), torch.full((1,), -1, dtype=torch.int32, device="cuda"))
+
+
+def _filter(m, t, info, radius, max_items, cap, noalloc, outputs=None):
+    import torch
+    offsets, bins, status = outputs if outputs is not None else _outputs(info, cap)
+    if outputs is not None:
+        offsets.fill_(-1)
+        bins.fill_(-1)
+        status.fill_(-1)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     L = m.lib()
     if noalloc:
@@ -80,3 +91,32 @@ def test_noalloc_filter_refuses_oversized_scratch():
     t = torch.zeros((3072, 3072), dtype=torch.int16, device="cuda")
     with pytest.raises(m.STPCapacityError):
         _filter(m, t, info, 32, 64, 1024 * 1024, noalloc=True)
+
+
+def test_noalloc_filter_allocates_nothing_and_follows_a_changed_layout():
+    """Consecutive calls on the same 3x3 x 512^2 map with max_items 8, then 13, then 8 move the
+    sub-arrays inside the shared scratch (their offsets grow with max_items); every call must still
+    equal the workspace path bit for bit, so no call may read an entry an earlier call left behind.
+    Once the first call on the device has looked up the array's address, two further calls leave
+    the device's free memory (cudaMemGetInfo) exactly where it was."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import superterrainplus_gb300 as m
+    S, radius, nb = 512, 32, 8
+    info = m.NNInfo.make((S, S), (3, 3))
+    t = torch.empty((3 * S, 3 * S), dtype=torch.int16, device="cuda")
+    m.DeviceOps().voronoi_biomemap(t, 3 * S, 3 * S, 3 * S, (-S, -S), 192, nb, 11)
+    cap = S * S * nb
+    want = {k: _filter(m, t, info, radius, k, cap, noalloc=False) for k in (8, 13)}
+    outs = _outputs(info, cap)
+    for k in (8, 13, 8):
+        off, bins = _filter(m, t, info, radius, k, cap, noalloc=True, outputs=outs)
+        assert np.array_equal(off, want[k][0]) and np.array_equal(bins, want[k][1]), f"max_items {k}"
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for k in (13, 8):
+        off, bins = _filter(m, t, info, radius, k, cap, noalloc=True, outputs=outs)
+        assert np.array_equal(off, want[k][0]) and np.array_equal(bins, want[k][1])
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
