@@ -121,6 +121,13 @@ STPGB_API const char* stpgb_last_error(void);
 /* Library version string. */
 STPGB_API const char* stpgb_version(void);
 
+/* No counterpart in the reference: a copy of `bytes` between any two host or
+ * device buffers, ordered on `stream` (cudaMemcpyAsync, the direction taken
+ * from the addresses); with `wait` nonzero the call returns after the copy.
+ * For callers that do not include the CUDA headers, such as the C++ façade's
+ * texture buffers staged in host memory. */
+STPGB_API int stpgb_copy(void* dst, const void* src, size_t bytes, void* stream, int wait);
+
 /* --------------------------------------------------- host-side tables --- */
 
 /* Validation of STPSimplexNoiseSetting
@@ -502,11 +509,69 @@ STPGB_API int stpgb_splatmap(stpgb_splat_generator* generator, const uint16_t* b
 
 typedef struct stpgb_generator stpgb_generator;
 
+/* One call of a multi-biome heightmap plugin: the arguments of
+ * STPDiversityGenerator::operator()
+ * (SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/World/Chunk/
+ * STPDiversityGenerator.hpp:14-39), whose texture buffers
+ * (STPNearestNeighbourTextureBuffer.h) become plain buffers: the chunk's
+ * heightmap to write and the merged biome neighbourhood to read, both already
+ * on the device, with the caller's host chunk arrays beside them for plugins
+ * that work on the host.  All work goes on `stream`. */
+typedef struct stpgb_diversity_call {
+	float* heightmap;                             /* device, MapSize floats, row-major: the chunk to write */
+	const uint16_t* biomemap;                     /* device, the merged DiversityNearestNeighbour region */
+	const uint16_t* const* biomemap_chunks_host;  /* the caller's host chunks, chunk i at (i % nx, i / nx) */
+	stpgb_nn_info heightmap_nn;                   /* MapSize, a 1x1 neighbourhood */
+	stpgb_nn_info biomemap_nn;                    /* MapSize, DiversityNearestNeighbour */
+	float offset_x, offset_y;                     /* the chunk's map offset in world coordinates */
+	void* stream;                                 /* cudaStream_t */
+} stpgb_diversity_call;
+
+/* The plugin's operator(): enqueues the heightmap's generation on
+ * call->stream and returns STPGB_OK, or an STPGB_* error code, which the
+ * generator returns to its caller.  Called from the thread that called
+ * stpgb_generator_generate; concurrent generate calls call it concurrently. */
+typedef int (*stpgb_diversity_fn)(void* user, const stpgb_diversity_call* call);
+
+/* STPDiversityGenerator as a C object: the function and its state. */
+typedef struct stpgb_diversity_generator {
+	stpgb_diversity_fn generate;
+	void* user;
+} stpgb_diversity_generator;
+
+/* STPHeightfieldGenerator::STPGeneratorSetup
+ * (SuperTerrain+/SuperTerrain+/Public/SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45). */
+typedef struct stpgb_generator_setup {
+	const stpgb_chunk_setting* ChunkSetting;
+	const stpgb_raindrop_setting* RainDropSetting;
+	const stpgb_diversity_generator* DiversityGenerator; /* not owned; must outlive the generator */
+} stpgb_generator_setup;
+
+/* Replaces STPHeightfieldGenerator::STPHeightfieldGenerator(const STPGeneratorSetup&)
+ * (STPHeightfieldGenerator.h:121, STPHeightfieldGenerator.cpp:115-150): validates the
+ * settings and builds the erosion brush on the device; generate() calls the
+ * setup's diversity plugin for the heightmap. */
+STPGB_API int stpgb_generator_create_setup(const stpgb_generator_setup* setup, stpgb_generator** out);
+
+/* The demo's multi-biome diversity plugin, STPBiomefieldGenerator
+ * (SuperDemo+/World/Biomes/STPBiomefieldGenerator.cpp:44-152): single
+ * histogram filter of the biome neighbourhood, then the multi-biome fractal
+ * simplex heightmap, both on the device.  stpgb_biomefield_generate is an
+ * stpgb_diversity_fn whose user pointer is the plugin object; it is
+ * thread-safe (each call takes its own scratch). */
+typedef struct stpgb_biomefield stpgb_biomefield;
+STPGB_API int stpgb_biomefield_create(const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table,
+	uint32_t biome_count, uint32_t interpolation_radius, stpgb_biomefield** out);
+STPGB_API int stpgb_biomefield_destroy(stpgb_biomefield* plugin);
+STPGB_API int stpgb_biomefield_generate(void* plugin, const stpgb_diversity_call* call);
+
 /* Replaces STPHeightfieldGenerator::STPHeightfieldGenerator
  * (SuperTerrain+/SuperTerrain+/Private/World/Chunk/STPHeightfieldGenerator.cpp:115-150)
  * together with the demo diversity plugin STPBiomefieldGenerator
  * (SuperDemo+/World/Biomes/STPBiomefieldGenerator.cpp:44-65): validates the
- * settings, builds the erosion brush and permutation on the device. */
+ * settings, builds the erosion brush and permutation on the device.  The same
+ * as stpgb_generator_create_setup with an stpgb_biomefield plugin that the
+ * generator owns. */
 STPGB_API int stpgb_generator_create(const stpgb_chunk_setting* chunk,
 	const stpgb_raindrop_setting* raindrop, const stpgb_simplex_setting* simplex,
 	const stpgb_biome_property* biome_table, uint32_t biome_count,

@@ -9,8 +9,12 @@
  *       (SuperAlgorithm+Host/STPPermutationGenerator.h:23-50)
  *   SuperTerrainPlus::STPAlgorithm::STPSingleHistogramFilter + STPFilterBuffer
  *       (SuperAlgorithm+Host/STPSingleHistogramFilter.h:36-190)
- *   SuperTerrainPlus::STPHeightfieldGenerator::generate / erode
- *       (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,145,159)
+ *   SuperTerrainPlus::STPHeightfieldGenerator(STPGeneratorSetup), generate / erode
+ *       (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,121,145,159)
+ *   SuperTerrainPlus::STPDiversityGenerator, the nearest-neighbour texture buffers
+ *       (SuperTerrain+/World/Chunk/STPDiversityGenerator.hpp:14-39,
+ *        STPNearestNeighbourTextureBuffer.h), STPDemo::STPBiomefieldGenerator
+ *       (SuperDemo+/World/Biomes/STPBiomefieldGenerator.h:26-98)
  *   SuperTerrainPlus::STPDiversity::STPBiomeFactory, STPDemo::STPLayerChainBuilder
  *       (SuperTerrain+/World/Diversity/STPBiomeFactory.h:19-63, SuperDemo+/World/Layers/STPAllLayers.h)
  *   SuperTerrainPlus::STPChunk coordinate functions
@@ -23,9 +27,12 @@
 #include "stpgb.h"
 
 #include <cstdint>
+#include <exception>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace SuperTerrainPlus {
@@ -294,49 +301,6 @@ inline stpgb_layer_biomes demo_ids() {
 
 } // namespace detail
 
-/* STPHeightfieldGenerator with the multi-biome diversity plugin
- * (STPBiomefieldGenerator) folded in: the plugin's biome table and
- * interpolation radius are constructor arguments. */
-class STPHeightfieldGenerator {
-public:
-	template<class V>
-	STPHeightfieldGenerator(const V& map_size, const V& diversity_nn, const V& erosion_nn,
-		const STPEnvironment::STPRainDropSetting& raindrop, const STPEnvironment::STPSimplexNoiseSetting& simplex,
-		const std::vector<stpgb_biome_property>& biome_table, unsigned int interpolation_radius) {
-		stpgb_chunk_setting c {};
-		c.MapSize[0] = static_cast<uint32_t>(map_size.x);
-		c.MapSize[1] = static_cast<uint32_t>(map_size.y);
-		c.DiversityNearestNeighbour[0] = static_cast<uint32_t>(diversity_nn.x);
-		c.DiversityNearestNeighbour[1] = static_cast<uint32_t>(diversity_nn.y);
-		c.ErosionNearestNeighbour[0] = static_cast<uint32_t>(erosion_nn.x);
-		c.ErosionNearestNeighbour[1] = static_cast<uint32_t>(erosion_nn.y);
-		stpgb_generator* g = nullptr;
-		detail::check(stpgb_generator_create(&c, &raindrop, &simplex, biome_table.data(),
-			static_cast<uint32_t>(biome_table.size()), interpolation_radius, &g), true);
-		Handle.reset(g);
-	}
-
-	/* STPHeightfieldGenerator::generate (STPHeightfieldGenerator.cpp:158-169) */
-	template<class V>
-	void generate(STPHeightFloat_t* heightfield, const STPSample_t* const* biomemap, const V& offset) {
-		detail::check(stpgb_generator_generate(Handle.get(), heightfield, biomemap, static_cast<float>(offset.x),
-			static_cast<float>(offset.y)));
-	}
-
-	/* STPHeightfieldGenerator::erode (STPHeightfieldGenerator.cpp:171-197) */
-	void erode(STPHeightFloat_t* const* heightfield, STPHeightFixed_t* const* heightfield_fixed) {
-		detail::check(stpgb_generator_erode(Handle.get(), heightfield, heightfield_fixed));
-	}
-
-private:
-	struct Deleter {
-		void operator()(stpgb_generator* g) const {
-			stpgb_generator_destroy(g);
-		}
-	};
-	std::unique_ptr<stpgb_generator, Deleter> Handle;
-};
-
 namespace detail {
 
 // Two-component results of STPChunk; they convert to any vector type built
@@ -363,6 +327,292 @@ void put2(T* out, const V& v) {
 }
 
 } // namespace detail
+
+#ifdef GLM_VERSION
+using STPVec2 = glm::vec2;
+using STPUVec2 = glm::uvec2;
+using STPDVec2 = glm::dvec2;
+using STPDVec3 = glm::dvec3;
+#else
+using STPVec2 = detail::vec2_of<float>;
+using STPUVec2 = detail::vec2_of<uint32_t>;
+using STPDVec2 = detail::vec2_of<double>;
+struct STPDVec3 {
+	double x, y, z;
+};
+#endif
+
+namespace STPEnvironment {
+
+/* STPChunkSetting (SuperTerrain+/Environment/STPChunkSetting.h:15-45) with
+ * validate() as STPEnvironment.cpp:17-41; the heightfield generator reads
+ * MapSize and the two nearest-neighbour counts. */
+struct STPChunkSetting {
+	STPUVec2 ChunkSize {}, MapSize {};
+	STPDVec3 ChunkOffset {};
+	STPDVec2 ChunkScale {}, MapOffset {};
+	STPUVec2 DiversityNearestNeighbour {}, ErosionNearestNeighbour {}, SplatNearestNeighbour {}, RenderDistance {};
+
+	void validate() const {
+		const auto positive = [](const STPUVec2& v) { return v.x > 0u && v.y > 0u; };
+		const auto odd = [](const STPUVec2& v) { return (v.x & 1u) && (v.y & 1u); };
+		const bool ok = positive(ChunkSize) && positive(MapSize) && ChunkScale.x > 0.0 && ChunkScale.y > 0.0
+			&& positive(DiversityNearestNeighbour) && positive(ErosionNearestNeighbour) && positive(SplatNearestNeighbour)
+			&& positive(RenderDistance) && odd(DiversityNearestNeighbour) && odd(ErosionNearestNeighbour)
+			&& odd(SplatNearestNeighbour) && odd(RenderDistance);
+		if (!ok) {
+			throw STPException::STPInvalidEnvironment("STPChunkSetting validation failed");
+		}
+	}
+};
+
+} // namespace STPEnvironment
+
+/* STPNearestNeighbourInformation (SuperTerrain+/World/Chunk/STPNearestNeighbourInformation.hpp:13-25) */
+struct STPNearestNeighbourInformation {
+	STPUVec2 MapSize, ChunkNearestNeighbour, TotalMapSize;
+};
+
+enum class STPNearestNeighbourTextureBufferMemoryMode : unsigned char {
+	ReadOnly = 0x00u,
+	WriteOnly = 0x01u,
+	ReadWrite = 0x02u
+};
+
+/* STPNearestNeighbourTextureBuffer (SuperTerrain+/World/Chunk/STPNearestNeighbourTextureBuffer.h),
+ * the buffers a diversity plugin receives.  The merged neighbourhood already
+ * lives on the device: STPMergedBuffer(DeviceMemory) hands it out directly;
+ * STPMergedBuffer(HostMemory) stages it in host memory (read from the
+ * caller's chunk arrays or the device copy) and, for a writable buffer,
+ * copies the host copy back to the device when it is destroyed, as the
+ * reference's merged buffer unpacks on destruction.  DeviceMemInfo.second is
+ * the call's stream (a cudaStream_t as void*); there is no memory pool. */
+template<typename T, STPNearestNeighbourTextureBufferMemoryMode MM>
+class STPNearestNeighbourTextureBuffer {
+public:
+	using TextureType = std::conditional_t<MM == STPNearestNeighbourTextureBufferMemoryMode::ReadOnly, const T, T>;
+	typedef std::pair<void*, void*> STPDeviceMemoryOperator;
+
+	enum class STPMemoryLocation : unsigned char {
+		HostMemory = 0x00u,
+		DeviceMemory = 0x01u
+	};
+
+	class STPMergedBuffer {
+	public:
+		using MutableT = std::remove_const_t<T>;
+
+		const STPMemoryLocation Location;
+
+		STPMergedBuffer(const STPNearestNeighbourTextureBuffer& main, const STPMemoryLocation location) :
+			Location(location), Main(main) {
+			if (location != STPMemoryLocation::HostMemory) {
+				return;
+			}
+			const STPNearestNeighbourInformation& nn = Main.NeighbourInfo;
+			Host.resize(static_cast<size_t>(nn.TotalMapSize.x) * nn.TotalMapSize.y);
+			if constexpr (MM == STPNearestNeighbourTextureBufferMemoryMode::WriteOnly) {
+				return;
+			}
+			if (Main.HostChunks) {
+				stpgb_nn_info i = Main.info();
+				detail::check(stpgb_nn_merge_host(reinterpret_cast<const void* const*>(Main.HostChunks), sizeof(T), &i,
+					Host.data()));
+			} else {
+				detail::check(stpgb_copy(Host.data(), Main.Device, Host.size() * sizeof(T), Main.DeviceMemInfo.second, 1));
+			}
+		}
+		STPMergedBuffer(const STPMergedBuffer&) = delete;
+		STPMergedBuffer& operator=(const STPMergedBuffer&) = delete;
+		~STPMergedBuffer() noexcept(false) {
+			if constexpr (MM != STPNearestNeighbourTextureBufferMemoryMode::ReadOnly) {
+				if (Location == STPMemoryLocation::HostMemory) {
+					detail::check(stpgb_copy(const_cast<MutableT*>(Main.Device), Host.data(), Host.size() * sizeof(T),
+						Main.DeviceMemInfo.second, 1));
+				}
+			}
+		}
+
+		MutableT* getHost() const noexcept {
+			return Host.empty() ? nullptr : const_cast<MutableT*>(Host.data());
+		}
+		MutableT* getDevice() const noexcept {
+			return const_cast<MutableT*>(Main.Device);
+		}
+
+	private:
+		const STPNearestNeighbourTextureBuffer& Main;
+		std::vector<MutableT> Host;
+	};
+
+	const STPNearestNeighbourInformation& NeighbourInfo;
+	const STPDeviceMemoryOperator DeviceMemInfo;
+
+	/* Made by the generator around its device buffers; `host_chunks` (may be
+	 * null) are the caller's host arrays of the neighbourhood's chunks. */
+	STPNearestNeighbourTextureBuffer(TextureType* device_merged, const T* const* host_chunks,
+		const STPNearestNeighbourInformation& info, void* stream) :
+		NeighbourInfo(info), DeviceMemInfo(nullptr, stream), Device(device_merged), HostChunks(host_chunks) {}
+	STPNearestNeighbourTextureBuffer(const STPNearestNeighbourTextureBuffer&) = delete;
+	STPNearestNeighbourTextureBuffer& operator=(const STPNearestNeighbourTextureBuffer&) = delete;
+
+private:
+	TextureType* const Device;
+	const T* const* const HostChunks;
+
+	stpgb_nn_info info() const {
+		stpgb_nn_info i {};
+		i.MapSize[0] = NeighbourInfo.MapSize.x;
+		i.MapSize[1] = NeighbourInfo.MapSize.y;
+		i.ChunkNearestNeighbour[0] = NeighbourInfo.ChunkNearestNeighbour.x;
+		i.ChunkNearestNeighbour[1] = NeighbourInfo.ChunkNearestNeighbour.y;
+		i.TotalMapSize[0] = NeighbourInfo.TotalMapSize.x;
+		i.TotalMapSize[1] = NeighbourInfo.TotalMapSize.y;
+		return i;
+	}
+};
+
+typedef STPNearestNeighbourTextureBuffer<STPHeightFloat_t, STPNearestNeighbourTextureBufferMemoryMode::WriteOnly>
+	STPNearestNeighbourHeightFloatWTextureBuffer;
+typedef STPNearestNeighbourTextureBuffer<STPHeightFloat_t, STPNearestNeighbourTextureBufferMemoryMode::ReadWrite>
+	STPNearestNeighbourHeightFloatRWTextureBuffer;
+typedef STPNearestNeighbourTextureBuffer<STPSample_t, STPNearestNeighbourTextureBufferMemoryMode::ReadOnly>
+	STPNearestNeighbourSampleRTextureBuffer;
+typedef STPNearestNeighbourTextureBuffer<STPHeightFixed_t, STPNearestNeighbourTextureBufferMemoryMode::WriteOnly>
+	STPNearestNeighbourHeightFixedWTextureBuffer;
+
+namespace detail {
+
+// The exception a diversity plugin threw, carried across the C boundary on
+// the calling thread and rethrown by the generator's caller.
+inline std::exception_ptr& plugin_exception() {
+	thread_local std::exception_ptr e;
+	return e;
+}
+
+inline STPNearestNeighbourInformation nn_of(const stpgb_nn_info& i) {
+	STPNearestNeighbourInformation n;
+	n.MapSize = STPUVec2 { i.MapSize[0], i.MapSize[1] };
+	n.ChunkNearestNeighbour = STPUVec2 { i.ChunkNearestNeighbour[0], i.ChunkNearestNeighbour[1] };
+	n.TotalMapSize = STPUVec2 { i.TotalMapSize[0], i.TotalMapSize[1] };
+	return n;
+}
+
+inline void rethrow_plugin(int rc, bool environment = false) {
+	if (rc != STPGB_OK && plugin_exception()) {
+		std::exception_ptr e = plugin_exception();
+		plugin_exception() = nullptr;
+		std::rethrow_exception(e);
+	}
+	check(rc, environment);
+}
+
+} // namespace detail
+
+/* STPDiversityGenerator (SuperTerrain+/World/Chunk/STPDiversityGenerator.hpp:14-39):
+ * the multi-biome heightmap plugin of the heightfield generator.  operator()
+ * writes one chunk's heightmap from its biome neighbourhood; an exception it
+ * throws reaches the caller of STPHeightfieldGenerator::generate. */
+class STPDiversityGenerator {
+public:
+	STPDiversityGenerator() = default;
+	virtual ~STPDiversityGenerator() = default;
+
+	virtual void operator()(const STPNearestNeighbourHeightFloatWTextureBuffer&,
+		const STPNearestNeighbourSampleRTextureBuffer&, STPVec2) = 0;
+
+	/* The plugin as an stpgb_diversity_generator for the C ABI. */
+	stpgb_diversity_generator cPlugin() noexcept {
+		return stpgb_diversity_generator { &STPDiversityGenerator::call, this };
+	}
+
+private:
+	static int call(void* user, const stpgb_diversity_call* c) noexcept {
+		try {
+			const STPNearestNeighbourInformation hnn = detail::nn_of(c->heightmap_nn), bnn = detail::nn_of(c->biomemap_nn);
+			const STPNearestNeighbourHeightFloatWTextureBuffer height(c->heightmap, nullptr, hnn, c->stream);
+			const STPNearestNeighbourSampleRTextureBuffer biome(c->biomemap, c->biomemap_chunks_host, bnn, c->stream);
+			(*static_cast<STPDiversityGenerator*>(user))(height, biome, STPVec2 { c->offset_x, c->offset_y });
+			return STPGB_OK;
+		} catch (...) {
+			detail::plugin_exception() = std::current_exception();
+			return STPGB_EINVAL;
+		}
+	}
+};
+
+
+/* STPHeightfieldGenerator (SuperTerrain+/World/Chunk/STPHeightfieldGenerator.h:35-45,121,145,159).
+ * The reference's constructor takes an STPGeneratorSetup with a diversity
+ * plugin; a second constructor folds the demo plugin in. */
+class STPHeightfieldGenerator {
+public:
+	struct STPGeneratorSetup {
+		const STPEnvironment::STPChunkSetting* ChunkSetting;
+		const STPEnvironment::STPRainDropSetting* RainDropSetting;
+		STPDiversityGenerator* DiversityGenerator;
+	};
+
+	/* STPHeightfieldGenerator(const STPGeneratorSetup&) (STPHeightfieldGenerator.cpp:115-150):
+	 * validates both settings; the plugin must outlive the generator. */
+	explicit STPHeightfieldGenerator(const STPGeneratorSetup& setup) {
+		if (!setup.ChunkSetting || !setup.RainDropSetting || !setup.DiversityGenerator) {
+			throw STPException::STPInvalidEnvironment("STPGeneratorSetup: null member");
+		}
+		setup.ChunkSetting->validate();
+		setup.RainDropSetting->validate();
+		stpgb_chunk_setting c {};
+		detail::put2(c.MapSize, setup.ChunkSetting->MapSize);
+		detail::put2(c.DiversityNearestNeighbour, setup.ChunkSetting->DiversityNearestNeighbour);
+		detail::put2(c.ErosionNearestNeighbour, setup.ChunkSetting->ErosionNearestNeighbour);
+		Plugin = setup.DiversityGenerator->cPlugin();
+		const stpgb_generator_setup cs { &c, setup.RainDropSetting, &Plugin };
+		stpgb_generator* g = nullptr;
+		detail::check(stpgb_generator_create_setup(&cs, &g), true);
+		Handle.reset(g);
+	}
+
+	/* The demo plugin folded in: its biome table and interpolation radius
+	 * are constructor arguments. */
+	template<class V>
+	STPHeightfieldGenerator(const V& map_size, const V& diversity_nn, const V& erosion_nn,
+		const STPEnvironment::STPRainDropSetting& raindrop, const STPEnvironment::STPSimplexNoiseSetting& simplex,
+		const std::vector<stpgb_biome_property>& biome_table, unsigned int interpolation_radius) {
+		stpgb_chunk_setting c {};
+		c.MapSize[0] = static_cast<uint32_t>(map_size.x);
+		c.MapSize[1] = static_cast<uint32_t>(map_size.y);
+		c.DiversityNearestNeighbour[0] = static_cast<uint32_t>(diversity_nn.x);
+		c.DiversityNearestNeighbour[1] = static_cast<uint32_t>(diversity_nn.y);
+		c.ErosionNearestNeighbour[0] = static_cast<uint32_t>(erosion_nn.x);
+		c.ErosionNearestNeighbour[1] = static_cast<uint32_t>(erosion_nn.y);
+		stpgb_generator* g = nullptr;
+		detail::check(stpgb_generator_create(&c, &raindrop, &simplex, biome_table.data(),
+			static_cast<uint32_t>(biome_table.size()), interpolation_radius, &g), true);
+		Handle.reset(g);
+	}
+
+	/* STPHeightfieldGenerator::generate (STPHeightfieldGenerator.cpp:158-169) */
+	template<class V>
+	void generate(STPHeightFloat_t* heightfield, const STPSample_t* const* biomemap, const V& offset) {
+		detail::rethrow_plugin(stpgb_generator_generate(Handle.get(), heightfield, biomemap, static_cast<float>(offset.x),
+			static_cast<float>(offset.y)));
+	}
+
+	/* STPHeightfieldGenerator::erode (STPHeightfieldGenerator.cpp:171-197) */
+	void erode(STPHeightFloat_t* const* heightfield, STPHeightFixed_t* const* heightfield_fixed) {
+		detail::check(stpgb_generator_erode(Handle.get(), heightfield, heightfield_fixed));
+	}
+
+private:
+	struct Deleter {
+		void operator()(stpgb_generator* g) const {
+			stpgb_generator_destroy(g);
+		}
+	};
+	stpgb_diversity_generator Plugin {};
+	std::unique_ptr<stpgb_generator, Deleter> Handle;
+};
+
 
 /* The static coordinate functions of STPChunk
  * (SuperTerrain+/World/Chunk/STPChunk.h:110-157): chunk coordinates are in
@@ -467,6 +717,47 @@ public:
 	template<class V>
 	STPLayerChainBuilder(const V& dimension, SuperTerrainPlus::STPSeed_t global_seed, const stpgb_layer_biomes& ids) :
 		STPBiomeFactory(dimension, global_seed, SuperTerrainPlus::detail::demo_chain(), ids) {}
+};
+
+/* The demo's multi-biome plugin STPBiomefieldGenerator
+ * (SuperDemo+/World/Biomes/STPBiomefieldGenerator.h:26-98): the single
+ * histogram filter and the multi-biome fractal simplex heightmap, on the
+ * device.  The biome table and interpolation radius are constructor
+ * arguments (the demo reads them from its ini files). */
+class STPBiomefieldGenerator : public SuperTerrainPlus::STPDiversityGenerator {
+public:
+	STPBiomefieldGenerator(const SuperTerrainPlus::STPEnvironment::STPSimplexNoiseSetting& simplex,
+		const std::vector<stpgb_biome_property>& biome_table, unsigned int interpolation_radius) {
+		stpgb_biomefield* f = nullptr;
+		SuperTerrainPlus::detail::check(stpgb_biomefield_create(&simplex, biome_table.data(), static_cast<uint32_t>(biome_table.size()),
+			interpolation_radius, &f), true);
+		Handle.reset(f);
+	}
+
+	void operator()(const SuperTerrainPlus::STPNearestNeighbourHeightFloatWTextureBuffer& heightmap_buffer,
+		const SuperTerrainPlus::STPNearestNeighbourSampleRTextureBuffer& biomemap_buffer, const SuperTerrainPlus::STPVec2 offset) override {
+		const SuperTerrainPlus::STPNearestNeighbourHeightFloatWTextureBuffer::STPMergedBuffer height(heightmap_buffer,
+			SuperTerrainPlus::STPNearestNeighbourHeightFloatWTextureBuffer::STPMemoryLocation::DeviceMemory);
+		const SuperTerrainPlus::STPNearestNeighbourSampleRTextureBuffer::STPMergedBuffer biome(biomemap_buffer,
+			SuperTerrainPlus::STPNearestNeighbourSampleRTextureBuffer::STPMemoryLocation::DeviceMemory);
+		stpgb_diversity_call c {};
+		c.heightmap = height.getDevice();
+		c.biomemap = biome.getDevice();
+		c.heightmap_nn = SuperTerrainPlus::detail::nn(heightmap_buffer.NeighbourInfo.MapSize, heightmap_buffer.NeighbourInfo.ChunkNearestNeighbour);
+		c.biomemap_nn = SuperTerrainPlus::detail::nn(biomemap_buffer.NeighbourInfo.MapSize, biomemap_buffer.NeighbourInfo.ChunkNearestNeighbour);
+		c.offset_x = static_cast<float>(offset.x);
+		c.offset_y = static_cast<float>(offset.y);
+		c.stream = heightmap_buffer.DeviceMemInfo.second;
+		SuperTerrainPlus::detail::check(stpgb_biomefield_generate(Handle.get(), &c));
+	}
+
+private:
+	struct Deleter {
+		void operator()(stpgb_biomefield* f) const {
+			stpgb_biomefield_destroy(f);
+		}
+	};
+	std::unique_ptr<stpgb_biomefield, Deleter> Handle;
 };
 
 } // namespace STPDemo

@@ -19,14 +19,14 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import (STPGB_MAX_LAYERS, AltitudeRule, BiomeProperty, ChunkSetting, GradientRule, Layer, LayerBiomes,
+from ._capi import (STPGB_EINVAL, STPGB_MAX_LAYERS, STPGB_OK, AltitudeRule, BiomeProperty, ChunkSetting, GradientRule, Layer, LayerBiomes,
                     NNInfo, Permutation, RaindropSetting, SimplexSetting, SplatChunk, STPCapacityError, STPCUDAError, STPException, STPInsufficientMemory, STPInvalidEnvironment,
                     STPNumericDomainError, STPTimeout, check, lib)
 
 __all__ = [
     "BiomeProperty", "ChunkSetting", "NNInfo", "Permutation", "RaindropSetting", "SimplexSetting",
     "STPCapacityError", "STPCUDAError", "STPException", "STPInsufficientMemory", "STPInvalidEnvironment",
-    "STPNumericDomainError", "STPTimeout", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
+    "STPNumericDomainError", "STPTimeout", "STPDiversityGenerator", "STPBiomefieldGenerator", "BIN_DTYPE", "BIOME_DTYPE", "lib", "check",
     "permutation_generate", "erosion_brush", "lifetime_min_water_volume", "STPSingleHistogramFilter",
     "STPFilterBuffer", "STPHeightfieldGenerator", "DeviceOps", "Batch", "Layer", "LayerBiomes",
     "layer_chain_demo", "STPLayerChainBuilder", "AltitudeRule", "GradientRule", "SplatChunk", "splat_rules_demo",
@@ -296,8 +296,62 @@ class STPSingleHistogramFilter:
 # ------------------------------------------------------ plain generator
 
 
+class STPDiversityGenerator:
+    """STPDiversityGenerator (SuperTerrain+/World/Chunk/STPDiversityGenerator.hpp:14-39): subclass and
+    implement __call__(heightmap, biomemap, offset, call), where `heightmap` (device address, MapSize
+    float32, row-major) is the chunk to write, `biomemap` (device address) the merged biome
+    neighbourhood, `offset` the chunk's map offset and `call` the full stpgb_diversity_call (nearest-
+    neighbour information, stream).  Work goes on call.stream; an exception fails the generate call."""
+
+    def __call__(self, heightmap, biomemap, offset, call):
+        raise NotImplementedError
+
+    def c_plugin(self):
+        """The stpgb_diversity_generator that calls this object."""
+        from ._capi import DIVERSITY_FN, DiversityGenerator
+
+        def fn(user, call):
+            c = call.contents
+            try:
+                self(c.heightmap, c.biomemap, (c.offset_x, c.offset_y), c)
+                return STPGB_OK
+            except Exception as e:  # the C boundary carries a status; the exception is kept for the caller
+                self.error = e
+                return STPGB_EINVAL
+
+        self._fn = DIVERSITY_FN(fn)
+        return DiversityGenerator(self._fn, None)
+
+
+class STPBiomefieldGenerator:
+    """The demo's multi-biome plugin STPBiomefieldGenerator (SuperDemo+/World/Biomes/
+    STPBiomefieldGenerator.cpp:44-152): single histogram filter + multi-biome fractal simplex
+    heightmap on the device (stpgb_biomefield_*)."""
+
+    def __init__(self, simplex_setting, biome_table, interpolation_radius):
+        table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
+        h = C.c_void_p()
+        check(lib().stpgb_biomefield_create(C.byref(simplex_setting), _p(table), len(table), interpolation_radius,
+                                            C.byref(h)), env_error=True)
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().stpgb_biomefield_destroy(h)
+            self._h = None
+
+    def c_plugin(self):
+        from ._capi import DIVERSITY_FN, DiversityGenerator
+        self._fn = DIVERSITY_FN(("stpgb_biomefield_generate", lib()))
+        return DiversityGenerator(self._fn, self._h)
+
+
 class STPHeightfieldGenerator:
-    """STPHeightfieldGenerator + the multi-biome diversity plugin, over host arrays."""
+    """STPHeightfieldGenerator over host arrays.  Either the reference's constructor,
+    STPHeightfieldGenerator.setup(chunk_setting, raindrop_setting, diversity_generator)
+    (STPHeightfieldGenerator.h:35-45,121), with any diversity plugin, or this constructor, which folds
+    the demo's multi-biome plugin in."""
 
     def __init__(self, chunk_setting, raindrop_setting, simplex_setting, biome_table, interpolation_radius):
         table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
@@ -308,6 +362,25 @@ class STPHeightfieldGenerator:
         self._h = h
         self.chunk = chunk_setting
         self.raindrop = raindrop_setting
+        self.plugin = None
+
+    @classmethod
+    def setup(cls, chunk_setting, raindrop_setting, diversity_generator):
+        """STPHeightfieldGenerator(const STPGeneratorSetup&): `diversity_generator` is an
+        STPDiversityGenerator subclass instance or an STPBiomefieldGenerator; it is kept alive by the
+        generator."""
+        from ._capi import GeneratorSetup
+        self = cls.__new__(cls)
+        self._h = None
+        self.plugin = diversity_generator
+        self._c_plugin = diversity_generator.c_plugin()
+        st = GeneratorSetup(C.pointer(chunk_setting), C.pointer(raindrop_setting), C.pointer(self._c_plugin))
+        h = C.c_void_p()
+        check(lib().stpgb_generator_create_setup(C.byref(st), C.byref(h)), env_error=True)
+        self._h = h
+        self.chunk = chunk_setting
+        self.raindrop = raindrop_setting
+        return self
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -320,7 +393,12 @@ class STPHeightfieldGenerator:
         arrs = [np.ascontiguousarray(b, np.uint16) for b in biomemap]
         ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
         assert heightfield.dtype == np.float32 and heightfield.flags.c_contiguous
-        check(lib().stpgb_generator_generate(self._h, _p(heightfield), ptrs, offset[0], offset[1]))
+        rc = lib().stpgb_generator_generate(self._h, _p(heightfield), ptrs, offset[0], offset[1])
+        err = getattr(self.plugin, "error", None)
+        if rc != STPGB_OK and err is not None:
+            self.plugin.error = None
+            raise err
+        check(rc)
 
     def erode(self, heightfield, heightfield_fixed, starts=None):
         """heightfield: list of float32 chunks (in/out); heightfield_fixed: list of uint16 chunks (out).

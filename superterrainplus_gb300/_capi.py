@@ -148,6 +148,24 @@ class SplatChunk(C.Structure):
                 ("ChunkMapOffsetY", f32)]
 
 
+class DiversityCall(C.Structure):
+    """stpgb_diversity_call: one call of a multi-biome heightmap plugin (STPDiversityGenerator::operator())."""
+    _fields_ = [("heightmap", vp), ("biomemap", vp), ("biomemap_chunks_host", vp), ("heightmap_nn", NNInfo),
+                ("biomemap_nn", NNInfo), ("offset_x", f32), ("offset_y", f32), ("stream", vp)]
+
+
+DIVERSITY_FN = C.CFUNCTYPE(C.c_int, vp, C.POINTER(DiversityCall))
+
+
+class DiversityGenerator(C.Structure):
+    _fields_ = [("generate", DIVERSITY_FN), ("user", vp)]
+
+
+class GeneratorSetup(C.Structure):
+    _fields_ = [("ChunkSetting", C.POINTER(ChunkSetting)), ("RainDropSetting", C.POINTER(RaindropSetting)),
+                ("DiversityGenerator", C.POINTER(DiversityGenerator))]
+
+
 STPGB_BATCH_GRAPH = 1
 STPGB_BATCH_AUTOTUNE = 2
 
@@ -195,6 +213,11 @@ PROTOTYPES = {
     "stpgb_generator_create": (C.c_int, [C.POINTER(ChunkSetting), C.POINTER(RaindropSetting),
                                          C.POINTER(SimplexSetting), vp, u32, u32, C.POINTER(vp)]),
     "stpgb_generator_destroy": (C.c_int, [vp]),
+    "stpgb_generator_create_setup": (C.c_int, [C.POINTER(GeneratorSetup), C.POINTER(vp)]),
+    "stpgb_biomefield_create": (C.c_int, [C.POINTER(SimplexSetting), vp, u32, u32, C.POINTER(vp)]),
+    "stpgb_biomefield_destroy": (C.c_int, [vp]),
+    "stpgb_biomefield_generate": (C.c_int, [vp, C.POINTER(DiversityCall)]),
+    "stpgb_copy": (C.c_int, [vp, vp, sz, vp, C.c_int]),
     "stpgb_generator_generate": (C.c_int, [vp, vp, vp, f32, f32]),
     "stpgb_generator_erode": (C.c_int, [vp, vp, vp]),
     "stpgb_generator_erode_starts": (C.c_int, [vp, vp, vp, vp, u32, C.POINTER(f64)]),

@@ -1,8 +1,9 @@
-// Plain per-chunk drop-in: the heightfield generator with the multi-biome
-// diversity plugin, over host arrays, synchronous per call like the
-// reference (SuperTerrain+/SuperTerrain+/Private/World/Chunk/
-// STPHeightfieldGenerator.cpp:115-197 with SuperDemo+/World/Biomes/
-// STPBiomefieldGenerator.cpp:79-152).
+// Plain per-chunk drop-in: the heightfield generator over host arrays,
+// synchronous per call like the reference (SuperTerrain+/SuperTerrain+/
+// Private/World/Chunk/STPHeightfieldGenerator.cpp:115-197), calling a
+// diversity plugin for each chunk's heightmap (STPDiversityGenerator.hpp:
+// 14-39), and the demo's multi-biome plugin as one such plugin
+// (SuperDemo+/World/Biomes/STPBiomefieldGenerator.cpp:44-152).
 //
 // The reference merges the neighbour chunks into a pinned host buffer and
 // then copies it to the device (STPNearestNeighbourTextureBuffer.cpp:18-113);
@@ -53,9 +54,6 @@ struct Slot {
 	cudaStream_t stream = nullptr;
 	// generate
 	DevBuf<uint16_t> biome;
-	DevBuf<unsigned char> ws;
-	DevBuf<uint32_t> offsets;
-	DevBuf<stpgb_bin> bins;
 	DevBuf<float> height;
 	// erode
 	DevBuf<float> merged;
@@ -70,6 +68,14 @@ struct Slot {
 	}
 };
 
+// Scratch of one call of the multi-biome plugin.
+struct FieldScratch {
+	DevBuf<unsigned char> ws;
+	DevBuf<uint32_t> offsets;
+	DevBuf<stpgb_bin> bins;
+	DevBuf<uint32_t> status;
+};
+
 } // namespace
 
 int shf_launch(const ShfJob*, const ShfJob&, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, cudaStream_t);
@@ -78,18 +84,41 @@ int shf_launch(const ShfJob*, const ShfJob&, uint32_t, uint32_t, uint32_t, uint3
 
 using namespace stpgb;
 
-struct stpgb_generator {
-	stpgb_chunk_setting chunk;
-	stpgb_raindrop_setting rain;
+struct stpgb_biomefield {
 	uint32_t radius = 0u;
 	uint32_t biome_count = 0u;
 	uint32_t max_items = 0u;
-	stpgb_nn_info div_nn {}, ero_nn {};
-	int device = 0;
 	DevBuf<uint8_t> perm;
 	DevBuf<float> grad;
 	stpgb_permutation permutation {};
 	DevBuf<stpgb_biome_property> table;
+
+	std::mutex mu;
+	std::vector<std::unique_ptr<FieldScratch>> free_scratch;
+
+	std::unique_ptr<FieldScratch> acquire() {
+		std::lock_guard<std::mutex> lk(mu);
+		if (free_scratch.empty()) {
+			return std::make_unique<FieldScratch>();
+		}
+		auto s = std::move(free_scratch.back());
+		free_scratch.pop_back();
+		return s;
+	}
+	void release(std::unique_ptr<FieldScratch> s) {
+		std::lock_guard<std::mutex> lk(mu);
+		free_scratch.push_back(std::move(s));
+	}
+};
+
+struct stpgb_generator {
+	stpgb_chunk_setting chunk;
+	stpgb_raindrop_setting rain;
+	stpgb_nn_info div_nn {}, ero_nn {};
+	int device = 0;
+	stpgb_diversity_generator diversity {};
+	// the demo plugin, when the generator was made with it
+	std::unique_ptr<stpgb_biomefield> owned_plugin;
 	DevBuf<int32_t> brush_index;
 	DevBuf<float> brush_weight;
 	uint32_t brush_size = 0u;
@@ -225,42 +254,96 @@ int erode_common(stpgb_generator* g, float* const* heightfield, uint16_t* const*
 
 extern "C" {
 
-int stpgb_generator_create(const stpgb_chunk_setting* chunk, const stpgb_raindrop_setting* raindrop,
-	const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table, uint32_t biome_count,
-	uint32_t interpolation_radius, stpgb_generator** out) {
-	if (!chunk || !raindrop || !simplex || !biome_table || !out || biome_count == 0u) {
-		return inval("stpgb_generator_create: null argument or empty biome table");
+int stpgb_biomefield_create(const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table,
+	uint32_t biome_count, uint32_t interpolation_radius, stpgb_biomefield** out) {
+	if (!simplex || !biome_table || !out || biome_count == 0u) {
+		return inval("stpgb_biomefield_create: null argument or empty biome table");
 	}
+	STPGB_TRY(stpgb_simplex_setting_validate(simplex));
+	auto f = std::make_unique<stpgb_biomefield>();
+	f->radius = interpolation_radius;
+	f->biome_count = biome_count;
+	f->max_items = std::min<uint32_t>(biome_count, kShfMaxItems);
+	// permutation (STPCommonCompiler.cpp:72 -> STPPermutationGenerator::generate)
+	std::vector<uint8_t> perm(512);
+	std::vector<float> grad(2u * simplex->Distribution);
+	STPGB_TRY(stpgb_permutation_generate(simplex, perm.data(), grad.data(), static_cast<uint32_t>(grad.size())));
+	STPGB_TRY(f->perm.alloc(512));
+	STPGB_TRY(f->grad.alloc(grad.size()));
+	STPGB_CUDA_TRY(cudaMemcpy(f->perm.p, perm.data(), 512, cudaMemcpyHostToDevice));
+	STPGB_CUDA_TRY(cudaMemcpy(f->grad.p, grad.data(), grad.size() * sizeof(float), cudaMemcpyHostToDevice));
+	f->permutation = stpgb_permutation { f->perm.p, f->grad.p, simplex->Distribution };
+	STPGB_TRY(f->table.alloc(biome_count));
+	STPGB_CUDA_TRY(cudaMemcpy(f->table.p, biome_table, biome_count * sizeof(stpgb_biome_property), cudaMemcpyHostToDevice));
+	*out = f.release();
+	return STPGB_OK;
+}
+
+int stpgb_biomefield_destroy(stpgb_biomefield* plugin) {
+	delete plugin;
+	return STPGB_OK;
+}
+
+// STPBiomefieldGenerator::operator() (STPBiomefieldGenerator.cpp:79-152): the
+// filter of the biome neighbourhood, then the multi-biome heightmap kernel;
+// the filter's output stays on the device.  The call waits for its own work
+// (the filter's status is read back), so its scratch is free on return.
+int stpgb_biomefield_generate(void* plugin, const stpgb_diversity_call* call) {
+	auto* const f = static_cast<stpgb_biomefield*>(plugin);
+	if (!f || !call || !call->heightmap || !call->biomemap) {
+		return inval("stpgb_biomefield_generate: null argument");
+	}
+	const stpgb_nn_info& nn = call->biomemap_nn;
+	const uint32_t W = nn.MapSize[0], H = nn.MapSize[1];
+	if (call->heightmap_nn.MapSize[0] != W || call->heightmap_nn.MapSize[1] != H) {
+		return inval("stpgb_biomefield_generate: heightmap and biome map chunk sizes differ");
+	}
+	const size_t npix = static_cast<size_t>(W) * H;
+	const cudaStream_t s = as_stream(call->stream);
+	std::unique_ptr<FieldScratch> sc = f->acquire();
+	auto body = [&]() -> int {
+		size_t ws = 0u;
+		STPGB_TRY(stpgb_shf_workspace_size(&nn, f->radius, f->max_items, &ws));
+		const uint64_t cap = npix * shf_kcap_h(f->radius, f->max_items);
+		STPGB_TRY(sc->ws.alloc(ws));
+		STPGB_TRY(sc->offsets.alloc(npix + 1u));
+		STPGB_TRY(sc->bins.alloc(cap));
+		STPGB_TRY(sc->status.alloc(1u));
+		STPGB_TRY(stpgb_shf_filter(call->biomemap, &nn, f->radius, f->max_items, sc->ws.p, ws, sc->offsets.p,
+			sc->bins.p, cap, sc->status.p, s));
+		STPGB_TRY(stpgb_multibiome_heightmap(call->heightmap, W, sc->offsets.p, sc->bins.p, W, H, call->offset_x,
+			call->offset_y, &f->permutation, f->table.p, f->biome_count, s));
+		STPGB_TRY(stpgb_status_check(sc->status.p, s));
+		return STPGB_OK;
+	};
+	const int rc = body();
+	if (rc != STPGB_OK) {
+		cudaStreamSynchronize(s);
+	}
+	f->release(std::move(sc));
+	return rc;
+}
+
+int stpgb_generator_create_setup(const stpgb_generator_setup* setup, stpgb_generator** out) {
+	if (!setup || !setup->ChunkSetting || !setup->RainDropSetting || !setup->DiversityGenerator
+		|| !setup->DiversityGenerator->generate || !out) {
+		return inval("stpgb_generator_create_setup: null argument or diversity generator without a function");
+	}
+	const stpgb_chunk_setting* const chunk = setup->ChunkSetting;
+	const stpgb_raindrop_setting* const raindrop = setup->RainDropSetting;
 	// STPChunkSetting::validate (SuperTerrain+/SuperTerrain+/Private/STPEnvironment.cpp:17-41), heightfield part
 	if (chunk->MapSize[0] == 0u || chunk->MapSize[1] == 0u || !odd_positive(chunk->DiversityNearestNeighbour)
 		|| !odd_positive(chunk->ErosionNearestNeighbour)) {
 		return inval("STPChunkSetting: MapSize must be positive and neighbour counts positive and odd");
 	}
 	STPGB_TRY(stpgb_raindrop_setting_validate(raindrop));
-	STPGB_TRY(stpgb_simplex_setting_validate(simplex));
 	auto g = std::make_unique<stpgb_generator>();
 	g->chunk = *chunk;
 	g->rain = *raindrop;
-	g->radius = interpolation_radius;
-	g->biome_count = biome_count;
-	g->max_items = std::min<uint32_t>(biome_count, kShfMaxItems);
+	g->diversity = *setup->DiversityGenerator;
 	g->div_nn = make_nn(chunk->MapSize, chunk->DiversityNearestNeighbour);
 	g->ero_nn = make_nn(chunk->MapSize, chunk->ErosionNearestNeighbour);
-	size_t ws = 0u;
-	STPGB_TRY(stpgb_shf_workspace_size(&g->div_nn, interpolation_radius, g->max_items, &ws));
 	STPGB_CUDA_TRY(cudaGetDevice(&g->device));
-
-	// permutation (STPCommonCompiler.cpp:72 -> STPPermutationGenerator::generate)
-	std::vector<uint8_t> perm(512);
-	std::vector<float> grad(2u * simplex->Distribution);
-	STPGB_TRY(stpgb_permutation_generate(simplex, perm.data(), grad.data(), static_cast<uint32_t>(grad.size())));
-	STPGB_TRY(g->perm.alloc(512));
-	STPGB_TRY(g->grad.alloc(grad.size()));
-	STPGB_CUDA_TRY(cudaMemcpy(g->perm.p, perm.data(), 512, cudaMemcpyHostToDevice));
-	STPGB_CUDA_TRY(cudaMemcpy(g->grad.p, grad.data(), grad.size() * sizeof(float), cudaMemcpyHostToDevice));
-	g->permutation = stpgb_permutation { g->perm.p, g->grad.p, simplex->Distribution };
-	STPGB_TRY(g->table.alloc(biome_count));
-	STPGB_CUDA_TRY(cudaMemcpy(g->table.p, biome_table, biome_count * sizeof(stpgb_biome_property), cudaMemcpyHostToDevice));
 
 	// erosion brush over the merged erosion map (STPHeightfieldGenerator.cpp:130-131)
 	uint32_t bs = 0u;
@@ -275,6 +358,33 @@ int stpgb_generator_create(const stpgb_chunk_setting* chunk, const stpgb_raindro
 	STPGB_CUDA_TRY(cudaMemcpy(g->brush_weight.p, bw.data(), bs * sizeof(float), cudaMemcpyHostToDevice));
 	g->brush_size = bs;
 	*out = g.release();
+	return STPGB_OK;
+}
+
+int stpgb_generator_create(const stpgb_chunk_setting* chunk, const stpgb_raindrop_setting* raindrop,
+	const stpgb_simplex_setting* simplex, const stpgb_biome_property* biome_table, uint32_t biome_count,
+	uint32_t interpolation_radius, stpgb_generator** out) {
+	if (!chunk || !raindrop || !simplex || !biome_table || !out || biome_count == 0u) {
+		return inval("stpgb_generator_create: null argument or empty biome table");
+	}
+	// the filter's own checks of the radius against the diversity neighbourhood, at creation
+	const stpgb_nn_info div = make_nn(chunk->MapSize, chunk->DiversityNearestNeighbour);
+	if (chunk->MapSize[0] == 0u || chunk->MapSize[1] == 0u || !odd_positive(chunk->DiversityNearestNeighbour)
+		|| !odd_positive(chunk->ErosionNearestNeighbour)) {
+		return inval("STPChunkSetting: MapSize must be positive and neighbour counts positive and odd");
+	}
+	STPGB_TRY(stpgb_raindrop_setting_validate(raindrop));
+	size_t ws = 0u;
+	STPGB_TRY(stpgb_shf_workspace_size(&div, interpolation_radius, std::min<uint32_t>(biome_count, kShfMaxItems), &ws));
+	stpgb_biomefield* plugin = nullptr;
+	STPGB_TRY(stpgb_biomefield_create(simplex, biome_table, biome_count, interpolation_radius, &plugin));
+	std::unique_ptr<stpgb_biomefield> owned(plugin);
+	const stpgb_diversity_generator dg { stpgb_biomefield_generate, plugin };
+	const stpgb_generator_setup setup { chunk, raindrop, &dg };
+	stpgb_generator* g = nullptr;
+	STPGB_TRY(stpgb_generator_create_setup(&setup, &g));
+	g->owned_plugin = std::move(owned);
+	*out = g;
 	return STPGB_OK;
 }
 
@@ -295,22 +405,28 @@ int stpgb_generator_generate(stpgb_generator* g, float* heightfield, const uint1
 	const uint32_t W = nn.MapSize[0], H = nn.MapSize[1];
 	const size_t npix = static_cast<size_t>(W) * H;
 	auto body = [&]() -> int {
-		size_t ws = 0u;
-		STPGB_TRY(stpgb_shf_workspace_size(&nn, g->radius, g->max_items, &ws));
-		const uint64_t cap = npix * shf_kcap_h(g->radius, g->max_items);
 		STPGB_TRY(slot->biome.alloc(static_cast<size_t>(nn.TotalMapSize[0]) * nn.TotalMapSize[1]));
-		STPGB_TRY(slot->ws.alloc(ws));
-		STPGB_TRY(slot->offsets.alloc(npix + 1u));
-		STPGB_TRY(slot->bins.alloc(cap));
 		STPGB_TRY(slot->height.alloc(npix));
-		STPGB_TRY(slot->status.alloc(1u));
 		STPGB_TRY(merge<uint16_t>(slot->biome.p, biomemap, nn, s));
-		STPGB_TRY(stpgb_shf_filter(slot->biome.p, &nn, g->radius, g->max_items, slot->ws.p, ws, slot->offsets.p,
-			slot->bins.p, cap, slot->status.p, s));
-		STPGB_TRY(stpgb_multibiome_heightmap(slot->height.p, W, slot->offsets.p, slot->bins.p, W, H, offset_x, offset_y,
-			&g->permutation, g->table.p, g->biome_count, s));
+		stpgb_diversity_call call {};
+		call.heightmap = slot->height.p;
+		call.biomemap = slot->biome.p;
+		call.biomemap_chunks_host = biomemap;
+		const uint32_t one[2] = { 1u, 1u };
+		call.heightmap_nn = make_nn(nn.MapSize, one);
+		call.biomemap_nn = nn;
+		call.offset_x = offset_x;
+		call.offset_y = offset_y;
+		call.stream = s;
+		const int prc = g->diversity.generate(g->diversity.user, &call);
+		if (prc != STPGB_OK) {
+			if (prc < STPGB_OK || prc > STPGB_ECAPACITY) {
+				return inval("diversity generator failed with code " + std::to_string(prc));
+			}
+			return prc;
+		}
 		STPGB_CUDA_TRY(cudaMemcpyAsync(heightfield, slot->height.p, npix * sizeof(float), cudaMemcpyDeviceToHost, s));
-		STPGB_TRY(stpgb_status_check(slot->status.p, s));
+		STPGB_CUDA_TRY(cudaStreamSynchronize(s));
 		return STPGB_OK;
 	};
 	const int rc = body();

@@ -217,6 +217,122 @@ void generator_round_trip() {
 	CHECK(after <= before + 1e-3 * before); // sediment only leaves the map
 }
 
+// A user-written diversity plugin, as a SuperTerrain+ caller writes one
+// against STPDiversityGenerator.hpp: both maps staged in host memory through
+// STPMergedBuffer; the height of a pixel is a function of its own biome
+// sample, its four axis neighbours 7 pixels away in the merged neighbourhood
+// (reaching into the neighbour chunks) and the chunk offset.
+struct TerracePlugin : STPDiversityGenerator {
+	unsigned int Calls = 0u;
+	void operator()(const STPNearestNeighbourHeightFloatWTextureBuffer& heightmap_buffer,
+		const STPNearestNeighbourSampleRTextureBuffer& biomemap_buffer, const STPVec2 offset) override {
+		using HB = STPNearestNeighbourHeightFloatWTextureBuffer;
+		using BB = STPNearestNeighbourSampleRTextureBuffer;
+		const HB::STPMergedBuffer height(heightmap_buffer, HB::STPMemoryLocation::HostMemory);
+		const BB::STPMergedBuffer biome(biomemap_buffer, BB::STPMemoryLocation::HostMemory);
+		const auto& nn = biomemap_buffer.NeighbourInfo;
+		const unsigned int W = nn.MapSize.x, H = nn.MapSize.y, TW = nn.TotalMapSize.x;
+		const unsigned int ox = (nn.ChunkNearestNeighbour.x / 2u) * W, oy = (nn.ChunkNearestNeighbour.y / 2u) * H;
+		const STPSample_t* const b = biome.getHost();
+		float* const h = height.getHost();
+		for (unsigned int y = 0u; y < H; y++) {
+			for (unsigned int x = 0u; x < W; x++) {
+				const size_t c = static_cast<size_t>(y + oy) * TW + (x + ox);
+				const unsigned int around = b[c - 7u] + b[c + 7u] + b[c - 7u * TW] + b[c + 7u * TW];
+				h[static_cast<size_t>(y) * W + x] = 0.1f * b[c] + 0.01f * around + 1e-4f * static_cast<float>(offset.x);
+			}
+		}
+		Calls++;
+	}
+};
+
+struct FailingPlugin : STPDiversityGenerator {
+	struct Refused : std::runtime_error {
+		using std::runtime_error::runtime_error;
+	};
+	void operator()(const STPNearestNeighbourHeightFloatWTextureBuffer&, const STPNearestNeighbourSampleRTextureBuffer&,
+		STPVec2) override {
+		throw Refused("this plugin refuses every chunk");
+	}
+};
+
+STPEnvironment::STPChunkSetting chunk_setting(unsigned int S) {
+	STPEnvironment::STPChunkSetting c;
+	c.ChunkSize = STPUVec2 { S, S };
+	c.MapSize = STPUVec2 { S, S };
+	c.ChunkScale = STPDVec2 { 1.0, 1.0 };
+	c.DiversityNearestNeighbour = STPUVec2 { 3u, 3u };
+	c.ErosionNearestNeighbour = STPUVec2 { 3u, 3u };
+	c.SplatNearestNeighbour = STPUVec2 { 3u, 3u };
+	c.RenderDistance = STPUVec2 { 5u, 5u };
+	return c;
+}
+
+void plugin_setup_errors() {
+	TerracePlugin plugin;
+	auto chunk = chunk_setting(32u);
+	const auto rain = raindrop(100u);
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] {
+		STPHeightfieldGenerator g(STPHeightfieldGenerator::STPGeneratorSetup { &chunk, &rain, nullptr });
+	}));
+	chunk.DiversityNearestNeighbour = STPUVec2 { 2u, 3u };
+	CHECK(throws<STPException::STPInvalidEnvironment>([&] {
+		STPHeightfieldGenerator g(STPHeightfieldGenerator::STPGeneratorSetup { &chunk, &rain, &plugin });
+	}));
+	CHECK(plugin.Calls == 0u);
+}
+
+void user_plugin_generates() {
+	const unsigned int S = 48u;
+	TerracePlugin plugin;
+	const auto chunk = chunk_setting(S);
+	const auto rain = raindrop(5000u);
+	STPHeightfieldGenerator gen(STPHeightfieldGenerator::STPGeneratorSetup { &chunk, &rain, &plugin });
+	std::vector<std::vector<STPSample_t>> biomes(9, std::vector<STPSample_t>(S * S));
+	std::vector<const STPSample_t*> bp;
+	for (int c = 0; c < 9; c++) {
+		for (unsigned int i = 0; i < S * S; i++) {
+			biomes[c][i] = static_cast<STPSample_t>((i * 7u + (i / S) * 3u + static_cast<unsigned int>(c) * 5u) % 11u);
+		}
+		bp.push_back(biomes[c].data());
+	}
+	std::vector<float> h(S * S, -1.0f);
+	gen.generate(h.data(), bp.data(), vec2 { 96.0f, -48.0f });
+	CHECK(plugin.Calls == 1u);
+	// the same formula on the caller's own chunks
+	auto at = [&](int x, int y) {
+		const int cx = (x + static_cast<int>(S)) / static_cast<int>(S), cy = (y + static_cast<int>(S)) / static_cast<int>(S);
+		const int lx = x + static_cast<int>(S) - cx * static_cast<int>(S), ly = y + static_cast<int>(S) - cy * static_cast<int>(S);
+		return static_cast<unsigned int>(biomes[cy * 3 + cx][ly * S + lx]);
+	};
+	bool equal = true;
+	for (int y = 0; y < static_cast<int>(S); y++) {
+		for (int x = 0; x < static_cast<int>(S); x++) {
+			const unsigned int around = at(x - 7, y) + at(x + 7, y) + at(x, y - 7) + at(x, y + 7);
+			const float want = 0.1f * at(x, y) + 0.01f * around + 1e-4f * 96.0f;
+			equal = equal && h[y * S + x] == want;
+		}
+	}
+	CHECK(equal);
+	// an exception thrown by the plugin reaches the caller of generate unchanged
+	FailingPlugin bad;
+	STPHeightfieldGenerator gen_bad(STPHeightfieldGenerator::STPGeneratorSetup { &chunk, &rain, &bad });
+	CHECK(throws<FailingPlugin::Refused>([&] { gen_bad.generate(h.data(), bp.data(), vec2 { 0.0f, 0.0f }); }));
+	// the demo plugin through the setup constructor gives the folded constructor's heightmap
+	STPEnvironment::STPSimplexNoiseSetting s {};
+	s.Seed = 42u;
+	s.Distribution = 8u;
+	s.Offset = 0.2181661565;
+	std::vector<stpgb_biome_property> table(11, stpgb_biome_property { 96.0f, 5u, 0.5f, 2.0f, 0.0f, 0.7f });
+	STPDemo::STPBiomefieldGenerator field(s, table, 8u);
+	STPHeightfieldGenerator via_setup(STPHeightfieldGenerator::STPGeneratorSetup { &chunk, &rain, &field });
+	STPHeightfieldGenerator folded(uvec2 { S, S }, uvec2 { 3u, 3u }, uvec2 { 3u, 3u }, rain, s, table, 8u);
+	std::vector<float> a(S * S), b(S * S);
+	via_setup.generate(a.data(), bp.data(), vec2 { 48.0f, 0.0f });
+	folded.generate(b.data(), bp.data(), vec2 { 48.0f, 0.0f });
+	CHECK(a == b);
+}
+
 struct ivec2 {
 	int x, y;
 	ivec2(int a, int b) : x(a), y(b) {}
@@ -318,7 +434,9 @@ int main(int argc, char** argv) {
 	biome_factory_errors();
 	splat_generator_errors();
 	chunk_coordinates();
+	plugin_setup_errors();
 	if (!cpu_only) {
+		user_plugin_generates();
 		histogram_known_answer();
 		generator_round_trip();
 		biome_factory_reference_maps();

@@ -67,3 +67,68 @@ def test_erode_mass_balance_and_format(stpgb, dev, oracle):
         assert np.array_equal(fixed[i], oracle.format(chunks[i]))
     # the default droplet source (Philox keyed by the raindrop seed) also runs
     gen.erode(chunks, fixed)
+
+
+def _chunks(S, seed):
+    rng = np.random.default_rng(seed)
+    return [rng.integers(0, 4, (S, S)).astype(np.uint16) for _ in range(9)]
+
+
+def test_setup_with_the_demo_plugin_equals_the_folded_constructor(stpgb):
+    """STPHeightfieldGenerator(STPGeneratorSetup) with the demo's multi-biome plugin as its diversity
+    generator gives the heightmap of the constructor that folds the plugin in, bit for bit."""
+    S = 64
+    cs = stpgb.ChunkSetting()
+    cs.MapSize[:] = [S, S]
+    cs.DiversityNearestNeighbour[:] = [3, 3]
+    cs.ErosionNearestNeighbour[:] = [3, 3]
+    rd = stpgb.RaindropSetting(**helpers.raindrop_dict(1000))
+    simplex = stpgb.SimplexSetting(42, 8, 0.2181661565)
+    table = helpers.biome_table(4, 3)
+    plugin = stpgb.STPBiomefieldGenerator(simplex, table, 8)
+    a = stpgb.STPHeightfieldGenerator.setup(cs, rd, plugin)
+    b = stpgb.STPHeightfieldGenerator(cs, rd, simplex, table, 8)
+    chunks = _chunks(S, 1)
+    ha, hb = np.zeros((S, S), np.float32), np.zeros((S, S), np.float32)
+    a.generate(ha, chunks, (64.0, -128.0))
+    b.generate(hb, chunks, (64.0, -128.0))
+    assert np.array_equal(ha, hb) and ha.max() > 0.0
+
+
+def test_user_plugin_writes_the_heightmap_and_its_errors_reach_the_caller(stpgb):
+    """A diversity plugin written by the caller: it reads the merged biome neighbourhood off the device
+    and writes its own function of it into the chunk's heightmap (stpgb_copy on the call's stream).
+    An exception it raises comes back out of generate unchanged."""
+    S = 48
+
+    class Terrace(stpgb.STPDiversityGenerator):
+        calls = 0
+
+        def __call__(self, heightmap, biomemap, offset, call):
+            nn = call.biomemap_nn
+            tw, th = nn.TotalMapSize[0], nn.TotalMapSize[1]
+            merged = np.zeros((th, tw), np.uint16)
+            stpgb.check(stpgb.lib().stpgb_copy(merged.ctypes.data, biomemap, merged.nbytes, call.stream, 1))
+            centre = merged[S:2 * S, S:2 * S].astype(np.float32)
+            out = np.ascontiguousarray(0.1 * centre + np.float32(1e-3) * np.float32(offset[0]), np.float32)
+            stpgb.check(stpgb.lib().stpgb_copy(heightmap, out.ctypes.data, out.nbytes, call.stream, 1))
+            Terrace.calls += 1
+
+    class Refuse(stpgb.STPDiversityGenerator):
+        def __call__(self, heightmap, biomemap, offset, call):
+            raise KeyError("no heightmap for this chunk")
+
+    cs = stpgb.ChunkSetting()
+    cs.MapSize[:] = [S, S]
+    cs.DiversityNearestNeighbour[:] = [3, 3]
+    cs.ErosionNearestNeighbour[:] = [3, 3]
+    rd = stpgb.RaindropSetting(**helpers.raindrop_dict(1000))
+    gen = stpgb.STPHeightfieldGenerator.setup(cs, rd, Terrace())
+    chunks = _chunks(S, 2)
+    h = np.full((S, S), -1.0, np.float32)
+    gen.generate(h, chunks, (96.0, 0.0))
+    assert Terrace.calls == 1
+    assert np.array_equal(h, (0.1 * chunks[4].astype(np.float32) + np.float32(1e-3) * np.float32(96.0)).astype(np.float32))
+    bad = stpgb.STPHeightfieldGenerator.setup(cs, rd, Refuse())
+    with pytest.raises(KeyError):
+        bad.generate(h, chunks, (0.0, 0.0))
