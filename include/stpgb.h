@@ -599,6 +599,36 @@ STPGB_API int stpgb_generator_erode_starts(stpgb_generator* gen, float* const* h
 	uint16_t* const* heightfield_fixed, const float* starts_xy, uint32_t count,
 	double* residual_sediment);
 
+/* -------------------------------------------------- roofline kernels -- */
+
+/* No counterpart in the reference: the measurement kernels behind the
+ * roofline denominators of the kernels that HBM copy bandwidth does not
+ * bound.  Each launch is `blocks` blocks of 256 threads, asynchronous on
+ * `stream`; time it with events on that stream.
+ *   RED_F32     every thread adds 1.0f with a scalar red.global to `iters`
+ *               pseudo-random floats of `buffer` (`elements` floats, a power
+ *               of two): 4 bytes per operation;
+ *   RED_V4_F32  the same with 16-byte vector reductions (red.global.add.v4.f32)
+ *               to aligned groups of four floats: 16 bytes per operation;
+ *   LOAD_V4_F32 `iters` pseudo-random 16-byte loads per thread, kept in L2
+ *               (ld.global.cg); `sink` is one float that is never written for a
+ *               map of zeros;
+ *   CHASE       one thread follows the uint32 table `buffer` of `elements`
+ *               entries from entry 0 for `iters` dependent loads and writes the
+ *               elapsed clock64 ticks to sink[0] (uint64, then the last index);
+ *   FMA_F32     eight independent chains of `iters` fused multiply-adds per
+ *               thread (16 flop per thread and iteration); `buffer` is one
+ *               float, never written. */
+enum {
+	STPGB_ROOFLINE_RED_F32 = 0,
+	STPGB_ROOFLINE_RED_V4_F32 = 1,
+	STPGB_ROOFLINE_LOAD_V4_F32 = 2,
+	STPGB_ROOFLINE_CHASE = 3,
+	STPGB_ROOFLINE_FMA_F32 = 4
+};
+STPGB_API int stpgb_roofline_launch(uint32_t kind, void* buffer, uint64_t elements, uint32_t blocks,
+	uint32_t iters, void* sink, void* stream);
+
 /* ------------------------------------------------------ batched pipeline -- */
 
 /* No counterpart in the reference, which generates one chunk per call: many

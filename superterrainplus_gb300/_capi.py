@@ -218,6 +218,7 @@ PROTOTYPES = {
     "stpgb_biomefield_destroy": (C.c_int, [vp]),
     "stpgb_biomefield_generate": (C.c_int, [vp, C.POINTER(DiversityCall)]),
     "stpgb_copy": (C.c_int, [vp, vp, sz, vp, C.c_int]),
+    "stpgb_roofline_launch": (C.c_int, [u32, vp, u64, u32, u32, vp, vp]),
     "stpgb_generator_generate": (C.c_int, [vp, vp, vp, f32, f32]),
     "stpgb_generator_erode": (C.c_int, [vp, vp, vp]),
     "stpgb_generator_erode_starts": (C.c_int, [vp, vp, vp, vp, u32, C.POINTER(f64)]),

@@ -35,6 +35,10 @@ namespace stpgb {
 namespace {
 
 constexpr uint32_t kVBlock = 64u;
+// rows of vertical output staged per column, and the accumulator capacity up
+// to which the vertical pass stages its output
+constexpr uint32_t kStageRows = 8u;
+constexpr uint32_t kStageCap = 16u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
 // threads per SM the segmented passes aim for
@@ -76,6 +80,13 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	extern __shared__ uint32_t vsm[];
 	uint32_t* const acc = vsm + threadIdx.x;              // entry j at acc[j * kVBlock]
 	uint32_t* const key = vsm + kcap * kVBlock + threadIdx.x; // run start of entry j (segment start)
+	// output staging: 8 rows of entries and entry counts, written out as
+	// whole 32-byte sectors of the column-major buffers
+	uint32_t* const st_e = vsm + 2u * kcap * kVBlock + threadIdx.x;                  // [8][kcap][kVBlock]
+	uint32_t* const st_n = vsm + (2u + kStageRows) * kcap * kVBlock + threadIdx.x;   // [8][kVBlock]
+	const bool staged = kcap <= kStageCap && (J.H % kStageRows) == 0u
+		&& (reinterpret_cast<uintptr_t>(J.vbuf) % 16u) == 0u && (reinterpret_cast<uintptr_t>(J.vn) % 16u) == 0u;
+	uint32_t gmax = 0u;
 	uint32_t n = 0u;
 	bool overflow = false;
 
@@ -116,11 +127,60 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	auto at = [&](const int q) {
 		return static_cast<uint32_t>(__ldg(col + static_cast<uint64_t>(static_cast<int64_t>(J.sy) + q) * pitch));
 	};
+	// column-major output ([column][entry][row]): the horizontal pass's warps
+	// (consecutive rows) read one line per entry plane and column
+	uint16_t* const vn_col = J.vn + static_cast<size_t>(k) * J.H;
+	uint32_t* const vb_col = J.vbuf + static_cast<size_t>(k) * kcap * J.H;
+	auto write_row = [&](const uint32_t y, const uint32_t cnt, const uint32_t* const src, const uint32_t stride) {
+		vn_col[y] = static_cast<uint16_t>(cnt);
+		for (uint32_t j = 0u; j < cnt; j++) {
+			vb_col[static_cast<size_t>(j) * J.H + y] = src[j * stride];
+		}
+	};
+	// rows [g0, y] of the staging buffer (slots y & 7); a whole aligned group of
+	// eight goes out as one 16-byte store of counts and two per entry plane
+	// (slots past a row's count carry stale values, which readers skip)
+	auto flush = [&](const uint32_t y) {
+		const uint32_t g0 = max(y_a, y & ~(kStageRows - 1u));
+		if (y - g0 == kStageRows - 1u) {
+			uint32_t nn[kStageRows];
+#pragma unroll
+			for (uint32_t i = 0u; i < kStageRows; i++) {
+				nn[i] = st_n[i * kVBlock];
+			}
+			*reinterpret_cast<uint4*>(vn_col + g0) = make_uint4(nn[0] | (nn[1] << 16), nn[2] | (nn[3] << 16),
+				nn[4] | (nn[5] << 16), nn[6] | (nn[7] << 16));
+			for (uint32_t j = 0u; j < gmax; j++) {
+				uint32_t e[kStageRows];
+#pragma unroll
+				for (uint32_t i = 0u; i < kStageRows; i++) {
+					e[i] = st_e[(i * kcap + j) * kVBlock];
+				}
+				uint4* const dst = reinterpret_cast<uint4*>(vb_col + static_cast<size_t>(j) * J.H + g0);
+				dst[0] = make_uint4(e[0], e[1], e[2], e[3]);
+				dst[1] = make_uint4(e[4], e[5], e[6], e[7]);
+			}
+		} else {
+			for (uint32_t yy = g0; yy <= y; yy++) {
+				const uint32_t i = yy & (kStageRows - 1u);
+				write_row(yy, st_n[i * kVBlock], st_e + i * kcap * kVBlock, kVBlock);
+			}
+		}
+		gmax = 0u;
+	};
 	auto emit = [&](const uint32_t y) {
-		J.vn[static_cast<size_t>(y) * ncols + k] = static_cast<uint16_t>(n);
-		uint32_t* const out = J.vbuf + static_cast<size_t>(y) * kcap * ncols + k;
+		if (!staged) {
+			write_row(y, n, acc, kVBlock);
+			return;
+		}
+		const uint32_t i = y & (kStageRows - 1u);
+		st_n[i * kVBlock] = n;
 		for (uint32_t j = 0u; j < n; j++) {
-			out[static_cast<size_t>(j) * ncols] = acc[j * kVBlock];
+			st_e[(i * kcap + j) * kVBlock] = acc[j * kVBlock];
+		}
+		gmax = max(gmax, n);
+		if (i == kStageRows - 1u || y + 1u == y_b) {
+			flush(y);
 		}
 	};
 
@@ -171,9 +231,21 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 		}
 	}
 	emit(y_a);
+	// A step whose added and removed samples are equal leaves the accumulator
+	// as it was (the item is present throughout, so nothing is inserted or
+	// erased); the next step's two samples are loaded one step ahead.
+	uint32_t va = y_a + 1u < y_b ? at(static_cast<int>(y_a + 1u) + r) : 0u;
+	uint32_t vr = y_a + 1u < y_b ? at(static_cast<int>(y_a) - r) : 0u;
 	for (uint32_t y = y_a + 1u; y < y_b; y++) {
-		inc(at(static_cast<int>(y) + r));
-		dec(at(static_cast<int>(y) - 1 - r));
+		const uint32_t add = va, sub = vr;
+		if (y + 1u < y_b) {
+			va = at(static_cast<int>(y + 1u) + r);
+			vr = at(static_cast<int>(y) - r);
+		}
+		if (add != sub) {
+			inc(add);
+			dec(sub);
+		}
 		emit(y);
 	}
 	if (overflow) {
@@ -205,6 +277,8 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	}
 	const uint32_t x_b = min(J.W, x_a + seg_len);
 	extern __shared__ uint32_t hsm[];
+	// staging words of the write pass after the accumulator (an even count, for 8-byte alignment)
+	const uint32_t hstage = 2u * kcap * kHBlock + ((kcap * kHBlock + 3u) / 4u) * 2u;
 	uint32_t* const cnt = hsm + threadIdx.x;                                               // [kcap][kHBlock]
 	uint32_t* const key = hsm + kcap * kHBlock + threadIdx.x;                              // [kcap][kHBlock]
 	uint16_t* const item = reinterpret_cast<uint16_t*>(hsm + 2u * kcap * kHBlock) + threadIdx.x; // [kcap][kHBlock]
@@ -242,20 +316,27 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 			}
 		}
 	};
-	const uint32_t ncols = J.W + 2u * J.r;
-	const uint16_t* const vn = J.vn + static_cast<size_t>(y) * ncols;
-	const uint32_t* const vrow = J.vbuf + static_cast<size_t>(y) * kcap_v * ncols;
+	// the vertical histogram of column kc for this row: vn_at(kc) entries, entry j at ent(kc, j)
+	const uint64_t H = J.H;
+	const uint16_t* const vn = J.vn + y;
+	const uint32_t* const vcol = J.vbuf + y;
+	auto vn_at = [&](const uint32_t kc) {
+		return min(static_cast<uint32_t>(vn[kc * H]), kcap_v); // the vertical pass never writes more
+	};
+	auto ent = [&](const uint32_t kc, const uint32_t j) {
+		return vcol[(kc * static_cast<uint64_t>(kcap_v) + j) * H];
+	};
 	auto add_col = [&](const uint32_t kc) {
-		const uint32_t nv = vn[kc];
+		const uint32_t nv = vn_at(kc);
 		for (uint32_t j = 0u; j < nv; j++) {
-			const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+			const uint32_t e = ent(kc, j);
 			inc(e >> 16, e & 0xFFFFu);
 		}
 	};
 	auto sub_col = [&](const uint32_t kc) {
-		const uint32_t nv = vn[kc];
+		const uint32_t nv = vn_at(kc);
 		for (uint32_t j = 0u; j < nv; j++) {
-			const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+			const uint32_t e = ent(kc, j);
 			dec(e >> 16, e & 0xFFFFu);
 		}
 	};
@@ -268,9 +349,9 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	} else {
 		// counts of the window, each item keyed by (first column, place in its histogram)
 		for (uint32_t kc = x_a; kc < x_a + side; kc++) {
-			const uint32_t nv = vn[kc];
+			const uint32_t nv = vn_at(kc);
 			for (uint32_t j = 0u; j < nv; j++) {
-				const uint32_t e = vrow[static_cast<size_t>(j) * ncols + kc];
+				const uint32_t e = ent(kc, j);
 				const uint32_t before = n;
 				inc(e >> 16, e & 0xFFFFu);
 				if (n > before) {
@@ -281,7 +362,7 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 		// leftward sweep: extend each run while its columns stay within 2r+1
 		uint32_t open = n;
 		for (int kc = static_cast<int>(x_a) - 1; kc >= 0 && open > 0u; kc--) {
-			const uint32_t nv = vn[kc];
+			const uint32_t nv = vn_at(static_cast<uint32_t>(kc));
 			for (uint32_t i = 0u; i < n; i++) {
 				const uint32_t ki = key[i * kHBlock];
 				if (ki & kResolved) {
@@ -295,7 +376,7 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 				}
 				const uint32_t v = item[i * kHBlock];
 				for (uint32_t j = 0u; j < nv; j++) {
-					if ((vrow[static_cast<size_t>(j) * ncols + kc] >> 16) == v) {
+					if ((ent(static_cast<uint32_t>(kc), j) >> 16) == v) {
 						key[i * kHBlock] = (static_cast<uint32_t>(kc) << 12) | j;
 						break;
 					}
@@ -323,26 +404,139 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	uint64_t running = Write ? J.rows[slot] : 0u;
 	uint32_t* const off_row = J.offsets + static_cast<size_t>(y) * J.W;
 	uint2* const bins = reinterpret_cast<uint2*>(J.bins);
-	auto emit = [&](const uint32_t x) {
-		if constexpr (Write) {
-			off_row[x] = static_cast<uint32_t>(running);
-			for (uint32_t j = 0u; j < n; j++) {
-				const uint64_t o = running + j;
-				if (o < J.bins_capacity) {
-					const float w = __fmul_rn(__uint2float_rn(cnt[j * kHBlock]), norm);
-					bins[o] = make_uint2(item[j * kHBlock], __float_as_uint(w));
+	// Write pass: a lane's bins and offsets are contiguous runs of the output;
+	// four of each are staged and leave as 16-byte stores (two per 32-byte
+	// sector of bins), after single stores up to the first aligned position.
+	uint2* const bst = reinterpret_cast<uint2*>(hsm + hstage) + threadIdx.x; // [4][kHBlock]
+	uint32_t* const ost = hsm + hstage + 8u * kHBlock + threadIdx.x;        // [4][kHBlock]
+	const bool bvec = (reinterpret_cast<uintptr_t>(J.bins) % 16u) == 0u;
+	const bool ovec = (reinterpret_cast<uintptr_t>(off_row) % 16u) == 0u;
+	uint64_t bpos = running;
+	uint32_t bpend = 0u, opend = 0u;
+	auto bin_single = [&](const uint64_t o, const uint2 b) {
+		if (o < J.bins_capacity) {
+			bins[o] = b;
+		}
+	};
+	auto put_bin = [&](const uint2 b) {
+		if (bpend == 0u && ((bpos & 1u) || !bvec)) {
+			bin_single(bpos++, b);
+			return;
+		}
+		bst[bpend * kHBlock] = b;
+		if (++bpend == 4u) {
+			if (bpos + 4u <= J.bins_capacity) {
+				uint4* const dst = reinterpret_cast<uint4*>(bins + bpos);
+				const uint2 b0 = bst[0], b1 = bst[kHBlock], b2 = bst[2u * kHBlock], b3 = bst[3u * kHBlock];
+				dst[0] = make_uint4(b0.x, b0.y, b1.x, b1.y);
+				dst[1] = make_uint4(b2.x, b2.y, b3.x, b3.y);
+			} else {
+				for (uint32_t i = 0u; i < 4u; i++) {
+					bin_single(bpos + i, bst[i * kHBlock]);
 				}
 			}
+			bpos += 4u;
+			bpend = 0u;
+		}
+	};
+	auto put_off = [&](const uint32_t x, const uint32_t v) {
+		if (opend == 0u && (!ovec || (x & 3u))) {
+			off_row[x] = v;
+			return;
+		}
+		ost[opend * kHBlock] = v;
+		if (++opend == 4u) {
+			*reinterpret_cast<uint4*>(off_row + x - 3u) = make_uint4(ost[0], ost[kHBlock], ost[2u * kHBlock],
+				ost[3u * kHBlock]);
+			opend = 0u;
+		}
+	};
+	uint32_t last_x = x_a;
+	auto emit = [&](const uint32_t x) {
+		if constexpr (Write) {
+			put_off(x, static_cast<uint32_t>(running));
+			for (uint32_t j = 0u; j < n; j++) {
+				const float w = __fmul_rn(__uint2float_rn(cnt[j * kHBlock]), norm);
+				put_bin(make_uint2(item[j * kHBlock], __float_as_uint(w)));
+			}
+			last_x = x;
 		}
 		running += n;
 	};
+	auto drain = [&]() {
+		if constexpr (Write) {
+			for (uint32_t i = 0u; i < bpend; i++) {
+				bin_single(bpos + i, bst[i * kHBlock]);
+			}
+			for (uint32_t i = 0u; i < opend; i++) {
+				off_row[last_x + 1u - opend + i] = ost[i * kHBlock];
+			}
+		}
+	};
 
+	// The slide proper.  A step adds column x + 2r and removes column x - 1.
+	// Their entry counts and first two entries do not depend on the
+	// accumulator, so they are loaded kAhead steps early (a ring of register
+	// slots) and the loads overlap the steps in between; entries past the
+	// second (few columns hold more than two items) are loaded when applied.
+	// Entry slots past a column's count hold stale data and are not used.
+	struct ColData {
+		uint32_t n, e0, e1;
+	};
+	const bool two = kcap_v >= 2u;
+	auto fetch = [&](const uint32_t kc) {
+		ColData c;
+		c.n = vn_at(kc);
+		c.e0 = ent(kc, 0u);
+		c.e1 = two ? ent(kc, 1u) : 0u;
+		return c;
+	};
+	auto apply = [&](const uint32_t kc, const ColData& c, const bool add) {
+		if (c.n > 0u) {
+			add ? inc(c.e0 >> 16, c.e0 & 0xFFFFu) : dec(c.e0 >> 16, c.e0 & 0xFFFFu);
+		}
+		if (c.n > 1u) {
+			add ? inc(c.e1 >> 16, c.e1 & 0xFFFFu) : dec(c.e1 >> 16, c.e1 & 0xFFFFu);
+		}
+		for (uint32_t j = 2u; j < c.n; j++) {
+			const uint32_t e = ent(kc, j);
+			add ? inc(e >> 16, e & 0xFFFFu) : dec(e >> 16, e & 0xFFFFu);
+		}
+	};
+	const uint32_t r2 = 2u * J.r;
+	ColData a0 {}, a1 {}, a2 {}, a3 {}, s0 {}, s1 {}, s2 {}, s3 {};
+	auto prefetch = [&](const uint32_t xx, ColData& a, ColData& sb) {
+		if (xx < x_b) {
+			a = fetch(xx + r2);
+			sb = fetch(xx - 1u);
+		}
+	};
+	// a step whose added and removed columns hold the same histogram (at most
+	// two entries, equal item and count in order) changes nothing: every item
+	// of the removed column is present before the step and stays present
+	auto step = [&](const uint32_t xx, ColData& a, ColData& sb) {
+		if (xx < x_b) {
+			const bool same = a.n == sb.n && a.n <= 2u && (a.n < 1u || a.e0 == sb.e0) && (a.n < 2u || a.e1 == sb.e1);
+			if (!same) {
+				apply(xx + r2, a, true);
+				apply(xx - 1u, sb, false);
+			}
+			emit(xx);
+			prefetch(xx + 4u, a, sb);
+		}
+	};
 	emit(x_a);
-	for (uint32_t x = x_a + 1u; x < x_b; x++) {
-		add_col(x + 2u * J.r);
-		sub_col(x - 1u);
-		emit(x);
+	prefetch(x_a + 1u, a0, s0);
+	prefetch(x_a + 2u, a1, s1);
+	prefetch(x_a + 3u, a2, s2);
+	prefetch(x_a + 4u, a3, s3);
+	for (uint32_t x = x_a + 1u; x < x_b; x += 4u) {
+		step(x, a0, s0);
+		step(x + 1u, a1, s1);
+		step(x + 2u, a2, s2);
+		step(x + 3u, a3, s3);
 	}
+	drain();
 	if constexpr (!Write) {
 		J.rows[slot] = static_cast<uint32_t>(min(running, static_cast<uint64_t>(0xFFFFFFFFu)));
 	}
@@ -455,8 +649,10 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	};
 	const uint32_t segs_v = segments(ncols, max_H), segs_h = segments(max_H, max_W);
 	const uint32_t len_v = (max_H + segs_v - 1u) / segs_v, len_h = (max_W + segs_h - 1u) / segs_h;
-	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * 2u * sizeof(uint32_t);
-	const size_t hsmem = static_cast<size_t>(kcap_h) * kHBlock * (2u * sizeof(uint32_t) + sizeof(uint16_t));
+	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * 2u * sizeof(uint32_t)
+		+ (kcap_v <= kStageCap ? static_cast<size_t>(kStageRows) * (kcap_v + 1u) * kVBlock * sizeof(uint32_t) : 0u);
+	const size_t hsmem = (2u * static_cast<size_t>(kcap_h) * kHBlock + ((kcap_h * kHBlock + 3u) / 4u) * 2u
+		+ 12u * kHBlock) * sizeof(uint32_t);
 	const dim3 vgrid(static_cast<uint32_t>((ncols * segs_v + kVBlock - 1u) / kVBlock), njobs);
 	const dim3 hgrid(static_cast<uint32_t>((static_cast<uint64_t>(max_H) * segs_h + kHBlock - 1u) / kHBlock), njobs);
 	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v, segs_v, len_v);

@@ -23,8 +23,8 @@ struct ShfJob {
 	uint32_t W, H, sx, sy, r;
 	uint32_t kcap_v; // accumulator capacity of the vertical pass (<= 2r+1)
 	// workspace
-	uint32_t* vbuf;  // [H][kcap_v][W+2r] packed (item << 16 | count)
-	uint16_t* vn;    // [H][W+2r] entries per vertical histogram
+	uint32_t* vbuf;  // [W+2r][kcap_v][H] packed (item << 16 | count), column-major
+	uint16_t* vn;    // [W+2r][H] entries per vertical histogram
 	uint32_t* rows;  // [H*segments+1] bins per (row, segment), then exclusive prefix + total
 	// output
 	uint32_t* offsets;  // [W*H+1]
