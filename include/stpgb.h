@@ -755,8 +755,22 @@ typedef struct stpgb_server_config {
 	 * demo's IDs 0 / 1 / 3, which the biome table must cover), as the
 	 * reference's world pipeline generates biomemaps */
 	uint32_t BiomeSource;
+	/* STPGB_EROSION_PRIVATE: each request erodes a private copy of its
+	 * neighbourhood (results independent of the request mix).
+	 * STPGB_EROSION_IN_PLACE: the reference's world-pipeline semantics
+	 * (SuperTerrain+/SuperTerrain+/Private/World/STPWorldPipeline.cpp:
+	 * 339-403,485-541,640-662): a request erodes the resident chunks of its
+	 * neighbourhood in place, so a chunk carries its neighbours' erosion;
+	 * a centre chunk is eroded once (later requests for it return the
+	 * current state); the requests of one launch sequence are ordered by the
+	 * reference's priority schedule (overlapping neighbourhoods in
+	 * successive priority levels, smallest first, non-overlapping ones
+	 * together) and sequences touching the same chunks run one after the
+	 * other.  Evicting a chunk discards the erosion it carried. */
+	uint32_t ErosionMode;
 } stpgb_server_config;
 enum { STPGB_BIOMES_VORONOI = 0, STPGB_BIOMES_LAYER_CHAIN = 1 };
+enum { STPGB_EROSION_PRIVATE = 0, STPGB_EROSION_IN_PLACE = 1 };
 
 typedef struct stpgb_serve_request {
 	int32_t ChunkX, ChunkY;       /* centre chunk of the 3x3 neighbourhood */
@@ -776,6 +790,11 @@ typedef struct stpgb_serve_result {
 	const float* Heightmap;        /* device, eroded (3*MapSize)^2 neighbourhood */
 	const uint16_t* HeightmapFixed; /* device, its uint16 format */
 	double ResidualSediment;
+	/* STPGB_EROSION_IN_PLACE: the request's place in the server's erosion
+	 * order (1, 2, ...; requests of one priority level take consecutive
+	 * places and erode together), or 0 if its centre chunk had been eroded
+	 * already and it returned the current state; 0 in the private mode. */
+	uint64_t ErosionOrder;
 } stpgb_serve_result;
 
 typedef struct stpgb_server_stats {
@@ -791,6 +810,12 @@ STPGB_API int stpgb_server_create(const stpgb_server_config* config, const stpgb
 STPGB_API int stpgb_server_destroy(stpgb_server* server);
 /* Thread-safe, non-blocking.  STPGB_ENOMEM if one request alone exceeds the budget. */
 STPGB_API int stpgb_server_submit(stpgb_server* server, const stpgb_serve_request* request, uint64_t* ticket);
+/* Several requests that enter the queue together, in order, as the chunks of
+ * one STPWorldPipeline::requestChunk call do (STPWorldPipeline.cpp:640-662):
+ * the scheduler sees all of them at once.  `tickets` (may be NULL) receives
+ * `count` tickets.  Checks every request first and queues none if one fails. */
+STPGB_API int stpgb_server_submit_batch(stpgb_server* server, const stpgb_serve_request* requests, uint32_t count,
+	uint64_t* tickets);
 /* Up to `capacity` completed results; waits up to `wait_ms` (-1 = until one completes). */
 STPGB_API int stpgb_server_poll(stpgb_server* server, stpgb_serve_result* results, uint32_t capacity,
 	uint32_t* count, int wait_ms);

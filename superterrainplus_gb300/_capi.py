@@ -98,10 +98,11 @@ class BatchRequest(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("HbmBudget", C.c_uint64), ("MaxInFlight", C.c_uint32), ("MaxBatch", C.c_uint32),
                 ("Streams", C.c_uint32), ("VoronoiCell", C.c_uint32), ("BiomeSeed", C.c_uint64),
-                ("BiomeSource", C.c_uint32)]
+                ("BiomeSource", C.c_uint32), ("ErosionMode", C.c_uint32)]
 
 
 STPGB_BIOMES_VORONOI, STPGB_BIOMES_LAYER_CHAIN = 0, 1
+STPGB_EROSION_PRIVATE, STPGB_EROSION_IN_PLACE = 0, 1
 
 
 class ServeRequest(C.Structure):
@@ -113,7 +114,7 @@ class ServeRequest(C.Structure):
 class ServeResult(C.Structure):
     _fields_ = [("Ticket", C.c_uint64), ("UserTag", C.c_uint64), ("Status", C.c_int), ("MapSize", C.c_uint32),
                 ("LatencyMs", C.c_double), ("Heightmap", C.c_void_p), ("HeightmapFixed", C.c_void_p),
-                ("ResidualSediment", C.c_double)]
+                ("ResidualSediment", C.c_double), ("ErosionOrder", C.c_uint64)]
 
 
 class ServerStats(C.Structure):
@@ -242,6 +243,7 @@ PROTOTYPES = {
                                       vp, u32, C.POINTER(vp)]),
     "stpgb_server_destroy": (C.c_int, [vp]),
     "stpgb_server_submit": (C.c_int, [vp, C.POINTER(ServeRequest), C.POINTER(u64)]),
+    "stpgb_server_submit_batch": (C.c_int, [vp, vp, u32, vp]),
     "stpgb_server_poll": (C.c_int, [vp, C.POINTER(ServeResult), u32, C.POINTER(u32), C.c_int]),
     "stpgb_server_release": (C.c_int, [vp, u64]),
     "stpgb_server_download": (C.c_int, [vp, u64, vp, vp]),

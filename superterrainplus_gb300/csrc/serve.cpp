@@ -21,10 +21,18 @@
 //     launched request still needs are evicted when the pool is full.  A
 //     request that needs a chunk another sequence is still generating waits
 //     for that sequence's event on the device, not on the host;
-//   * isolation: each request erodes a private merged copy of its
-//     neighbourhood, so its result is the same alone and in a mix (up to the
-//     erosion's own run-to-run spread), unlike the reference, which erodes
-//     shared chunks in place and makes results depend on request order.
+//   * erosion, private mode (default): each request erodes a private merged
+//     copy of its neighbourhood, so its result is the same alone and in a
+//     mix (up to the erosion's own run-to-run spread);
+//   * erosion, in-place mode (the reference's semantics, STPWorldPipeline.cpp:
+//     339-403,485-541,640-662): a request gathers its neighbourhood from the
+//     resident chunks, erodes it and scatters it back, so chunks carry their
+//     neighbours' erosion; a centre is eroded once; the requests of one
+//     sequence run in the reference's priority levels (a centre takes the
+//     lowest level none of its neighbourhood's chunks has, smallest level
+//     first, one level after another on the stream) and a sequence that
+//     touches chunks an earlier sequence still uses waits for it on the
+//     device.
 #include "erosion.cuh"
 #include "noise.cuh"
 #include "serve.cuh"
@@ -131,6 +139,10 @@ struct Chunk {
 	std::shared_ptr<Iteration> maker;  // the sequence generating it, while not resident
 	int refs = 0;                      // launched requests still to gather it
 	uint64_t last_use = 0u;
+	// in-place mode: eroded (or scheduled to be) as a centre, and the last
+	// launched sequence that reads or writes the chunk
+	bool centre_done = false;
+	std::shared_ptr<Iteration> toucher;
 };
 
 struct Request {
@@ -142,6 +154,11 @@ struct Request {
 	double latency_ms = 0.0, residual = 0.0;
 	int status = STPGB_OK;
 	bool complete = false;
+	// in-place mode: whether the request erodes (its centre was not yet done),
+	// its priority level in its sequence and its place in the erosion order
+	bool erode = true;
+	uint32_t level = 0u;
+	uint64_t order = 0u;
 };
 
 struct StreamSlot {
@@ -190,7 +207,7 @@ struct stpgb_server {
 	int fatal = STPGB_OK;
 	std::string fatal_msg;
 
-	uint64_t next_ticket = 1u, clock = 0u;
+	uint64_t next_ticket = 1u, clock = 0u, erosion_order = 0u;
 	std::unordered_map<uint64_t, Request> requests;
 	std::deque<uint64_t> pending, admitted;
 	std::deque<uint64_t> done;
@@ -293,6 +310,69 @@ struct stpgb_server {
 		return STPGB_OK;
 	}
 
+	bool in_place() const {
+		return cfg.ErosionMode == STPGB_EROSION_IN_PLACE;
+	}
+
+	// checks a submitted request and fills its sizes (no lock needed)
+	int prepare(const stpgb_serve_request& q, Request& r) const;
+
+	// The reference's erosion schedule (STPWorldPipeline.cpp:339-403) over the
+	// eroding requests of one sequence, in admission order: a centre whose
+	// neighbourhood holds no scheduled chunk takes level 1; otherwise the
+	// level below the smallest one present if that is above 1, else the first
+	// free level above a run of consecutive ones; all nine chunks then carry
+	// its level.  Levels run smallest first, one after another; requests that
+	// do not erode come after every level.  Reorders `take` by level (stable)
+	// and numbers the requests in that order.
+	void schedule_levels(std::vector<uint64_t>& take) {
+		std::unordered_multimap<ChunkKey, uint32_t, ChunkKeyHash> scheduled;
+		for (const uint64_t t : take) {
+			Request& r = requests[t];
+			if (!r.erode) {
+				r.level = 0xFFFFFFFFu;
+				continue;
+			}
+			std::vector<uint32_t> present;
+			for (int c = 0; c < 9; c++) {
+				const ChunkKey k { r.req.MapSize, r.req.InterpolationRadius, r.req.ChunkX + (c % 3) - 1,
+					r.req.ChunkY + (c / 3) - 1 };
+				const auto range = scheduled.equal_range(k);
+				for (auto e = range.first; e != range.second; ++e) {
+					if (std::find(present.begin(), present.end(), e->second) == present.end()) {
+						present.push_back(e->second);
+					}
+				}
+			}
+			std::sort(present.begin(), present.end());
+			uint32_t level = 1u;
+			if (!present.empty()) {
+				if (present.front() > 1u) {
+					level = present.front() - 1u;
+				} else {
+					level = present.back() + 1u;
+					for (size_t i = 0; i + 1u < present.size(); i++) {
+						if (present[i + 1u] - present[i] > 1u) {
+							level = present[i] + 1u;
+							break;
+						}
+					}
+				}
+			}
+			r.level = level;
+			for (int c = 0; c < 9; c++) {
+				scheduled.emplace(ChunkKey { r.req.MapSize, r.req.InterpolationRadius, r.req.ChunkX + (c % 3) - 1,
+					r.req.ChunkY + (c / 3) - 1 }, level);
+			}
+		}
+		std::stable_sort(take.begin(), take.end(),
+			[this](const uint64_t a, const uint64_t b) { return requests[a].level < requests[b].level; });
+		for (const uint64_t t : take) {
+			Request& r = requests[t];
+			r.order = r.erode ? ++erosion_order : 0u;
+		}
+	}
+
 	// ---------------------------------------------------------------- worker
 
 	void complete(const std::shared_ptr<Iteration>& it) {
@@ -315,7 +395,11 @@ struct stpgb_server {
 			c.maker.reset();
 		}
 		for (const ChunkKey& k : it->used) {
-			chunks[k].refs--;
+			Chunk& c = chunks[k];
+			c.refs--;
+			if (c.toucher == it) {
+				c.toucher.reset();
+			}
 		}
 		if (it->scratch_bytes) {
 			pool.release(it->scratch_off, it->scratch_bytes);
@@ -444,6 +528,28 @@ struct stpgb_server {
 			return false;
 		}
 		it->scratch_bytes = scratch;
+		if (in_place()) {
+			// the sequence is placed: in admission order, a request erodes if its
+			// centre has not been eroded (or scheduled) before; every chunk it
+			// touches makes the sequence wait for the last earlier sequence that
+			// touched it, and then belongs to this one
+			for (const uint64_t t : take) {
+				Request& rq = requests[t];
+				for (int c = 0; c < 9; c++) {
+					Chunk& ch = chunks[ChunkKey { rq.req.MapSize, rq.req.InterpolationRadius, rq.req.ChunkX + (c % 3) - 1,
+						rq.req.ChunkY + (c / 3) - 1 }];
+					if (ch.toucher && ch.toucher != it && std::find(waits.begin(), waits.end(), ch.toucher) == waits.end()) {
+						waits.push_back(ch.toucher);
+					}
+					ch.toucher = it;
+					if (c == 4) {
+						rq.erode = !ch.centre_done;
+						ch.centre_done = true;
+					}
+				}
+			}
+			schedule_levels(take);
+		}
 		it->tickets = take;
 		it->generated = gen;
 		const int rc = enqueue(*it, sl, waits);
@@ -598,43 +704,71 @@ struct stpgb_server {
 		// (erosion_choice on its brush, its droplet density and its droplets in
 		// flight per pixel), the jobs of one variant are made contiguous and
 		// eroded by one launch.  One variant for the whole sequence would hold
-		// every request to what its densest one allows.
+		// every request to what its densest one allows.  In the in-place mode
+		// each priority level is grouped on its own.
 		struct ErosionGroup {
 			ErosionChoice ec;
 			uint32_t dpg, first, n, maxCount, maxBrush, minRadius;
 		};
-		std::vector<ErosionGroup> egroups;
-		{
-			std::vector<ErosionJob> by_request(ero, ero + nr);
-			std::vector<std::pair<uint32_t, uint32_t>> keyed(nr); // (variant key, request)
-			std::vector<ErosionChoice> choice(nr);
-			std::vector<uint32_t> dpgs(nr);
-			for (size_t i = 0; i < nr; i++) {
-				const Request& r = requests[it.tickets[i]];
+		auto group_range = [&](const size_t b, const size_t e, std::vector<ErosionGroup>& egroups) {
+			std::vector<ErosionJob> by_request(ero + b, ero + e);
+			std::vector<std::pair<uint32_t, uint32_t>> keyed(e - b); // (variant key, request)
+			std::vector<ErosionChoice> choice(e - b);
+			std::vector<uint32_t> dpgs(e - b);
+			for (size_t q = 0; q < e - b; q++) {
+				const Request& r = requests[it.tickets[b + q]];
 				const double area = static_cast<double>(r.req.MapSize) * r.req.MapSize;
 				const double density = r.droplets / area, in_flight = erosion_in_flight(r.droplets, area);
-				choice[i] = erosion_choice(r.req.BrushRadius, by_request[i].brush_size, density, in_flight, true);
+				choice[q] = erosion_choice(r.req.BrushRadius, by_request[q].brush_size, density, in_flight, true);
 				// the stable point-wise variant with two droplets per group where rows are not allowed
-				dpgs[i] = !choice[i].rows && choice[i].lanes >= 4u
-						&& erosion_variant_stable(choice[i].lanes, 2u, false, density, in_flight)
+				dpgs[q] = !choice[q].rows && choice[q].lanes >= 4u
+						&& erosion_variant_stable(choice[q].lanes, 2u, false, density, in_flight)
 					? 2u
 					: 1u;
-				keyed[i] = { choice[i].lanes * 8u + dpgs[i] * 2u + (choice[i].rows ? 1u : 0u), static_cast<uint32_t>(i) };
+				keyed[q] = { choice[q].lanes * 8u + dpgs[q] * 2u + (choice[q].rows ? 1u : 0u), static_cast<uint32_t>(q) };
 			}
 			std::stable_sort(keyed.begin(), keyed.end(),
-				[](const auto& a, const auto& b) { return a.first < b.first; });
-			for (size_t pos = 0; pos < nr; pos++) {
-				const uint32_t i = keyed[pos].second;
-				ero[pos] = by_request[i];
+				[](const auto& x, const auto& y) { return x.first < y.first; });
+			for (size_t pos = 0; pos < e - b; pos++) {
+				const uint32_t q = keyed[pos].second;
+				ero[b + pos] = by_request[q];
 				if (pos == 0u || keyed[pos].first != keyed[pos - 1u].first) {
-					egroups.push_back(ErosionGroup { choice[i], dpgs[i], static_cast<uint32_t>(pos), 0u, 0u, 0u, 0xFFFFFFFFu });
+					egroups.push_back(ErosionGroup { choice[q], dpgs[q], static_cast<uint32_t>(b + pos), 0u, 0u, 0u,
+						0xFFFFFFFFu });
 				}
 				ErosionGroup& g = egroups.back();
 				g.n++;
-				g.maxCount = std::max(g.maxCount, ero[pos].count);
-				g.maxBrush = std::max(g.maxBrush, ero[pos].brush_size);
-				g.minRadius = std::min(g.minRadius, requests[it.tickets[i]].req.BrushRadius);
+				g.maxCount = std::max(g.maxCount, ero[b + pos].count);
+				g.maxBrush = std::max(g.maxBrush, ero[b + pos].brush_size);
+				g.minRadius = std::min(g.minRadius, requests[it.tickets[b + q]].req.BrushRadius);
 			}
+		};
+		// request ranges eroded one after another: every request (private mode),
+		// or one range per priority level of the eroding requests (in place)
+		struct Level {
+			size_t b, e;
+			std::vector<ErosionGroup> groups;
+		};
+		std::vector<Level> levels;
+		size_t n_erode = nr;
+		if (in_place()) {
+			n_erode = 0u;
+			while (n_erode < nr && requests[it.tickets[n_erode]].erode) {
+				n_erode++;
+			}
+			for (size_t i = 0; i < n_erode;) {
+				size_t j = i + 1u;
+				while (j < n_erode && requests[it.tickets[j]].level == requests[it.tickets[i]].level) {
+					j++;
+				}
+				levels.push_back(Level { i, j, {} });
+				i = j;
+			}
+		} else if (nr) {
+			levels.push_back(Level { 0u, nr, {} });
+		}
+		for (Level& L : levels) {
+			group_range(L.b, L.e, L.groups);
 		}
 		std::fill(it.residual_host, it.residual_host + nr, 0.0);
 		*it.status_host = 0u;
@@ -655,16 +789,28 @@ struct stpgb_server {
 		for (const auto& w : waits) {
 			STPGB_CUDA_TRY(cudaStreamWaitEvent(s, slots[static_cast<size_t>(w->slot)].done, 0));
 		}
-		STPGB_TRY(gather_jobs_launch(reinterpret_cast<GatherJob*>(sl.dev + o_gather), static_cast<uint32_t>(nr), maxRS, s));
-		STPGB_TRY(starts_jobs_launch(reinterpret_cast<StartsJob*>(sl.dev + o_starts), static_cast<uint32_t>(nr), maxCount,
-			this->base.Seed, s));
-		// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
-		// pitches 3 * MapSize); each job reads several blocks per round trip
-		// where few of its droplets are in flight per pixel
-		for (const ErosionGroup& g : egroups) {
-			STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero) + g.first, ero[g.first], g.n,
-				g.maxCount, g.maxBrush, s, g.ec.lanes, false, g.dpg, g.ec.rows, erosion_rows_wide(g.minRadius),
-				erosion_rows_atomic(g.minRadius, g.ec.lanes)));
+		GatherJob* const gat_dev = reinterpret_cast<GatherJob*>(sl.dev + o_gather);
+		StartsJob* const sts_dev = reinterpret_cast<StartsJob*>(sl.dev + o_starts);
+		for (const Level& L : levels) {
+			const uint32_t n = static_cast<uint32_t>(L.e - L.b);
+			STPGB_TRY(gather_jobs_launch(gat_dev + L.b, n, maxRS, s));
+			STPGB_TRY(starts_jobs_launch(sts_dev + L.b, n, maxCount, this->base.Seed, s));
+			// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
+			// pitches 3 * MapSize); each job reads several blocks per round trip
+			// where few of its droplets are in flight per pixel
+			for (const ErosionGroup& g : L.groups) {
+				STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero) + g.first, ero[g.first], g.n,
+					g.maxCount, g.maxBrush, s, g.ec.lanes, false, g.dpg, g.ec.rows, erosion_rows_wide(g.minRadius),
+					erosion_rows_atomic(g.minRadius, g.ec.lanes)));
+			}
+			if (in_place()) {
+				// the eroded neighbourhoods go back into the resident chunks
+				STPGB_TRY(scatter_jobs_launch(gat_dev + L.b, n, maxRS, s));
+			}
+		}
+		if (n_erode < nr) {
+			// requests whose centre was eroded before: the current state, after every level
+			STPGB_TRY(gather_jobs_launch(gat_dev + n_erode, static_cast<uint32_t>(nr - n_erode), maxRS, s));
 		}
 		STPGB_TRY(format_batch_launch(reinterpret_cast<FormatJob*>(sl.dev + o_fmt), static_cast<uint32_t>(nr), 3u * maxRS,
 			3u * maxRS, s));
@@ -738,6 +884,9 @@ int stpgb_server_create(const stpgb_server_config* cfg, const stpgb_raindrop_set
 	if (cfg->BiomeSource > STPGB_BIOMES_LAYER_CHAIN) {
 		return inval("stpgb_server_create: BiomeSource must be STPGB_BIOMES_VORONOI or STPGB_BIOMES_LAYER_CHAIN");
 	}
+	if (cfg->ErosionMode > STPGB_EROSION_IN_PLACE) {
+		return inval("stpgb_server_create: ErosionMode must be STPGB_EROSION_PRIVATE or STPGB_EROSION_IN_PLACE");
+	}
 	if (cfg->BiomeSource == STPGB_BIOMES_LAYER_CHAIN) {
 		STPGB_TRY(layer_chain_demo(cfg->BiomeSeed, &sv->chain));
 	}
@@ -783,25 +932,16 @@ int stpgb_server_destroy(stpgb_server* sv) {
 }
 
 int stpgb_server_submit(stpgb_server* sv, const stpgb_serve_request* req, uint64_t* ticket) {
-	if (!sv || !req) {
+	return stpgb_server_submit_batch(sv, req, 1u, ticket);
+}
+
+int stpgb_server_submit_batch(stpgb_server* sv, const stpgb_serve_request* reqs, uint32_t count, uint64_t* tickets) {
+	if (!sv || (!reqs && count)) {
 		return inval("stpgb_server_submit: null argument");
 	}
-	if (req->MapSize == 0u || (req->MapSize & 7u) || req->MapSize > 16384u || req->InterpolationRadius == 0u
-		|| (req->InterpolationRadius & 1u) || req->InterpolationRadius > req->MapSize || req->BrushRadius == 0u
-		|| !(req->DropletsPerPixel >= 0.0f)) {
-		return inval("stpgb_server_submit: MapSize must be a multiple of 8 and at most 16384, radius positive, even "
-					 "and <= MapSize, brush positive");
-	}
-	Request r;
-	r.req = *req;
-	r.submitted = Clock::now();
-	r.droplets = sv->droplets_of(*req);
-	r.bytes = stpgb_server::request_bytes(req->MapSize, r.droplets);
-	const size_t gen = 9u * (sv->generation_bytes(req->MapSize, req->InterpolationRadius)
-		+ static_cast<size_t>(req->MapSize) * req->MapSize * sizeof(float));
-	if (r.bytes + gen > sv->cfg.HbmBudget) {
-		set_error("stpgb_server_submit: one request of this size does not fit the HBM budget");
-		return STPGB_ENOMEM;
+	std::vector<Request> batch(count);
+	for (uint32_t i = 0u; i < count; i++) {
+		STPGB_TRY(sv->prepare(reqs[i], batch[i]));
 	}
 	{
 		std::lock_guard<std::mutex> lk(sv->mu);
@@ -809,17 +949,45 @@ int stpgb_server_submit(stpgb_server* sv, const stpgb_serve_request* req, uint64
 			set_error(sv->fatal_msg);
 			return sv->fatal;
 		}
-		r.ticket = sv->next_ticket++;
-		if (ticket) {
-			*ticket = r.ticket;
+		for (uint32_t i = 0u; i < count; i++) {
+			Request& r = batch[i];
+			r.ticket = sv->next_ticket++;
+			if (tickets) {
+				tickets[i] = r.ticket;
+			}
+			sv->requests[r.ticket] = r;
+			sv->pending.push_back(r.ticket);
+			sv->stats.Submitted++;
 		}
-		sv->requests[r.ticket] = r;
-		sv->pending.push_back(r.ticket);
-		sv->stats.Submitted++;
 	}
 	sv->cv_work.notify_one();
 	return STPGB_OK;
 }
+
+} // extern "C"
+
+int stpgb_server::prepare(const stpgb_serve_request& q, Request& r) const {
+	const stpgb_serve_request* const req = &q;
+	if (req->MapSize == 0u || (req->MapSize & 7u) || req->MapSize > 16384u || req->InterpolationRadius == 0u
+		|| (req->InterpolationRadius & 1u) || req->InterpolationRadius > req->MapSize || req->BrushRadius == 0u
+		|| !(req->DropletsPerPixel >= 0.0f)) {
+		return inval("stpgb_server_submit: MapSize must be a multiple of 8 and at most 16384, radius positive, even "
+					 "and <= MapSize, brush positive");
+	}
+	r.req = *req;
+	r.submitted = Clock::now();
+	r.droplets = droplets_of(*req);
+	r.bytes = stpgb_server::request_bytes(req->MapSize, r.droplets);
+	const size_t gen = 9u * (generation_bytes(req->MapSize, req->InterpolationRadius)
+		+ static_cast<size_t>(req->MapSize) * req->MapSize * sizeof(float));
+	if (r.bytes + gen > cfg.HbmBudget) {
+		set_error("stpgb_server_submit: one request of this size does not fit the HBM budget");
+		return STPGB_ENOMEM;
+	}
+	return STPGB_OK;
+}
+
+extern "C" {
 
 int stpgb_server_poll(stpgb_server* sv, stpgb_serve_result* out, uint32_t capacity, uint32_t* count, int wait_ms) {
 	if (!sv || (!out && capacity) || !count) {
@@ -847,6 +1015,7 @@ int stpgb_server_poll(stpgb_server* sv, stpgb_serve_result* out, uint32_t capaci
 		o.HeightmapFixed = reinterpret_cast<const uint16_t*>(sv->at(r.fixed));
 		o.ResidualSediment = r.residual;
 		o.MapSize = r.req.MapSize;
+		o.ErosionOrder = r.order;
 	}
 	*count = n;
 	if (sv->fatal != STPGB_OK) {

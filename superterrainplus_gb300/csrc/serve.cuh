@@ -31,6 +31,8 @@ struct StartsJob {
 int voronoi_jobs_launch(const VoronoiJob* jobs, uint32_t njobs, uint32_t max_w, uint32_t max_h, uint64_t seed,
 	uint32_t biomes, cudaStream_t s);
 int gather_jobs_launch(const GatherJob* jobs, uint32_t njobs, uint32_t max_S, cudaStream_t s);
+// the inverse of gather_jobs_launch: each merged map back into its nine chunks
+int scatter_jobs_launch(const GatherJob* jobs, uint32_t njobs, uint32_t max_S, cudaStream_t s);
 int starts_jobs_launch(const StartsJob* jobs, uint32_t njobs, uint32_t max_count, uint64_t seed, cudaStream_t s);
 
 } // namespace stpgb

@@ -61,6 +61,21 @@ __global__ void gather_jobs_kernel(const GatherJob* __restrict__ jobs) {
 	*reinterpret_cast<float4*>(J.merged + static_cast<uint64_t>(y) * W + x) = v;
 }
 
+// one (3S)^2 merged map -> its nine S x S chunk heightfields, the inverse of
+// gather_jobs_kernel (the in-place mode's write-back of an eroded neighbourhood)
+__global__ void scatter_jobs_kernel(const GatherJob* __restrict__ jobs) {
+	const GatherJob& J = jobs[blockIdx.y];
+	const uint32_t S = J.S, W = 3u * S, quads = W / 4u;
+	const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (t >= static_cast<uint64_t>(quads) * W) {
+		return;
+	}
+	const uint32_t y = static_cast<uint32_t>(t / quads), x = static_cast<uint32_t>(t % quads) * 4u;
+	const uint32_t c = (y / S) * 3u + x / S;
+	const float4 v = *reinterpret_cast<const float4*>(J.merged + static_cast<uint64_t>(y) * W + x);
+	*reinterpret_cast<float4*>(const_cast<float*>(J.chunk[c]) + static_cast<uint64_t>(y % S) * S + x % S) = v;
+}
+
 __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
 #pragma unroll
 	for (int round = 0; round < 10; round++) {
@@ -111,6 +126,16 @@ int gather_jobs_launch(const GatherJob* jobs, uint32_t njobs, uint32_t max_S, cu
 	}
 	const uint64_t threads = static_cast<uint64_t>(3u * max_S / 4u) * (3u * max_S);
 	gather_jobs_kernel<<<dim3(static_cast<uint32_t>((threads + 255u) / 256u), njobs), 256u, 0, s>>>(jobs);
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
+}
+
+int scatter_jobs_launch(const GatherJob* jobs, uint32_t njobs, uint32_t max_S, cudaStream_t s) {
+	if (njobs == 0u) {
+		return STPGB_OK;
+	}
+	const uint64_t threads = static_cast<uint64_t>(3u * max_S / 4u) * (3u * max_S);
+	scatter_jobs_kernel<<<dim3(static_cast<uint32_t>((threads + 255u) / 256u), njobs), 256u, 0, s>>>(jobs);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }

@@ -47,12 +47,15 @@ def camera_walk(n, seed, rate=200.0, speed=1.0, turn_every=5.0, lods=(256, 512, 
 
 class Server:
     def __init__(self, base_setting, simplex_setting, biome_table, hbm_budget=40 << 30, max_in_flight=64,
-                 max_batch=16, streams=3, voronoi_cell=192, biome_seed=42, layer_chain_biomes=False):
+                 max_batch=16, streams=3, voronoi_cell=192, biome_seed=42, layer_chain_biomes=False,
+                 in_place=False):
         """`layer_chain_biomes`: generate biomemaps with the demo's layer chain (the reference's
-        STPLayerChainBuilder) instead of the synthetic Voronoi map."""
+        STPLayerChainBuilder) instead of the synthetic Voronoi map.  `in_place`: erode the resident
+        chunks in place in the reference's priority-batched order (STPGB_EROSION_IN_PLACE) instead
+        of a private copy per request."""
         table = np.ascontiguousarray(biome_table, BIOME_DTYPE)
         cfg = ServerConfig(hbm_budget, max_in_flight, max_batch, streams, voronoi_cell, biome_seed,
-                           int(bool(layer_chain_biomes)))
+                           int(bool(layer_chain_biomes)), int(bool(in_place)))
         h = C.c_void_p()
         check(lib().stpgb_server_create(C.byref(cfg), C.byref(base_setting), C.byref(simplex_setting),
                                         table.ctypes.data_as(C.c_void_p), len(table), C.byref(h)))
@@ -69,6 +72,14 @@ class Server:
         t = C.c_uint64(0)
         check(lib().stpgb_server_submit(self._h, C.byref(ServeRequest(**req)), C.byref(t)))
         return t.value
+
+    def submit_many(self, requests):
+        """All `requests` enter the queue together (stpgb_server_submit_batch); returns their tickets."""
+        n = len(requests)
+        arr = (ServeRequest * n)(*[ServeRequest(**r) for r in requests])
+        t = (C.c_uint64 * n)()
+        check(lib().stpgb_server_submit_batch(self._h, arr, n, t))
+        return list(t)
 
     def poll(self, capacity=64, wait_ms=0):
         out = (ServeResult * capacity)()

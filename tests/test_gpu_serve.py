@@ -139,3 +139,100 @@ def test_serve_camera_walk_replay(stpgb, dev):
     assert np.all(lat > 0.0) and wall >= times[-1]
     assert sv.stats()["Completed"] == len(reqs)
     sv.close()
+
+
+# ------------------------------------------------------------ in-place erosion (the reference's world pipeline)
+
+
+def run_serial(server, reqs):
+    """One request at a time: each is submitted after the previous one completed."""
+    out = {}
+    for r in reqs:
+        server.submit(**r)
+        got = []
+        while not got:
+            got = server.poll(wait_ms=5000)
+        (res,) = got
+        assert res.Status == 0
+        h, _ = server.download(res)
+        out[res.UserTag] = (h, res.ErosionOrder)
+        server.release(res.Ticket)
+    return out
+
+
+def test_in_place_priority_levels_follow_the_reference_schedule(stpgb):
+    """One sequence of [A (0,0), B (2,0), C (4,0)]: B's neighbourhood shares chunk column 1 with A's, C's
+    shares column 3 with B's only.  The reference's schedule (STPWorldPipeline.cpp:339-403) gives A level
+    1, B level 2 (a chunk of level 1 in its neighbourhood) and C level 1 (the only level present, 2, is
+    above 1): C erodes together with A, before B, although it came after B."""
+    sv = make_server(stpgb, in_place=True, max_batch=3, streams=1)
+    reqs = [dict(REQS[0], ChunkX=x, ChunkY=0, UserTag=t) for t, x in enumerate([0, 2, 4])]
+    sv.submit_many(reqs)
+    order = {}
+    while len(order) < 3:
+        for res in sv.poll(wait_ms=5000):
+            assert res.Status == 0
+            order[res.UserTag] = res.ErosionOrder
+            sv.release(res.Ticket)
+    sv.close()
+    assert sorted(order.values()) == [1, 2, 3]
+    assert order[2] < order[1] and order[0] < order[1]
+
+
+def test_in_place_results_carry_earlier_erosion(stpgb):
+    """A (0,0) erodes its neighbourhood and writes it back; a second request for centre (0,0) returns that
+    state without eroding again (ErosionOrder 0, the same heights bit for bit); B (1,0) then erodes a
+    neighbourhood that shares two chunk columns with A's, and a third request for (0,0) sees column -1 as A
+    left it and columns 0 and 1 as B left them."""
+    S = REQS[0]["MapSize"]
+    sv = make_server(stpgb, in_place=True, max_batch=1, streams=1)
+    base = dict(REQS[0], ChunkY=0)
+    out = run_serial(sv, [dict(base, ChunkX=0, UserTag=0), dict(base, ChunkX=0, UserTag=1),
+                          dict(base, ChunkX=1, UserTag=2), dict(base, ChunkX=0, UserTag=3)])
+    sv.close()
+    (a, oa), (a2, oa2), (b, ob), (d, od) = out[0], out[1], out[2], out[3]
+    assert oa == 1 and oa2 == 0 and ob == 2 and od == 0
+    assert np.array_equal(a2, a)
+    assert not np.array_equal(b[:, :2 * S], a[:, S:])  # B eroded the shared columns further
+    assert np.array_equal(d[:, :S], a[:, :S])
+    assert np.array_equal(d[:, S:], b[:, :2 * S])
+
+
+def test_in_place_camera_walk_matches_a_serial_replay(stpgb):
+    """A camera walk of 24 overlapping 64^2 requests, all submitted at once, through the in-place server
+    (sequences of up to 6 requests in priority levels, three streams, sequences that share chunks ordered on
+    the device) against a serial replay of the same requests one at a time in the server's erosion order.
+    Each request's eroded neighbourhood agrees with the serial one within the erosion's run-to-run spread:
+    three times the largest RMS between two serial replays."""
+    from superterrainplus_gb300.serve import camera_walk
+    reqs, _ = camera_walk(24, 5, rate=1e6, speed=3.0, turn_every=2.0, lods=(64,), probs=(1.0,), radius=16,
+                          droplets_per_px=2.3, brush=3, lifetime=30)
+    sv = make_server(stpgb, in_place=True, max_batch=6, streams=3)
+    sv.submit_many(reqs)
+    batched = {}
+    while len(batched) < len(reqs):
+        for res in sv.poll(wait_ms=5000):
+            assert res.Status == 0
+            h, _ = sv.download(res)
+            batched[res.UserTag] = (h, res.ErosionOrder)
+            sv.release(res.Ticket)
+    sv.close()
+    orders = sorted(o for _, o in batched.values())
+    assert orders == list(range(1, len(reqs) + 1))  # distinct centres: every request erodes once
+    in_order = sorted(reqs, key=lambda r: batched[r["UserTag"]][1])
+    serial = []
+    for _ in range(2):
+        s = make_server(stpgb, in_place=True, max_batch=1, streams=1)
+        serial.append(run_serial(s, in_order))
+        s.close()
+    rms = lambda a, b: float(np.sqrt(np.mean((a.astype(np.float64) - b) ** 2)))
+    spread = max(rms(serial[0][t][0], serial[1][t][0]) for t in batched)
+    worst = max(rms(batched[t][0], serial[0][t][0]) for t in batched)
+    print(f"in-place camera walk: batched vs serial RMS {worst:.3g}, serial run-to-run spread {spread:.3g}")
+    assert worst <= 3.0 * spread + 1e-6
+    # the walk's neighbourhoods overlap: erosion carried between requests changes later results
+    private = make_server(stpgb, max_batch=1, streams=1)
+    alone = run_serial(private, in_order[-1:])
+    private.close()
+    t_last = in_order[-1]["UserTag"]
+    assert rms(alone[t_last][0], serial[0][t_last][0]) > 3.0 * spread
