@@ -35,10 +35,6 @@ namespace stpgb {
 namespace {
 
 constexpr uint32_t kVBlock = 64u;
-// rows of vertical output staged per column, and the accumulator capacity up
-// to which the vertical pass stages its output
-constexpr uint32_t kStageRows = 8u;
-constexpr uint32_t kStageCap = 16u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
 // threads per SM the segmented passes aim for
@@ -80,13 +76,6 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	extern __shared__ uint32_t vsm[];
 	uint32_t* const acc = vsm + threadIdx.x;              // entry j at acc[j * kVBlock]
 	uint32_t* const key = vsm + kcap * kVBlock + threadIdx.x; // run start of entry j (segment start)
-	// output staging: 8 rows of entries and entry counts, written out as
-	// whole 32-byte sectors of the column-major buffers
-	uint32_t* const st_e = vsm + 2u * kcap * kVBlock + threadIdx.x;                  // [8][kcap][kVBlock]
-	uint32_t* const st_n = vsm + (2u + kStageRows) * kcap * kVBlock + threadIdx.x;   // [8][kVBlock]
-	const bool staged = kcap <= kStageCap && (J.H % kStageRows) == 0u
-		&& (reinterpret_cast<uintptr_t>(J.vbuf) % 16u) == 0u && (reinterpret_cast<uintptr_t>(J.vn) % 16u) == 0u;
-	uint32_t gmax = 0u;
 	uint32_t n = 0u;
 	bool overflow = false;
 
@@ -137,51 +126,13 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 			vb_col[static_cast<size_t>(j) * J.H + y] = src[j * stride];
 		}
 	};
-	// rows [g0, y] of the staging buffer (slots y & 7); a whole aligned group of
-	// eight goes out as one 16-byte store of counts and two per entry plane
-	// (slots past a row's count carry stale values, which readers skip)
-	auto flush = [&](const uint32_t y) {
-		const uint32_t g0 = max(y_a, y & ~(kStageRows - 1u));
-		if (y - g0 == kStageRows - 1u) {
-			uint32_t nn[kStageRows];
-#pragma unroll
-			for (uint32_t i = 0u; i < kStageRows; i++) {
-				nn[i] = st_n[i * kVBlock];
-			}
-			*reinterpret_cast<uint4*>(vn_col + g0) = make_uint4(nn[0] | (nn[1] << 16), nn[2] | (nn[3] << 16),
-				nn[4] | (nn[5] << 16), nn[6] | (nn[7] << 16));
-			for (uint32_t j = 0u; j < gmax; j++) {
-				uint32_t e[kStageRows];
-#pragma unroll
-				for (uint32_t i = 0u; i < kStageRows; i++) {
-					e[i] = st_e[(i * kcap + j) * kVBlock];
-				}
-				uint4* const dst = reinterpret_cast<uint4*>(vb_col + static_cast<size_t>(j) * J.H + g0);
-				dst[0] = make_uint4(e[0], e[1], e[2], e[3]);
-				dst[1] = make_uint4(e[4], e[5], e[6], e[7]);
-			}
-		} else {
-			for (uint32_t yy = g0; yy <= y; yy++) {
-				const uint32_t i = yy & (kStageRows - 1u);
-				write_row(yy, st_n[i * kVBlock], st_e + i * kcap * kVBlock, kVBlock);
-			}
-		}
-		gmax = 0u;
-	};
+	// Writes go straight to the column-major buffers.  Staging rows in shared
+	// memory to write whole sectors made this pass faster alone, but its
+	// 18 KB per block of shared memory kept the pass's blocks off the SMs
+	// that run another stream's erosion kernel, and batches that overlap on
+	// two streams lost far more than the pass gained.
 	auto emit = [&](const uint32_t y) {
-		if (!staged) {
-			write_row(y, n, acc, kVBlock);
-			return;
-		}
-		const uint32_t i = y & (kStageRows - 1u);
-		st_n[i * kVBlock] = n;
-		for (uint32_t j = 0u; j < n; j++) {
-			st_e[(i * kcap + j) * kVBlock] = acc[j * kVBlock];
-		}
-		gmax = max(gmax, n);
-		if (i == kStageRows - 1u || y + 1u == y_b) {
-			flush(y);
-		}
+		write_row(y, n, acc, kVBlock);
 	};
 
 	const int r = static_cast<int>(J.r);
@@ -649,8 +600,7 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	};
 	const uint32_t segs_v = segments(ncols, max_H), segs_h = segments(max_H, max_W);
 	const uint32_t len_v = (max_H + segs_v - 1u) / segs_v, len_h = (max_W + segs_h - 1u) / segs_h;
-	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * 2u * sizeof(uint32_t)
-		+ (kcap_v <= kStageCap ? static_cast<size_t>(kStageRows) * (kcap_v + 1u) * kVBlock * sizeof(uint32_t) : 0u);
+	const size_t vsmem = static_cast<size_t>(kcap_v) * kVBlock * 2u * sizeof(uint32_t);
 	const size_t hsmem = (2u * static_cast<size_t>(kcap_h) * kHBlock + ((kcap_h * kHBlock + 3u) / 4u) * 2u
 		+ 12u * kHBlock) * sizeof(uint32_t);
 	const dim3 vgrid(static_cast<uint32_t>((ncols * segs_v + kVBlock - 1u) / kVBlock), njobs);
