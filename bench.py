@@ -378,9 +378,11 @@ def run_ours(args):
     sh = stream.cuda_stream
     batch.synthesize(VORONOI_CELL, SEED, sh)
     stream.synchronize()
-    # the autotuner times the erosion kernel on these inputs, then the graph is re-captured
+    # the autotuner times the filter's segment counts, the noise block sizes and the erosion
+    # variants on these inputs, then the graph is re-captured
     batch.tune()
     lanes, tune_ms = batch.tuning()
+    stage_tune = batch.tuning_stages()
 
     def barrier():
         torch.cuda.synchronize()
@@ -580,7 +582,11 @@ def run_ours(args):
             "splatmap": splatmap,
             "large_field": large,
             "uneven_batch": uneven,
-            "autotune": {"erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
+            "autotune": {"filter_segments": stage_tune[0],
+                         "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
+                         "noise_block": stage_tune[2],
+                         "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()},
+                         "erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
                                                             for (a, b, r), v in tune_ms.items()}},
@@ -684,6 +690,7 @@ def uneven_batch_section(m, np, torch, reps=3):
     torch.cuda.synchronize()
     b.tune()
     choice, tune_ms = b.tuning()
+    stage_tune = b.tuning_stages()
     st = torch.cuda.current_stream()
     for _ in range(3):
         b.run()
@@ -719,7 +726,11 @@ def uneven_batch_section(m, np, torch, reps=3):
             "stage_ms": dict(zip(["single_histogram_filter", "multibiome_noise", "hydraulic_erosion", "format"],
                                  stage_ms)),
             "autotune_dominant_group": {"lanes_per_droplet": choice[0], "droplets_per_group": choice[1],
-                                        "brush_rows": bool(choice[2])}}
+                                        "brush_rows": bool(choice[2])},
+            "autotune_stages": {"filter_segments": stage_tune[0],
+                                "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
+                                "noise_block": stage_tune[2],
+                                "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()}}}
 
 
 def large_field_section(m, np, torch, reps=3):

@@ -514,6 +514,15 @@ class Batch:
         return ((lanes.value, dpg.value, rows.value),
                 {(1 << ((i % 18) // 3), 1 << (i % 3), i // 18): ms[i] for i in range(36) if ms[i] > 0})
 
+    def tuning_stages(self):
+        """The autotuner's filter segment count (0 = from the launch size) and noise block size,
+        with {candidate: ms} for each (candidates not tried are left out)."""
+        seg, blk = C.c_uint32(0), C.c_uint32(0)
+        sms, nms = (C.c_float * 6)(), (C.c_float * 3)()
+        check(lib().stpgb_batch_tuning_stages(self._h, C.byref(seg), sms, C.byref(blk), nms))
+        return (seg.value, {c: sms[i] for i, c in enumerate((0, 1, 2, 4, 8, 16)) if sms[i] > 0},
+                blk.value, {c: nms[i] for i, c in enumerate((128, 256, 512)) if nms[i] > 0})
+
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)
         check(lib().stpgb_batch_counters(self._h, C.byref(a), C.byref(b), int(reset)))

@@ -136,6 +136,13 @@ struct stpgb_batch {
 	std::vector<ErosionJob> ero_h; // per request, request order (the plain sequence)
 	std::vector<FormatJob> fmt_h;
 	uint32_t max_S = 0u, max_r = 0u, kcap_v = 0u, kcap_h = 0u;
+	// the filter's segment count (0 = from the launch size) and the noise
+	// kernel's block size, chosen by the autotuner; its times per candidate
+	static constexpr uint32_t kShfSegCands = 6u, kNoiseBlockCands = 3u;
+	static constexpr uint32_t shf_seg_cands[kShfSegCands] = { 0u, 1u, 2u, 4u, 8u, 16u };
+	static constexpr uint32_t noise_block_cands[kNoiseBlockCands] = { 128u, 256u, 512u };
+	uint32_t shf_segments = 0u, noise_block = 256u;
+	float shf_tune_ms[kShfSegCands] = {}, noise_tune_ms[kNoiseBlockCands] = {};
 	// erosion variant groups (brush rows in 16-byte blocks need aligned maps:
 	// every merged map of a batch is 512-byte aligned with a pitch of
 	// 3 * MapSize, a multiple of 24 floats); group_of[n] is request n's group
@@ -259,10 +266,10 @@ struct stpgb_batch {
 		const uint32_t nchunks = static_cast<uint32_t>(shf_h.size());
 		switch (st) {
 		case 0u:
-			return shf_launch(shf_jobs, shf_h[0], nchunks, max_S, max_S, max_r, kcap_v, kcap_h, s);
+			return shf_launch(shf_jobs, shf_h[0], nchunks, max_S, max_S, max_r, kcap_v, kcap_h, s, shf_segments);
 		case 1u:
 			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
-				table, biome_count, s);
+				table, biome_count, s, noise_block);
 		case 2u:
 			return erode(s);
 		case 3u:
@@ -272,16 +279,58 @@ struct stpgb_batch {
 		}
 	}
 
-	// Autotuner: times each group's erosion launch with every candidate
+	// Autotuner: the filter's segment count and the noise kernel's block size
+	// (each candidate timed twice, the faster kept; every candidate gives the
+	// same output), then each group's erosion launch with every candidate
 	// variant (noise regenerates the heights before each trial, so every
-	// trial erodes the same map) and keeps the fastest per group.
+	// trial erodes the same map), keeping the fastest per group.
 	int autotune() {
 		cudaStream_t s;
 		STPGB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
 		cudaEvent_t e0, e1;
 		STPGB_CUDA_TRY(cudaEventCreate(&e0));
 		STPGB_CUDA_TRY(cudaEventCreate(&e1));
-		int rc = stage(0u, s);
+		int rc = STPGB_OK;
+		auto time_stage = [&](const uint32_t st, float& out) {
+			for (int rep = 0; rep < 3 && rc == STPGB_OK; rep++) {
+				cudaEventRecord(e0, s);
+				rc = stage(st, s);
+				cudaEventRecord(e1, s);
+				if (cudaStreamSynchronize(s) != cudaSuccess) {
+					rc = cuda_fail(cudaGetLastError(), "autotune");
+				}
+				float ms = 0.0f;
+				cudaEventElapsedTime(&ms, e0, e1);
+				if (rep > 0) { // the first run warms the caches and the code
+					out = rep == 1 ? ms : std::min(out, ms);
+				}
+			}
+		};
+		float best_shf = 0.0f;
+		uint32_t pick_seg = shf_segments;
+		for (uint32_t c = 0u; c < kShfSegCands && rc == STPGB_OK; c++) {
+			shf_segments = shf_seg_cands[c];
+			time_stage(0u, shf_tune_ms[c]);
+			if (rc == STPGB_OK && (best_shf == 0.0f || shf_tune_ms[c] < best_shf)) {
+				best_shf = shf_tune_ms[c];
+				pick_seg = shf_segments;
+			}
+		}
+		shf_segments = pick_seg;
+		if (rc == STPGB_OK) {
+			rc = stage(0u, s);
+		}
+		float best_noise = 0.0f;
+		uint32_t pick_block = noise_block;
+		for (uint32_t c = 0u; c < kNoiseBlockCands && rc == STPGB_OK; c++) {
+			noise_block = noise_block_cands[c];
+			time_stage(1u, noise_tune_ms[c]);
+			if (rc == STPGB_OK && (best_noise == 0.0f || noise_tune_ms[c] < best_noise)) {
+				best_noise = noise_tune_ms[c];
+				pick_block = noise_block;
+			}
+		}
+		noise_block = pick_block;
 		const uint32_t cands[6] = { 1u, 2u, 4u, 8u, 16u, 32u };
 		const uint32_t dcands[3] = { 1u, 2u, 4u };
 		for (uint32_t gi = 0u; gi < ngroups && rc == STPGB_OK; gi++) {
@@ -770,6 +819,26 @@ int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32
 		for (int c = 0; c < 36; c++) {
 			erosion_ms[c] = G.tune_ms[c];
 		}
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_tuning_stages(const stpgb_batch* b, uint32_t* shf_segments, float* shf_ms, uint32_t* noise_block,
+	float* noise_ms) {
+	if (!b) {
+		return inval("stpgb_batch_tuning_stages: null batch");
+	}
+	if (shf_segments) {
+		*shf_segments = b->shf_segments;
+	}
+	if (noise_block) {
+		*noise_block = b->noise_block;
+	}
+	for (uint32_t c = 0u; c < stpgb_batch::kShfSegCands && shf_ms; c++) {
+		shf_ms[c] = b->shf_tune_ms[c];
+	}
+	for (uint32_t c = 0u; c < stpgb_batch::kNoiseBlockCands && noise_ms; c++) {
+		noise_ms[c] = b->noise_tune_ms[c];
 	}
 	return STPGB_OK;
 }

@@ -78,7 +78,6 @@ struct FieldScratch {
 
 } // namespace
 
-int shf_launch(const ShfJob*, const ShfJob&, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, cudaStream_t);
 
 } // namespace stpgb
 

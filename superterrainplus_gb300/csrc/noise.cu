@@ -20,7 +20,9 @@ namespace {
 
 constexpr uint32_t kNoiseBlock = 256u;
 
-__global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob* __restrict__ jobs,
+// one pixel per thread; the block size (128, 256 or 512) is the batch tuner's choice
+template<uint32_t Block>
+__global__ void __launch_bounds__(Block) multibiome_kernel(const NoiseJob* __restrict__ jobs,
 	const NoiseJob single, const stpgb_permutation perm, const stpgb_biome_property* __restrict__ table,
 	const uint32_t biome_count) {
 	__shared__ uint8_t sperm[512];
@@ -30,7 +32,7 @@ __global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob*
 
 	const NoiseJob& J = jobs ? jobs[blockIdx.y] : single;
 	const uint64_t npix = static_cast<uint64_t>(J.W) * J.H;
-	const uint64_t idx = static_cast<uint64_t>(blockIdx.x) * kNoiseBlock + threadIdx.x;
+	const uint64_t idx = static_cast<uint64_t>(blockIdx.x) * Block + threadIdx.x;
 	if (idx >= npix) {
 		return;
 	}
@@ -59,9 +61,23 @@ __global__ void __launch_bounds__(kNoiseBlock) multibiome_kernel(const NoiseJob*
 } // namespace
 
 int noise_launch(const NoiseJob* jobs, const NoiseJob& single, uint32_t njobs, uint64_t max_pixels,
-	const stpgb_permutation& perm, const stpgb_biome_property* table, uint32_t biome_count, cudaStream_t stream) {
-	const dim3 grid(static_cast<uint32_t>((max_pixels + kNoiseBlock - 1u) / kNoiseBlock), njobs);
-	multibiome_kernel<<<grid, kNoiseBlock, 0, stream>>>(jobs, single, perm, table, biome_count);
+	const stpgb_permutation& perm, const stpgb_biome_property* table, uint32_t biome_count, cudaStream_t stream,
+	const uint32_t block) {
+	const uint32_t b = block == 0u ? kNoiseBlock : block;
+	const dim3 grid(static_cast<uint32_t>((max_pixels + b - 1u) / b), njobs);
+	switch (b) {
+	case 128u:
+		multibiome_kernel<128u><<<grid, 128u, 0, stream>>>(jobs, single, perm, table, biome_count);
+		break;
+	case 256u:
+		multibiome_kernel<256u><<<grid, 256u, 0, stream>>>(jobs, single, perm, table, biome_count);
+		break;
+	case 512u:
+		multibiome_kernel<512u><<<grid, 512u, 0, stream>>>(jobs, single, perm, table, biome_count);
+		break;
+	default:
+		return inval("noise_launch: block size must be 128, 256 or 512");
+	}
 	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }

@@ -582,7 +582,7 @@ ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
 }
 
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
-	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream) {
+	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, const uint32_t segments_wanted) {
 	STPGB_TRY(once_per_device(SETUP_SHF_SMEM, shf_set_smem_attributes));
 	const uint64_t target_threads = uint64_t { current_sm_count() } * kShfThreadsPerSM;
 	// Segments per column / row: enough threads to fill the GPU when few
@@ -592,6 +592,9 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	// slower; on one chunk, 16 make it several times faster).
 	const uint64_t ncols = static_cast<uint64_t>(max_W) + 2u * max_r;
 	auto segments = [&](const uint64_t lanes, const uint32_t len) {
+		if (segments_wanted != 0u) {
+			return std::max(1u, std::min({ segments_wanted, kShfMaxSegments, std::max(len, 1u) }));
+		}
 		const uint64_t want = (target_threads + lanes * njobs - 1u) / (lanes * njobs);
 		if (want < 4u) {
 			return 1u;

@@ -44,7 +44,9 @@ uint32_t shf_kcap_h(uint32_t r, uint32_t max_items);
 
 // Runs the whole filter for `njobs` jobs (device array `jobs`, or `single`
 // when jobs == nullptr). max_W/max_H/max_r bound the grids.
+// `segments`: columns and rows cut into this many segments (clamped to
+// [1, kShfMaxSegments] and the slide length); 0 = chosen from the launch size.
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
-	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream);
+	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, uint32_t segments = 0u);
 
 } // namespace stpgb

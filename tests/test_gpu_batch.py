@@ -39,8 +39,16 @@ def heights(b):
     return out, fixed, res
 
 
-def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle):
+@pytest.mark.parametrize("tune", [False, True])
+def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, tune):
+    """Inputs bit-exact, heights within 2e-6 of the oracle, with the default filter segments and
+    noise block or with the autotuner's choice of both (every candidate was timed)."""
     b, table = make_batch(stpgb)
+    if tune:
+        b.tune()
+        seg, seg_ms, block, block_ms = b.tuning_stages()
+        assert set(seg_ms) == {0, 1, 2, 4, 8, 16} and seg in seg_ms
+        assert set(block_ms) == {128, 256, 512} and block in block_ms
     regions = [np.zeros((5 * r["MapSize"], 5 * r["MapSize"]), np.uint16) for r in REQS]
     starts = [np.zeros(2 * r["DropletCount"], np.float32) for r in REQS]
     b.download_inputs(regions, starts)
