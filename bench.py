@@ -586,6 +586,7 @@ def run_ours(args):
                          "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
                          "noise_block": stage_tune[2],
                          "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()},
+                         "erosion_coop_jobs_interleaved": stage_tune[4],
                          "erosion_lanes_per_droplet": lanes[0], "erosion_droplets_per_group": lanes[1],
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v

@@ -729,10 +729,11 @@ STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_d
 /* The autotuner's choices for the other stages: the filter's segment count
  * (0 = chosen from the launch size) with its time in ms for the candidates
  * 0, 1, 2, 4, 8, 16 (6 floats), and the noise kernel's block size with its
- * time for 128, 256, 512 threads (3 floats); 0 ms = not tried.  Any output
- * pointer may be NULL. */
+ * time for 128, 256, 512 threads (3 floats); 0 ms = not tried; and, where the
+ * dominant erosion group runs the warp-cooperative kernel, the number of jobs
+ * whose blocks it interleaves (else 0).  Any output pointer may be NULL. */
 STPGB_API int stpgb_batch_tuning_stages(const stpgb_batch* batch, uint32_t* shf_segments, float* shf_ms,
-	uint32_t* noise_block, float* noise_ms);
+	uint32_t* noise_block, float* noise_ms, uint32_t* coop_interleave);
 
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */

@@ -516,12 +516,13 @@ class Batch:
 
     def tuning_stages(self):
         """The autotuner's filter segment count (0 = from the launch size) and noise block size,
-        with {candidate: ms} for each (candidates not tried are left out)."""
-        seg, blk = C.c_uint32(0), C.c_uint32(0)
+        with {candidate: ms} for each (candidates not tried are left out), and the jobs the
+        warp-cooperative erosion kernel interleaves (0 where the dominant group runs another)."""
+        seg, blk, q = C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
         sms, nms = (C.c_float * 6)(), (C.c_float * 3)()
-        check(lib().stpgb_batch_tuning_stages(self._h, C.byref(seg), sms, C.byref(blk), nms))
+        check(lib().stpgb_batch_tuning_stages(self._h, C.byref(seg), sms, C.byref(blk), nms, C.byref(q)))
         return (seg.value, {c: sms[i] for i, c in enumerate((0, 1, 2, 4, 8, 16)) if sms[i] > 0},
-                blk.value, {c: nms[i] for i, c in enumerate((128, 256, 512)) if nms[i] > 0})
+                blk.value, {c: nms[i] for i, c in enumerate((128, 256, 512)) if nms[i] > 0}, q.value)
 
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)

@@ -77,6 +77,9 @@ struct ErosionGroup {
 	uint32_t lanes = 8u; // lanes per droplet
 	uint32_t dpg = 1u;   // droplets per lane group
 	bool rows = true;    // brush rows in 16-byte blocks
+	// warp-cooperative kernel: jobs interleaved beyond erosion_coop_interleave's
+	// rule (the autotuner's choice; more jobs keep fewer droplets of each in flight)
+	uint32_t interleave_extra = 0u;
 	// autotuner's erosion time per candidate, [rows 0, 1][lanes 1..32][droplets 1, 2, 4] (0 = not tried)
 	float tune_ms[36] = {};
 
@@ -106,7 +109,11 @@ struct ErosionGroup {
 	int launch(cudaStream_t s) const {
 		return erosion_launch(jobs, h[0], static_cast<uint32_t>(h.size()), max_count, max_brush, s, lanes, false, dpg,
 			rows, erosion_rows_wide(min_radius), erosion_rows_atomic(min_radius, lanes),
-			erosion_coop_interleave(h.data(), static_cast<uint32_t>(h.size())));
+			coop_interleave());
+	}
+
+	uint32_t coop_interleave() const {
+		return erosion_coop_interleave(h.data(), static_cast<uint32_t>(h.size())) + interleave_extra;
 	}
 };
 
@@ -336,7 +343,8 @@ struct stpgb_batch {
 		for (uint32_t gi = 0u; gi < ngroups && rc == STPGB_OK; gi++) {
 			ErosionGroup& G = grp[gi];
 			float best = 0.0f;
-			uint32_t best_lanes = G.lanes, best_dpg = G.dpg;
+			uint32_t best_lanes = G.lanes, best_dpg = G.dpg, best_extra = 0u;
+			G.interleave_extra = 0u;
 			bool best_rows = G.rows;
 			for (int c = 0; c < 36 && rc == STPGB_OK; c++) {
 				const bool cr = c >= 18;
@@ -384,6 +392,37 @@ struct stpgb_batch {
 			G.lanes = best_lanes;
 			G.dpg = best_dpg;
 			G.rows = best_rows;
+			// the warp-cooperative kernel over several jobs: also with 1, 2 and 4 more
+			// jobs interleaved than the rule gives (up to every job of the group)
+			if (rc == STPGB_OK && G.rows && G.lanes == 1u && G.dpg == 1u) {
+				const uint32_t base_q = G.coop_interleave();
+				for (const uint32_t extra : { 1u, 2u, 4u }) {
+					if (base_q + extra > G.h.size() || rc != STPGB_OK) {
+						break;
+					}
+					G.interleave_extra = extra;
+					float t = 0.0f;
+					for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {
+						rc = stage(1u, s);
+						if (rc == STPGB_OK) {
+							cudaEventRecord(e0, s);
+							rc = G.launch(s);
+							cudaEventRecord(e1, s);
+						}
+						if (cudaStreamSynchronize(s) != cudaSuccess) {
+							rc = cuda_fail(cudaGetLastError(), "autotune");
+						}
+						float ms = 0.0f;
+						cudaEventElapsedTime(&ms, e0, e1);
+						t = rep == 0 ? ms : std::min(t, ms);
+					}
+					if (rc == STPGB_OK && t < best) {
+						best = t;
+						best_extra = extra;
+					}
+				}
+				G.interleave_extra = best_extra;
+			}
 		}
 		cudaEventDestroy(e0);
 		cudaEventDestroy(e1);
@@ -824,9 +863,13 @@ int stpgb_batch_tuning(const stpgb_batch* b, uint32_t* lanes_per_droplet, uint32
 }
 
 int stpgb_batch_tuning_stages(const stpgb_batch* b, uint32_t* shf_segments, float* shf_ms, uint32_t* noise_block,
-	float* noise_ms) {
+	float* noise_ms, uint32_t* coop_interleave) {
 	if (!b) {
 		return inval("stpgb_batch_tuning_stages: null batch");
+	}
+	if (coop_interleave) {
+		const ErosionGroup& G = b->dominant();
+		*coop_interleave = G.rows && G.lanes == 1u && G.dpg == 1u ? G.coop_interleave() : 0u;
 	}
 	if (shf_segments) {
 		*shf_segments = b->shf_segments;

@@ -46,7 +46,7 @@ def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, tune):
     b, table = make_batch(stpgb)
     if tune:
         b.tune()
-        seg, seg_ms, block, block_ms = b.tuning_stages()
+        seg, seg_ms, block, block_ms, _ = b.tuning_stages()
         assert set(seg_ms) == {0, 1, 2, 4, 8, 16} and seg in seg_ms
         assert set(block_ms) == {128, 256, 512} and block in block_ms
     regions = [np.zeros((5 * r["MapSize"], 5 * r["MapSize"]), np.uint16) for r in REQS]
