@@ -392,11 +392,11 @@ struct stpgb_batch {
 			G.lanes = best_lanes;
 			G.dpg = best_dpg;
 			G.rows = best_rows;
-			// the warp-cooperative kernel over several jobs: also with 1, 2 and 4 more
-			// jobs interleaved than the rule gives (up to every job of the group)
+			// the warp-cooperative kernel over several jobs: also with 1, 2, 4, 8 and 12
+			// more jobs interleaved than the rule gives (up to every job of the group)
 			if (rc == STPGB_OK && G.rows && G.lanes == 1u && G.dpg == 1u) {
 				const uint32_t base_q = G.coop_interleave();
-				for (const uint32_t extra : { 1u, 2u, 4u }) {
+				for (const uint32_t extra : { 1u, 2u, 4u, 8u, 12u }) {
 					if (base_q + extra > G.h.size() || rc != STPGB_OK) {
 						break;
 					}

@@ -142,15 +142,15 @@ def test_batch_with_layer_chain_biomes(stpgb, dev, oracle):
 
 
 def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
-    """The headline path: four production requests (3x3 x 512^2, 8 biomes, filter radius 32, 600,000
-    droplets, brush 4, lifetime 50) through the autotuned graph, whatever erosion variant and job
-    interleaving the tuner settles on.  Request 0's eroded neighbourhood stays within the band of the
+    """The headline path: the bench's sixteen production requests (3x3 x 512^2, 8 biomes, filter radius
+    32, 600,000 droplets, brush 4, lifetime 50) through the autotuned graph, whatever erosion variant
+    and job interleaving the tuner settles on (up to all sixteen jobs).  Request 0's eroded neighbourhood stays within the band of the
     reference's own erosion kernel built for sm_103a around the FP64 serial result (five runs on the
     same map with the same droplets: its worst RMS plus its run-to-run spread)."""
     from test_gpu_erosion import rms
     S, count = 512, 600000
     reqs = [dict(MapSize=S, ChunkX=4 * n, ChunkY=0, InterpolationRadius=32, DropletCount=count, BrushRadius=4,
-                 Lifetime=50) for n in range(4)]
+                 Lifetime=50) for n in range(16)]
     base = stpgb.RaindropSetting(**helpers.raindrop_dict(count, radius=4, lifetime=50, seed=42))
     b = stpgb.Batch(reqs, base, stpgb.SimplexSetting(42, 8, 0.2181661565), helpers.biome_table(8, 42), graph=True)
     b.synthesize(192, 42)
@@ -159,7 +159,7 @@ def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
     b.run_stage(1)
     before = [np.zeros((3 * S, 3 * S), np.float32) for _ in reqs]
     b.download(before)
-    starts = [np.zeros(2 * count, np.float32) if n == 0 else None for n in range(4)]
+    starts = [np.zeros(2 * count, np.float32) if n == 0 else None for n in range(16)]
     b.download_inputs(starts=starts)
     b.status()
     b.run()
