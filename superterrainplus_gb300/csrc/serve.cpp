@@ -797,11 +797,13 @@ struct stpgb_server {
 			STPGB_TRY(starts_jobs_launch(sts_dev + L.b, n, maxCount, this->base.Seed, s));
 			// brush rows in 16-byte blocks (pool blocks are 256-byte aligned,
 			// pitches 3 * MapSize); each job reads several blocks per round trip
-			// where few of its droplets are in flight per pixel
+			// where few of its droplets are in flight per pixel; the
+			// warp-cooperative kernel alternates the blocks of every job of its
+			// group (the batch autotuner's choice for sixteen 512^2 jobs)
 			for (const ErosionGroup& g : L.groups) {
 				STPGB_TRY(erosion_launch(reinterpret_cast<ErosionJob*>(sl.dev + o_ero) + g.first, ero[g.first], g.n,
 					g.maxCount, g.maxBrush, s, g.ec.lanes, false, g.dpg, g.ec.rows, erosion_rows_wide(g.minRadius),
-					erosion_rows_atomic(g.minRadius, g.ec.lanes)));
+					erosion_rows_atomic(g.minRadius, g.ec.lanes), g.n));
 			}
 			if (in_place()) {
 				// the eroded neighbourhoods go back into the resident chunks
