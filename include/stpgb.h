@@ -255,6 +255,14 @@ STPGB_API int stpgb_shf_filter_host(const uint16_t* samplemap_host, const stpgb_
 	uint32_t radius, uint32_t* offsets_host, stpgb_bin* bins_host, uint64_t bins_capacity,
 	uint64_t* nbins);
 
+/* No counterpart in the reference.  The path the last stpgb_shf_filter call
+ * with this workspace (and the same nn, radius, max_items) took for its chunk:
+ * `*path` = 1 when the chunk's read region ((H+2r) x (W+2r) samples) held at
+ * most 8 distinct values and the few-values kernels filtered it, 0 when the
+ * sequential slides did.  Both give the same output.  Synchronises `stream`. */
+STPGB_API int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items,
+	const void* workspace, uint32_t* path, void* stream);
+
 /* Reads and decodes a device status word written by the kernels
  * (synchronises `stream`).  Returns STPGB_OK, STPGB_ECAPACITY or STPGB_ETIMEOUT. */
 STPGB_API int stpgb_status_check(const uint32_t* status, void* stream);

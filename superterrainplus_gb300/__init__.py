@@ -565,6 +565,22 @@ class DeviceOps:
                                      C.c_void_p(bins.data_ptr()), cap, C.c_void_p(status.data_ptr()), self._stream()))
         return offsets, bins, status
 
+    def shf_filter_path(self, workspace, map_size, nn, radius, max_items=0):
+        """1 if the last shf_filter call with `workspace` took the few-values path (at most 8
+        distinct values in the chunk's read region), 0 if the sequential slides."""
+        info = NNInfo.make(map_size, nn)
+        path = C.c_uint32(0)
+        check(lib().stpgb_shf_filter_path(C.byref(info), radius, max_items, C.c_void_p(workspace.data_ptr()),
+                                          C.byref(path), self._stream()))
+        return path.value
+
+    def shf_workspace(self, map_size, nn, radius, max_items=0):
+        """A device workspace of stpgb_shf_workspace_size bytes."""
+        info = NNInfo.make(map_size, nn)
+        ws = C.c_size_t(0)
+        check(lib().stpgb_shf_workspace_size(C.byref(info), radius, max_items, C.byref(ws)))
+        return self.empty(max(ws.value, 1), self.torch.uint8)
+
     def status_check(self, status):
         check(lib().stpgb_status_check(C.c_void_p(status.data_ptr()), self._stream()))
 

@@ -591,9 +591,7 @@ int stpgb_batch_create(const stpgb_batch_request* requests, uint32_t count, cons
 			j.sy = S;
 			j.r = r.InterpolationRadius;
 			j.kcap_v = b->kcap_v;
-			j.vbuf = reinterpret_cast<uint32_t*>(m + L.shf_ws[c] + sl.vbuf);
-			j.vn = reinterpret_cast<uint16_t*>(m + L.shf_ws[c] + sl.vn);
-			j.rows = reinterpret_cast<uint32_t*>(m + L.shf_ws[c] + sl.rows);
+			shf_bind_workspace(j, m + L.shf_ws[c], sl);
 			j.offsets = reinterpret_cast<uint32_t*>(m + L.offsets[c]);
 			j.bins = reinterpret_cast<stpgb_bin*>(m + L.bins[c]);
 			j.bins_capacity = L.bins_cap;

@@ -646,9 +646,7 @@ struct stpgb_server {
 			sj.sx = sj.sy = S;
 			sj.r = k.r;
 			sj.kcap_v = kv;
-			sj.vbuf = reinterpret_cast<uint32_t*>(ws + l.vbuf);
-			sj.vn = reinterpret_cast<uint16_t*>(ws + l.vn);
-			sj.rows = reinterpret_cast<uint32_t*>(ws + l.rows);
+			shf_bind_workspace(sj, ws, l);
 			sj.offsets = offsets;
 			sj.bins = bins;
 			sj.bins_capacity = cap;

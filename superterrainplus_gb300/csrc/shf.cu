@@ -65,6 +65,9 @@ constexpr uint32_t kResolved = 0x80000000u;
 __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict__ jobs, const ShfJob single,
 	const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
+	if (shf_job_fast(J)) {
+		return; // filtered by the few-values path
+	}
 	const uint32_t ncols = J.W + 2u * J.r;
 	const uint32_t t = blockIdx.x * kVBlock + threadIdx.x;
 	const uint32_t k = t % ncols, s = t / ncols;
@@ -214,6 +217,9 @@ template<bool Write>
 __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restrict__ jobs, const ShfJob single,
 	const uint32_t kcap_v, const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
+	if (shf_job_fast(J)) {
+		return;
+	}
 	const uint32_t t = blockIdx.x * kHBlock + threadIdx.x;
 	const uint32_t y = t % J.H, s = t / J.H;
 	const uint32_t x_a = s * seg_len;
@@ -497,10 +503,12 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 }
 
 // One block per job: rows[0..H*segs) (row-major over row, segment) ->
-// exclusive prefix, rows[H*segs] = total; offsets[W*H] = total.
+// exclusive prefix, rows[H*segs] = total; offsets[W*H] = total.  A job of
+// the few-values path has one count per row (segs = 1).
 __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t segs) {
+	const uint32_t segs_slide) {
 	const ShfJob& J = pick(jobs, single);
+	const uint32_t segs = shf_job_fast(J) ? 1u : segs_slide;
 	const uint32_t slots = J.H * segs;
 	__shared__ uint64_t warp_sum[kScanBlock / 32u];
 	__shared__ uint64_t carry_s;
@@ -577,8 +585,17 @@ ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
 	l.vbuf = 0u;
 	l.vn = align256(static_cast<size_t>(H) * kcap_v * ncols * sizeof(uint32_t));
 	l.rows = l.vn + align256(static_cast<size_t>(H) * ncols * sizeof(uint16_t));
-	l.total = l.rows + align256((static_cast<size_t>(H) * kShfMaxSegments + 1u) * sizeof(uint32_t));
+	l.fast = l.rows + align256((static_cast<size_t>(H) * kShfMaxSegments + 1u) * sizeof(uint32_t));
+	const size_t tiles = (static_cast<size_t>(H) + 2u * r + kShfPaletteRows - 1u) / kShfPaletteRows;
+	l.total = l.fast + align256((1u + tiles) * sizeof(ShfFastRecord));
 	return l;
+}
+
+void shf_bind_workspace(ShfJob& job, unsigned char* ws, const ShfLayout& l) {
+	job.vbuf = reinterpret_cast<uint32_t*>(ws + l.vbuf);
+	job.vn = reinterpret_cast<uint16_t*>(ws + l.vn);
+	job.rows = reinterpret_cast<uint32_t*>(ws + l.rows);
+	job.fast = reinterpret_cast<uint32_t*>(ws + l.fast);
 }
 
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
@@ -608,6 +625,12 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 		+ 12u * kHBlock) * sizeof(uint32_t);
 	const dim3 vgrid(static_cast<uint32_t>((ncols * segs_v + kVBlock - 1u) / kVBlock), njobs);
 	const dim3 hgrid(static_cast<uint32_t>((static_cast<uint64_t>(max_H) * segs_h + kHBlock - 1u) / kHBlock), njobs);
+	// Every job first takes the palette of its read region: at most
+	// kShfFastItems values go the few-values path (shf_fast.cu), the others
+	// the sequential slides; each kernel returns at once for jobs of the other.
+	const ShfFastLaunch fast = shf_fast_config(njobs, max_W, max_H, max_r);
+	STPGB_TRY(shf_fast_prepare(jobs, single, njobs, max_W, max_H, max_r, kcap_h, fast, stream));
+	STPGB_TRY(shf_fast_pass(jobs, single, njobs, fast, false, stream));
 	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v, segs_v, len_v);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	shf_horizontal<false><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
@@ -616,6 +639,7 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	STPGB_CUDA_TRY(cudaGetLastError());
 	shf_horizontal<true><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
 	STPGB_CUDA_TRY(cudaGetLastError());
+	STPGB_TRY(shf_fast_pass(jobs, single, njobs, fast, true, stream));
 	return STPGB_OK;
 }
 
@@ -696,14 +720,32 @@ int stpgb_shf_filter(const uint16_t* samplemap, const stpgb_nn_info* nn, uint32_
 	job.sy = sy;
 	job.r = radius;
 	job.kcap_v = kv;
-	job.vbuf = reinterpret_cast<uint32_t*>(ws + l.vbuf);
-	job.vn = reinterpret_cast<uint16_t*>(ws + l.vn);
-	job.rows = reinterpret_cast<uint32_t*>(ws + l.rows);
+	shf_bind_workspace(job, ws, l);
 	job.offsets = offsets;
 	job.bins = bins;
 	job.bins_capacity = bins_capacity;
 	job.status = status;
 	return shf_launch(nullptr, job, 1u, W, H, radius, kv, kh, s);
+}
+
+int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items, const void* workspace,
+	uint32_t* path, void* stream) {
+	uint32_t sx, sy;
+	STPGB_TRY(check_shf_args(nn, radius, max_items, sx, sy));
+	if (!workspace || !path) {
+		return inval("stpgb_shf_filter_path: null workspace or result");
+	}
+	if (max_items == 0u) {
+		max_items = kShfMaxItems;
+	}
+	const ShfLayout l = shf_layout(nn->MapSize[0], nn->MapSize[1], radius, shf_kcap_v(radius, max_items));
+	ShfFastRecord rec {};
+	const cudaStream_t s = as_stream(stream);
+	STPGB_CUDA_TRY(cudaMemcpyAsync(&rec, static_cast<const unsigned char*>(workspace) + l.fast, sizeof(rec),
+		cudaMemcpyDeviceToHost, s));
+	STPGB_CUDA_TRY(cudaStreamSynchronize(s));
+	*path = rec.mode == kShfModeFast ? 1u : 0u;
+	return STPGB_OK;
 }
 
 int stpgb_status_check(const uint32_t* status, void* stream) {

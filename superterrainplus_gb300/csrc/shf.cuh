@@ -26,6 +26,7 @@ struct ShfJob {
 	uint32_t* vbuf;  // [W+2r][kcap_v][H] packed (item << 16 | count), column-major
 	uint16_t* vn;    // [W+2r][H] entries per vertical histogram
 	uint32_t* rows;  // [H*segments+1] bins per (row, segment), then exclusive prefix + total
+	uint32_t* fast;  // [8] path record (ShfFastRecord), then [palette tiles][8] palette slots
 	// output
 	uint32_t* offsets;  // [W*H+1]
 	stpgb_bin* bins;
@@ -33,12 +34,39 @@ struct ShfJob {
 	uint32_t* status;
 };
 
+// The few-values path (shf_fast.cu) filters a chunk whose read region holds
+// at most kShfFastItems distinct sample values; other chunks take the
+// sequential slides.  Its vertical states at band starts overlay `vbuf`,
+// which that chunk does not use.
+constexpr uint32_t kShfFastItems = 8u;
+constexpr uint32_t kShfModeSlide = 0u, kShfModeFast = 1u;
+// Rows of the read region per palette tile, and at most this many columns
+// (W + 2r) on the few-values path (its per-row tables live in shared memory).
+constexpr uint32_t kShfPaletteRows = 32u;
+constexpr uint32_t kShfFastMaxCols = 4096u;
+// Fewest output rows per band of the few-values path.
+constexpr uint32_t kShfFastMinBandRows = 4u;
+
+// Record of the path a job takes, written by the palette merge: words
+// {mode, distinct values, 0, 0, then the values as 8 uint16, ascending}.
+struct ShfFastRecord {
+	uint32_t mode, count, pad0, pad1;
+	uint16_t item[kShfFastItems];
+};
+static_assert(sizeof(ShfFastRecord) == 32u, "record is 8 words");
+
+__device__ __forceinline__ bool shf_job_fast(const ShfJob& J) {
+	return reinterpret_cast<const ShfFastRecord*>(J.fast)->mode == kShfModeFast;
+}
+
 struct ShfLayout {
-	size_t vbuf, vn, rows, total;
+	size_t vbuf, vn, rows, fast, total;
 };
 
 // Workspace layout for one job (256-byte aligned sub-buffers).
 ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v);
+// Points the job's workspace fields at the sub-buffers of `ws` (laid out by shf_layout).
+void shf_bind_workspace(ShfJob& job, unsigned char* ws, const ShfLayout& l);
 uint32_t shf_kcap_v(uint32_t r, uint32_t max_items);
 uint32_t shf_kcap_h(uint32_t r, uint32_t max_items);
 
@@ -48,5 +76,18 @@ uint32_t shf_kcap_h(uint32_t r, uint32_t max_items);
 // [1, kShfMaxSegments] and the slide length); 0 = chosen from the launch size.
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
 	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, uint32_t segments = 0u);
+
+// The few-values path's launches around the sequential slides: palette and
+// vertical band states, then the bin count per row (before the row scan), and
+// the write pass (after it).  Jobs that do not qualify return at once.
+struct ShfFastLaunch {
+	uint32_t band_rows, bands, threads, cols_per_thread, max_cols;
+	size_t smem;
+};
+ShfFastLaunch shf_fast_config(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
+int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
+	uint32_t max_r, uint32_t kcap_h, const ShfFastLaunch& cfg, cudaStream_t stream);
+int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, const ShfFastLaunch& cfg, bool write,
+	cudaStream_t stream);
 
 } // namespace stpgb
