@@ -257,11 +257,20 @@ STPGB_API int stpgb_shf_filter_host(const uint16_t* samplemap_host, const stpgb_
 
 /* No counterpart in the reference.  The path the last stpgb_shf_filter call
  * with this workspace (and the same nn, radius, max_items) took for its chunk:
- * `*path` = 1 when the chunk's read region ((H+2r) x (W+2r) samples) held at
- * most 8 distinct values and the few-values kernels filtered it, 0 when the
- * sequential slides did.  Both give the same output.  Synchronises `stream`. */
+ * `*path` = 0 when the general sequential slides filtered it; 1 or 2 when the
+ * chunk's read region ((H+2r) x (W+2r) samples) held at most 8 distinct
+ * values and the few-values kernels did: 1 their packed sequential slides
+ * (launches of many chunks), 2 their row bands (launches of few).  All give
+ * the same output.  Synchronises `stream`. */
 STPGB_API int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max_items,
 	const void* workspace, uint32_t* path, void* stream);
+
+/* No counterpart in the reference.  Process-wide choice of the filter's path
+ * for every later launch (tuning and diagnostics): 0 = by chunk and launch
+ * size (the default), 1 = few-values packed slides, 2 = few-values row
+ * bands (chunks of more than 4096 - 2r columns still take the general
+ * slides), 3 = the general slides for every chunk.  STPGB_EINVAL above 3. */
+STPGB_API int stpgb_shf_set_path(uint32_t path);
 
 /* Reads and decodes a device status word written by the kernels
  * (synchronises `stream`).  Returns STPGB_OK, STPGB_ECAPACITY or STPGB_ETIMEOUT. */

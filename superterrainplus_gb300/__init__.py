@@ -566,13 +566,20 @@ class DeviceOps:
         return offsets, bins, status
 
     def shf_filter_path(self, workspace, map_size, nn, radius, max_items=0):
-        """1 if the last shf_filter call with `workspace` took the few-values path (at most 8
-        distinct values in the chunk's read region), 0 if the sequential slides."""
+        """The path the last shf_filter call with `workspace` took: 0 the general slides, 1 the
+        few-values packed slides, 2 the few-values row bands (at most 8 distinct values in the
+        chunk's read region)."""
         info = NNInfo.make(map_size, nn)
         path = C.c_uint32(0)
         check(lib().stpgb_shf_filter_path(C.byref(info), radius, max_items, C.c_void_p(workspace.data_ptr()),
                                           C.byref(path), self._stream()))
         return path.value
+
+    @staticmethod
+    def shf_set_path(path):
+        """Process-wide filter path for later launches: 0 by size, 1 packed slides, 2 row bands,
+        3 general slides."""
+        check(lib().stpgb_shf_set_path(path))
 
     def shf_workspace(self, map_size, nn, radius, max_items=0):
         """A device workspace of stpgb_shf_workspace_size bytes."""

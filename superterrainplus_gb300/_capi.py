@@ -192,6 +192,7 @@ PROTOTYPES = {
     "stpgb_shf_filter_host": (C.c_int, [vp, C.POINTER(NNInfo), u32, vp, vp, u64, C.POINTER(u64)]),
     "stpgb_shf_filter_noalloc": (C.c_int, [vp, C.POINTER(NNInfo), u32, u32, vp, vp, u64, vp, vp]),
     "stpgb_shf_filter_path": (C.c_int, [C.POINTER(NNInfo), u32, u32, vp, C.POINTER(u32), vp]),
+    "stpgb_shf_set_path": (C.c_int, [u32]),
     "stpgb_status_check": (C.c_int, [vp, vp]),
     "stpgb_multibiome_heightmap": (C.c_int, [vp, u32, vp, vp, u32, u32, f32, f32, C.POINTER(Permutation), vp,
                                              u32, vp]),

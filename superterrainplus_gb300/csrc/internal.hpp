@@ -39,7 +39,7 @@ inline cudaStream_t as_stream(void* s) {
 uint32_t current_sm_count();
 
 // Keys of one-time per-device set-up steps (function attributes are per device).
-enum : unsigned { SETUP_SHF_SMEM = 0u, SETUP_SHF_FAST_SMEM = 1u };
+enum : unsigned { SETUP_SHF_SMEM = 0u, SETUP_SHF_BAND_SMEM = 1u };
 
 // Runs `setup` on the current device the first time `key` is asked for there and it succeeds;
 // serialised under a lock, so concurrent first calls from several host threads set up once.

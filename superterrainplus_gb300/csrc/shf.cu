@@ -29,6 +29,7 @@
 #include "shf.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace stpgb {
 
@@ -579,6 +580,14 @@ uint32_t shf_kcap_h(uint32_t r, uint32_t max_items) {
 	return static_cast<uint32_t>(std::min<uint64_t>((side + 1u) * side, max_items));
 }
 
+namespace {
+std::atomic<uint32_t> g_shf_path { 0u };
+} // namespace
+
+uint32_t shf_path_override() {
+	return g_shf_path.load();
+}
+
 ShfLayout shf_layout(uint32_t W, uint32_t H, uint32_t r, uint32_t kcap_v) {
 	const size_t ncols = static_cast<size_t>(W) + 2u * r;
 	ShfLayout l;
@@ -628,9 +637,9 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	// Every job first takes the palette of its read region: at most
 	// kShfFastItems values go the few-values path (shf_fast.cu), the others
 	// the sequential slides; each kernel returns at once for jobs of the other.
-	const ShfFastLaunch fast = shf_fast_config(njobs, max_W, max_H, max_r);
+	const ShfFastPlan fast = shf_fast_plan(njobs, max_W, max_H, max_r);
 	STPGB_TRY(shf_fast_prepare(jobs, single, njobs, max_W, max_H, max_r, kcap_h, fast, stream));
-	STPGB_TRY(shf_fast_pass(jobs, single, njobs, fast, false, stream));
+	STPGB_TRY(shf_fast_pass(jobs, single, njobs, max_H, fast, false, stream));
 	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v, segs_v, len_v);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	shf_horizontal<false><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
@@ -639,7 +648,7 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	STPGB_CUDA_TRY(cudaGetLastError());
 	shf_horizontal<true><<<hgrid, kHBlock, hsmem, stream>>>(jobs, single, kcap_v, kcap_h, segs_h, len_h);
 	STPGB_CUDA_TRY(cudaGetLastError());
-	STPGB_TRY(shf_fast_pass(jobs, single, njobs, fast, true, stream));
+	STPGB_TRY(shf_fast_pass(jobs, single, njobs, max_H, fast, true, stream));
 	return STPGB_OK;
 }
 
@@ -744,7 +753,15 @@ int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max
 	STPGB_CUDA_TRY(cudaMemcpyAsync(&rec, static_cast<const unsigned char*>(workspace) + l.fast, sizeof(rec),
 		cudaMemcpyDeviceToHost, s));
 	STPGB_CUDA_TRY(cudaStreamSynchronize(s));
-	*path = rec.mode == kShfModeFast ? 1u : 0u;
+	*path = rec.mode == kShfModeFast ? rec.pad0 : 0u;
+	return STPGB_OK;
+}
+
+int stpgb_shf_set_path(uint32_t path) {
+	if (path > 3u) {
+		return inval("stpgb_shf_set_path: 0 (by size), 1 (packed slides), 2 (row bands) or 3 (general slides)");
+	}
+	g_shf_path.store(path);
 	return STPGB_OK;
 }
 

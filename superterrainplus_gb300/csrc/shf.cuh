@@ -34,18 +34,19 @@ struct ShfJob {
 	uint32_t* status;
 };
 
-// The few-values path (shf_fast.cu) filters a chunk whose read region holds
-// at most kShfFastItems distinct sample values; other chunks take the
-// sequential slides.  Its vertical states at band starts overlay `vbuf`,
-// which that chunk does not use.
+// The few-values path (shf_fast.cu, shf_band.cu) filters a chunk whose read
+// region holds at most kShfFastItems distinct sample values; other chunks
+// take the general slides.  Its packed vertical histograms (12 bytes per
+// column and row, or per band) overlay `vbuf`, which that chunk does not
+// otherwise use.
 constexpr uint32_t kShfFastItems = 8u;
 constexpr uint32_t kShfModeSlide = 0u, kShfModeFast = 1u;
-// Rows of the read region per palette tile, and at most this many columns
-// (W + 2r) on the few-values path (its per-row tables live in shared memory).
+// Rows of the read region per palette tile.
 constexpr uint32_t kShfPaletteRows = 32u;
-constexpr uint32_t kShfFastMaxCols = 4096u;
-// Fewest output rows per band of the few-values path.
-constexpr uint32_t kShfFastMinBandRows = 4u;
+// The row-band formulation keeps a row's tables in shared memory: at most
+// this many columns (W + 2r), bands of at least this many rows.
+constexpr uint32_t kShfBandMaxCols = 4096u;
+constexpr uint32_t kShfBandMinRows = 4u;
 
 // Record of the path a job takes, written by the palette merge: words
 // {mode, distinct values, 0, 0, then the values as 8 uint16, ascending}.
@@ -77,17 +78,35 @@ uint32_t shf_kcap_h(uint32_t r, uint32_t max_items);
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
 	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, uint32_t segments = 0u);
 
-// The few-values path's launches around the sequential slides: palette and
-// vertical band states, then the bin count per row (before the row scan), and
-// the write pass (after it).  Jobs that do not qualify return at once.
-struct ShfFastLaunch {
+// The few-values path's launches around the general slides: palette and
+// vertical histograms, then the bin count per row (before the row scan), and
+// the write pass (after it).  Jobs that do not qualify return at once.  Two
+// formulations: sequential slides in packed form (a thread per column, then
+// per row) for launches of many chunks, row bands with prefix scans (a block
+// per band of rows) for launches of few.
+struct ShfBandLaunch {
 	uint32_t band_rows, bands, threads, cols_per_thread, max_cols;
 	size_t smem;
 };
-ShfFastLaunch shf_fast_config(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
+struct ShfFastPlan {
+	bool bands;
+	uint32_t max_cols; // widest chunk (W + 2r) the few-values path takes; 0: none
+	ShfBandLaunch band;
+};
+// stpgb_shf_set_path's choice (0 = by size)
+uint32_t shf_path_override();
+// the record's pad0: the formulation that filtered the job
+constexpr uint32_t kShfFormSlides = 1u, kShfFormBands = 2u;
+ShfFastPlan shf_fast_plan(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
 int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
-	uint32_t max_r, uint32_t kcap_h, const ShfFastLaunch& cfg, cudaStream_t stream);
-int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, const ShfFastLaunch& cfg, bool write,
-	cudaStream_t stream);
+	uint32_t max_r, uint32_t kcap_h, const ShfFastPlan& plan, cudaStream_t stream);
+int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_H, const ShfFastPlan& plan,
+	bool write, cudaStream_t stream);
+// the row-band formulation (shf_band.cu)
+ShfBandLaunch shf_band_config(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
+int shf_band_carry_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_r,
+	uint32_t kcap_h, uint32_t max_cols, const ShfBandLaunch& cfg, cudaStream_t stream);
+int shf_band_rows_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, const ShfBandLaunch& cfg,
+	bool write, cudaStream_t stream);
 
 } // namespace stpgb

@@ -1,64 +1,48 @@
-// Single histogram filter, few-values path, on sm_103a.
-//
+// Single histogram filter, few-values path, on sm_103a: the palette, the
+// sequential-slide formulation for launches of many chunks, and the choice
+// between it and the row-band formulation (shf_band.cu) for launches of few.
 // Same output as the reference filter
 // (SuperTerrain+/SuperAlgorithm+/Host/Private/STPSingleHistogramFilter.cpp),
-// bin order included, for chunks whose read region ((H+2r) x (W+2r)
-// samples) holds at most kShfFastItems distinct values (biome maps: a
-// Voronoi map of 8 biomes, the demo's layer chain).  Values are renamed to
-// local indices 0..7 (their rank in the chunk's palette), which lets a
-// histogram live in registers: eight byte counts in one 64-bit word and the
-// accumulator's order as eight 4-bit indices in one 32-bit word.
+// bin order included.
 //
-// The order of a histogram is the reference accumulator's insertion order with
-// erase-compaction (:400-450).  Vertically the slide is cheap in this form
-// (one add and one remove of a 4-bit index per row and column) and is run as
-// the reference runs it.  Horizontally the order follows from a rule that
-// makes every pixel independent of the slide: when column k's vertical
-// histogram is added, an item is inserted iff none of columns
-// [max(0, k-2r-1), k-1] holds it (before the add, the window holds exactly
-// those columns; the initial fill is the case k <= 2r).  An item present at
-// pixel x was last inserted at the latest such column k0 <= x+2r, in the place
-// it has in column k0's vertical histogram, and erasures keep the relative
-// order of what remains, so the bins of pixel x are its present items sorted
-// by (k0, place in column k0's histogram).  Windowed counts and "latest
-// insertion column" are both prefix scans over the columns of a row: one sum
-// scan and one max scan of eight 16-bit fields per column.
+// In packed form (shf_fast.cuh) a slide step is a few SIMD operations: the
+// vertical slide adds and removes one 4-bit index, the horizontal one adds and
+// subtracts two columns' counts as eight 16-bit fields; an item that becomes
+// present is appended (in the order of the column that brings it), one whose
+// count drops to zero is erased, and both are rare on these maps.  The slides
+// run as the reference runs them, one thread per column and per row, so the
+// order is the reference's by construction.
 //
-//   shf_palette   block per (32-row tile of the read region, job): distinct
-//                 values through a 65536-bit map in shared memory.
-//   shf_carry     thread per column: merges the palette tiles (every block
-//                 does, block 0 records the job's path), then slides the
-//                 column's vertical histogram down all rows and keeps its
-//                 state at the first row of every band.
-//   shf_fast_rows block per (band of rows, job), thread per column(s): per
-//                 row, the vertical step, the count scan, the insertion scan
-//                 and the pixels' bins (COUNT: bins per row; WRITE: offsets
-//                 and bins after the row scan).
-#include "shf.cuh"
+//   shf_palette       block per (32-row tile of the read region, job):
+//                     distinct values through a 65536-bit map in shared
+//                     memory.
+//   shf_vertical_fast thread per column: merges the palette tiles (every
+//                     block does, block 0 records the job's path), slides the
+//                     column's vertical histogram down all rows and writes it
+//                     to row-major planes in the job's vbuf.
+//   shf_rows_fast     thread per row: the horizontal slide; COUNT writes the
+//                     bins per row (before the row scan), WRITE the offsets
+//                     and bins (after it).
+#include "shf_fast.cuh"
 
 #include <algorithm>
 
 namespace stpgb {
 
+using namespace shfx;
+
 namespace {
 
 constexpr uint32_t kPaletteBlock = 256u;
-constexpr uint32_t kCarryBlock = 64u;
-constexpr uint32_t kFastMaxThreads = 1024u;
-constexpr uint32_t kNoValue = 0xFFFFFFFFu;
-// words per palette slot and per record: {count, 0, values as uint16 pairs x4, 0, 0}
-constexpr uint32_t kSlotWords = 8u;
-// the byte counts hold 2r+2 (add before remove), the 16-bit window sums (2r+1)^2
-constexpr uint32_t kFastMaxRadius = 126u;
-
-__device__ __forceinline__ const ShfJob& pick(const ShfJob* jobs, const ShfJob& single) {
-	return jobs ? jobs[blockIdx.y] : single;
-}
-
-// first sample of the read region: row sy - r, column sx - r
-__device__ __forceinline__ const uint16_t* read_region(const ShfJob& J) {
-	return J.samplemap + static_cast<uint64_t>(J.sy - J.r) * J.pitch + (J.sx - J.r);
-}
+constexpr uint32_t kVertBlock = 64u;
+constexpr uint32_t kRowBlock = 64u;
+// rows of the vertical slide whose samples are loaded ahead of their use
+constexpr uint32_t kVertAhead = 16u;
+// local indices of a column's last kRing samples (>= 2r+2)
+constexpr uint32_t kRing = 256u;
+// Launches with fewer rows than this many per SM (rows of all chunks) take
+// the row bands: one thread per row would leave the SMs nearly idle.
+constexpr uint64_t kSlideRowsPerSM = 256u;
 
 // ---------------------------------------------------------------- palette --
 
@@ -131,593 +115,320 @@ __global__ void __launch_bounds__(kPaletteBlock) shf_palette(const ShfJob* __res
 	}
 }
 
-// ------------------------------------------------------ packed histograms --
-
-// number of nonzero bytes (present items)
-__device__ __forceinline__ uint32_t nonzero_bytes(const uint64_t v) {
-	const uint64_t low7 = 0x7F7F7F7F7F7F7F7Full;
-	return static_cast<uint32_t>(__popcll((((v & low7) + low7) | v) & 0x8080808080808080ull));
-}
-
-// place of item j in an order word (j is in its first nonzero_bytes nibbles):
-// the lowest zero nibble of order ^ (j in every nibble)
-__device__ __forceinline__ uint32_t place_of(const uint32_t order, const uint32_t j) {
-	const uint32_t x = order ^ (j * 0x11111111u);
-	const uint32_t z = (x - 0x11111111u) & ~x & 0x88888888u;
-	return static_cast<uint32_t>(__ffs(z) - 1) >> 2;
-}
-
-// the reference accumulator's add of one sample of item a: appended when absent
-__device__ __forceinline__ void hist_add(uint64_t& cnt, uint32_t& order, const uint32_t a) {
-	const uint32_t sh = 8u * a;
-	if (((cnt >> sh) & 0xFFull) == 0ull) {
-		order |= a << (4u * nonzero_bytes(cnt));
-	}
-	cnt += 1ull << sh;
-}
-
-// its remove: an item whose count drops to zero is erased, later ones close up
-__device__ __forceinline__ void hist_sub(uint64_t& cnt, uint32_t& order, const uint32_t b) {
-	const uint32_t sh = 8u * b;
-	cnt -= 1ull << sh;
-	if (((cnt >> sh) & 0xFFull) == 0ull) {
-		const uint32_t low = (1u << (4u * place_of(order, b))) - 1u;
-		order = (order & low) | ((order >> 4) & ~low);
-	}
-}
-
-// The palette as eight 16-bit fields (value j in word j/2, half j%2),
-// ascending, 0xFFFF past the count.
-using Palette = uint4;
-
-__device__ __forceinline__ Palette make_palette(const uint32_t* const vals, const uint32_t n) {
-	auto at = [&](const uint32_t j) {
-		return j < n ? (vals[j] & 0xFFFFu) : 0xFFFFu;
-	};
-	return make_uint4(at(0) | (at(1) << 16), at(2) | (at(3) << 16), at(4) | (at(5) << 16), at(6) | (at(7) << 16));
-}
-
-// local index of a palette value: the number of palette values below it
-// (a padding field, 0xFFFF, is never below a 16-bit value)
-__device__ __forceinline__ uint32_t local_index(const Palette p, const uint32_t v) {
-	const uint32_t vv = v * 0x00010001u;
-	return (__popc(__vcmpgtu2(vv, p.x)) + __popc(__vcmpgtu2(vv, p.y)) + __popc(__vcmpgtu2(vv, p.z))
-			   + __popc(__vcmpgtu2(vv, p.w)))
-		>> 4;
-}
-
-// Union of a job's palette slots, ascending; kShfModeFast when it has at most
-// kShfFastItems values and the job fits this path.
-__device__ void merge_palette(const ShfJob& J, const uint32_t kcap_h, uint32_t& mode, uint32_t& count,
-	uint32_t* const vals) {
-	const uint32_t NR = J.H + 2u * J.r, NC = J.W + 2u * J.r;
-	const uint32_t tiles = (NR + kShfPaletteRows - 1u) / kShfPaletteRows;
-	uint32_t n = 0u;
-	bool ok = NC <= kShfFastMaxCols && J.r <= kFastMaxRadius;
-	for (uint32_t t = 0u; t < tiles && ok; t++) {
-		const uint32_t* const slot = J.fast + kSlotWords * (1u + t);
-		const uint32_t c = slot[0];
-		if (c == kNoValue) {
-			ok = false;
-			break;
-		}
-		for (uint32_t i = 0u; i < c && ok; i++) {
-			const uint32_t x = (slot[2u + i / 2u] >> (16u * (i & 1u))) & 0xFFFFu;
-			uint32_t p = 0u;
-			while (p < n && vals[p] < x) {
-				p++;
-			}
-			if (p < n && vals[p] == x) {
-				continue;
-			}
-			if (n == kShfFastItems) {
-				ok = false;
-				break;
-			}
-			for (uint32_t m = n; m > p; m--) {
-				vals[m] = vals[m - 1u];
-			}
-			vals[p] = x;
-			n++;
-		}
-	}
-	// No accumulator of the slides could overflow (a vertical one holds at most
-	// 2r+2 samples, a horizontal one (2r+2)(2r+1)), and the band states fit in
-	// vbuf (bands * (W+2r) * 12 bytes against H * kcap_v * (W+2r) * 4).
-	const uint64_t side = 2ull * J.r + 1u;
-	const uint32_t max_bands = (J.H + kShfFastMinBandRows - 1u) / kShfFastMinBandRows;
-	const uint64_t items = n;
-	ok = ok && min(items, side + 1u) <= J.kcap_v && min(items, (side + 1u) * side) <= kcap_h
-		&& 3ull * max_bands <= static_cast<uint64_t>(J.H) * J.kcap_v;
-	for (uint32_t j = n; j < kShfFastItems; j++) {
-		vals[j] = kNoValue;
-	}
-	mode = ok ? kShfModeFast : kShfModeSlide;
-	count = n;
-}
-
-// ------------------------------------------------------------------ carry --
+// --------------------------------------------------------------- vertical --
 
 // Thread per column k of the read region: the vertical histogram of rows
 // [y, y+2r] (relative to the region) for y = 0..H-1, slid as the reference
-// slides it (:522-563), stored at y = 0, band_rows, 2 band_rows, ...:
-// counts [bands][W+2r] (8 bytes), then orders [bands][W+2r] (4-bit indices).
-__global__ void __launch_bounds__(kCarryBlock) shf_carry(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t kcap_h, const uint32_t band_rows) {
+// slides it (:522-563), written for every row to two row-major planes in
+// vbuf: counts [H][W+2r] (8 bytes) and orders [H][W+2r] (4-bit indices), so
+// that a warp's stores are consecutive.  The local indices of a column's last
+// kRing samples stay in shared memory, so only the entering sample is read
+// from global memory, kVertAhead rows early.
+__global__ void __launch_bounds__(kVertBlock) shf_vertical_fast(const ShfJob* __restrict__ jobs, const ShfJob single,
+	const uint32_t kcap_h, const uint32_t max_cols) {
 	const ShfJob& J = pick(jobs, single);
 	__shared__ uint32_t s_mode, s_count, s_val[kShfFastItems];
+	__shared__ uint8_t ring[kRing][kVertBlock];
 	if (threadIdx.x == 0u) {
 		uint32_t vals[kShfFastItems];
-		merge_palette(J, kcap_h, s_mode, s_count, vals);
+		merge_palette(J, kcap_h, max_cols, s_mode, s_count, vals);
 		for (uint32_t j = 0u; j < kShfFastItems; j++) {
 			s_val[j] = vals[j];
 		}
 		if (blockIdx.x == 0u) {
-			ShfFastRecord* const rec = reinterpret_cast<ShfFastRecord*>(J.fast);
-			rec->mode = s_mode;
-			rec->count = s_count;
-			rec->pad0 = 0u;
-			rec->pad1 = 0u;
-			for (uint32_t j = 0u; j < kShfFastItems; j++) {
-				rec->item[j] = static_cast<uint16_t>(j < s_count ? vals[j] : 0u);
-			}
+			write_record(J, s_mode, s_count, vals, kShfFormSlides);
 		}
 	}
 	__syncthreads();
 	const uint32_t NC = J.W + 2u * J.r;
-	const uint32_t k = blockIdx.x * kCarryBlock + threadIdx.x;
+	const uint32_t k = blockIdx.x * kVertBlock + threadIdx.x;
 	if (s_mode != kShfModeFast || k >= NC) {
 		return;
 	}
 	const Palette pal = make_palette(s_val, s_count);
-	const uint16_t* const col = read_region(J) + k;
 	const uint64_t pitch = J.pitch;
 	const uint32_t H = J.H, r2 = 2u * J.r;
-	const uint32_t bands = (H + band_rows - 1u) / band_rows;
-	uint64_t* const cvc = reinterpret_cast<uint64_t*>(J.vbuf);
-	uint32_t* const cvo = reinterpret_cast<uint32_t*>(cvc + static_cast<size_t>(bands) * NC);
-	auto at = [&](const uint32_t q) {
-		return static_cast<uint32_t>(__ldg(col + static_cast<uint64_t>(q) * pitch));
-	};
+	const uint16_t* src = read_region(J) + k; // the next sample to load
+	uint64_t* cv = reinterpret_cast<uint64_t*>(J.vbuf) + k;
+	uint32_t* ov = reinterpret_cast<uint32_t*>(reinterpret_cast<uint64_t*>(J.vbuf) + static_cast<size_t>(NC) * H) + k;
+	uint8_t* const mine = &ring[0][threadIdx.x];
 	uint64_t cnt = 0ull;
 	uint32_t order = 0u;
 	for (uint32_t q = 0u; q <= r2; q++) {
-		hist_add(cnt, order, local_index(pal, at(q)));
+		const uint32_t li = local_index(pal, __ldg(src));
+		src += pitch;
+		mine[(q & (kRing - 1u)) * kVertBlock] = static_cast<uint8_t>(li);
+		hist_add(cnt, order, li);
 	}
-	cvc[k] = cnt;
-	cvo[k] = order;
-	// row y adds region row y+2r and removes row y-1; the samples of the next
-	// four rows are loaded ahead (they do not depend on the histogram)
-	constexpr uint32_t kAhead = 4u;
-	uint32_t ra[kAhead], rb[kAhead];
+	cv[0] = cnt;
+	ov[0] = order;
+	// row y adds region row y+2r (prefetched) and removes row y-1 (from the ring)
+	uint32_t pre[kVertAhead];
 #pragma unroll
-	for (uint32_t i = 0u; i < kAhead; i++) {
-		const uint32_t y = 1u + i;
-		ra[i] = y < H ? at(y + r2) : 0u;
-		rb[i] = y < H ? at(y - 1u) : 0u;
+	for (uint32_t i = 0u; i < kVertAhead; i++) {
+		pre[i] = 1u + i < H ? __ldg(src + i * pitch) : 0u;
 	}
-	for (uint32_t y = 1u; y < H; y += kAhead) {
+	src += kVertAhead * pitch;
+	for (uint32_t y = 1u; y < H; y += kVertAhead) {
 #pragma unroll
-		for (uint32_t i = 0u; i < kAhead; i++) {
+		for (uint32_t i = 0u; i < kVertAhead; i++) {
 			const uint32_t yy = y + i;
 			if (yy < H) {
-				const uint32_t a = ra[i], b = rb[i];
-				if (yy + kAhead < H) {
-					ra[i] = at(yy + kAhead + r2);
-					rb[i] = at(yy + kAhead - 1u);
+				const uint32_t li = local_index(pal, pre[i]);
+				if (yy + kVertAhead < H) {
+					pre[i] = __ldg(src);
 				}
-				if (a != b) {
-					hist_add(cnt, order, local_index(pal, a));
-					hist_sub(cnt, order, local_index(pal, b));
+				src += pitch;
+				const uint32_t lo = mine[((yy - 1u) & (kRing - 1u)) * kVertBlock];
+				mine[((yy + r2) & (kRing - 1u)) * kVertBlock] = static_cast<uint8_t>(li);
+				if (li != lo) {
+					hist_add(cnt, order, li);
+					hist_sub(cnt, order, lo);
 				}
-				if (yy % band_rows == 0u) {
-					const size_t o = static_cast<size_t>(yy / band_rows) * NC + k;
-					cvc[o] = cnt;
-					cvo[o] = order;
-				}
+				cv[static_cast<size_t>(yy) * NC] = cnt;
+				ov[static_cast<size_t>(yy) * NC] = order;
 			}
 		}
 	}
 }
 
-// ------------------------------------------------------------------- rows --
+// ------------------------------------------------------------- horizontal --
 
-__device__ __forceinline__ uint4 add4(const uint4 a, const uint4 b) {
-	return make_uint4(__vadd2(a.x, b.x), __vadd2(a.y, b.y), __vadd2(a.z, b.z), __vadd2(a.w, b.w));
-}
-__device__ __forceinline__ uint4 sub4(const uint4 a, const uint4 b) {
-	return make_uint4(__vsub2(a.x, b.x), __vsub2(a.y, b.y), __vsub2(a.z, b.z), __vsub2(a.w, b.w));
-}
-__device__ __forceinline__ uint4 max4(const uint4 a, const uint4 b) {
-	return make_uint4(__vmaxu2(a.x, b.x), __vmaxu2(a.y, b.y), __vmaxu2(a.z, b.z), __vmaxu2(a.w, b.w));
-}
-__device__ __forceinline__ uint4 shfl_up4(const uint4 v, const uint32_t d) {
-	return make_uint4(__shfl_up_sync(0xFFFFFFFFu, v.x, d), __shfl_up_sync(0xFFFFFFFFu, v.y, d),
-		__shfl_up_sync(0xFFFFFFFFu, v.z, d), __shfl_up_sync(0xFFFFFFFFu, v.w, d));
-}
-
-// eight byte counts -> eight 16-bit fields (item j in word j/2, half j%2)
-__device__ __forceinline__ uint4 widen(const uint64_t c) {
-	const uint32_t lo = static_cast<uint32_t>(c), hi = static_cast<uint32_t>(c >> 32);
-	return make_uint4(__byte_perm(lo, 0u, 0x4140u), __byte_perm(lo, 0u, 0x4342u), __byte_perm(hi, 0u, 0x4140u),
-		__byte_perm(hi, 0u, 0x4342u));
-}
-
-// bit j set where field j is nonzero
-__device__ __forceinline__ uint32_t present_mask(const uint4 v) {
-	const uint32_t a = __vcmpne2(v.x, 0u), b = __vcmpne2(v.y, 0u), c = __vcmpne2(v.z, 0u), d = __vcmpne2(v.w, 0u);
-	return (a & 1u) | ((a >> 15) & 2u) | ((b & 1u) << 2) | ((b >> 13) & 8u) | ((c & 1u) << 4) | ((c >> 11) & 32u)
-		| ((d & 1u) << 6) | ((d >> 9) & 128u);
-}
-
-__device__ __forceinline__ uint32_t field(const uint4 v, const uint32_t j) {
-	const uint32_t w = (j & 4u) ? ((j & 2u) ? v.w : v.z) : ((j & 2u) ? v.y : v.x);
-	return (w >> (16u * (j & 1u))) & 0xFFFFu;
-}
-
-struct AddOp {
-	__device__ __forceinline__ uint4 operator()(const uint4 a, const uint4 b) const {
-		return add4(a, b);
-	}
-};
-struct MaxOp {
-	__device__ __forceinline__ uint4 operator()(const uint4 a, const uint4 b) const {
-		return max4(a, b);
-	}
-};
-
-// Exclusive scan of one uint4 per thread over the block (identity 0), with
-// `wt` (32 entries) for the warp totals; `total` gets the whole block's.
-template<class Op>
-__device__ __forceinline__ uint4 block_exscan(const uint4 v, uint4* const wt, uint4& total, const Op op) {
-	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-	uint4 inc = v;
-#pragma unroll
-	for (uint32_t d = 1u; d < 32u; d <<= 1) {
-		const uint4 t = shfl_up4(inc, d);
-		if (lane >= d) {
-			inc = op(inc, t);
-		}
-	}
-	uint4 ex = shfl_up4(inc, 1u);
-	if (lane == 0u) {
-		ex = zero;
-	}
-	if (lane == 31u) {
-		wt[warp] = inc;
-	}
-	__syncthreads();
-	if (warp == 0u) {
-		uint4 s = lane < nw ? wt[lane] : zero;
-#pragma unroll
-		for (uint32_t d = 1u; d < 32u; d <<= 1) {
-			const uint4 t = shfl_up4(s, d);
-			if (lane >= d) {
-				s = op(s, t);
-			}
-		}
-		if (lane < nw) {
-			wt[lane] = s;
-		}
-	}
-	__syncthreads();
-	total = wt[nw - 1u];
-	return warp ? op(wt[warp - 1u], ex) : ex;
-}
-
-__device__ __forceinline__ uint32_t block_exscan_u32(const uint32_t v, uint32_t* const wt, uint32_t& total) {
-	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	uint32_t inc = v;
-#pragma unroll
-	for (uint32_t d = 1u; d < 32u; d <<= 1) {
-		const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, d);
-		if (lane >= d) {
-			inc += t;
-		}
-	}
-	if (lane == 31u) {
-		wt[warp] = inc;
-	}
-	__syncthreads();
-	if (warp == 0u) {
-		uint32_t s = lane < nw ? wt[lane] : 0u;
-#pragma unroll
-		for (uint32_t d = 1u; d < 32u; d <<= 1) {
-			const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, s, d);
-			if (lane >= d) {
-				s += t;
-			}
-		}
-		if (lane < nw) {
-			wt[lane] = s;
-		}
-	}
-	__syncthreads();
-	total = wt[nw - 1u];
-	return (warp ? wt[warp - 1u] : 0u) + inc - v;
-}
-
-// Block (band of rows [b*band_rows, ...), job); thread t owns columns and
-// pixels [t*cpt, t*cpt+cpt), cpt = ceil((W+2r) / threads) <= Cols.
-// Shared memory: counts prefix P[W+2r+1], insertion scan M[W+2r] (uint4:
-// eight 16-bit fields), three sets of 32 warp totals, orders[W+2r].
-// Per row y: P[k] = counts of columns < k (the window of pixel x is
-// P[x+2r+1] - P[x]); column k inserts item j iff it holds j and columns
-// [max(0, k-2r-1), k-1] do not (P[k] - P[lo] == 0); M[k] = 1 + the latest
-// such column <= k, per item.
-template<bool Write, uint32_t Cols>
-__global__ void __launch_bounds__(kFastMaxThreads) shf_fast_rows(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t band_rows, const uint32_t max_cols) {
-	const ShfJob& J = pick(jobs, single);
-	const ShfFastRecord* const rec = reinterpret_cast<const ShfFastRecord*>(J.fast);
-	if (rec->mode != kShfModeFast) {
-		return;
-	}
-	const uint32_t y0 = blockIdx.x * band_rows;
-	if (y0 >= J.H) {
-		return;
-	}
-	const uint32_t y1 = min(J.H, y0 + band_rows);
-	const uint32_t W = J.W, r2 = 2u * J.r, NC = W + r2;
-	const uint32_t cpt = (NC + blockDim.x - 1u) / blockDim.x;
-	const uint32_t k0 = threadIdx.x * cpt;
-	extern __shared__ uint4 fsm[];
-	uint4* const P = fsm;
-	uint4* const M = P + max_cols + 1u;
-	uint4* const wt = M + max_cols;
-	uint32_t* const ord = reinterpret_cast<uint32_t*>(wt + 96u);
-	__shared__ uint32_t s_item[kShfFastItems];
-	const uint32_t* const rw = reinterpret_cast<const uint32_t*>(rec->item);
-	const uint32_t ncount = rec->count;
-	auto half = [&](const uint32_t j) {
-		return j < ncount ? ((rw[j / 2u] >> (16u * (j & 1u))) & 0xFFFFu) : 0xFFFFu;
-	};
-	const Palette pal = make_uint4(half(0) | (half(1) << 16), half(2) | (half(3) << 16), half(4) | (half(5) << 16),
-		half(6) | (half(7) << 16));
-	if (threadIdx.x < kShfFastItems) {
-		s_item[threadIdx.x] = rec->item[threadIdx.x];
-	}
-	const uint32_t bands = (J.H + band_rows - 1u) / band_rows;
-	const uint64_t* const cvc = reinterpret_cast<const uint64_t*>(J.vbuf);
-	const uint32_t* const cvo = reinterpret_cast<const uint32_t*>(cvc + static_cast<size_t>(bands) * NC);
-	const uint16_t* const base = read_region(J);
-	const uint64_t pitch = J.pitch;
-	uint64_t cnt[Cols];
-	uint32_t order[Cols], na[Cols], nb[Cols];
-	auto owned = [&](const uint32_t c) {
-		return c < cpt && k0 + c < NC;
-	};
-#pragma unroll
-	for (uint32_t c = 0u; c < Cols; c++) {
-		if (owned(c)) {
-			const size_t o = static_cast<size_t>(blockIdx.x) * NC + k0 + c;
-			cnt[c] = cvc[o];
-			order[c] = cvo[o];
-		} else {
-			cnt[c] = 0ull;
-			order[c] = 0u;
-		}
-		na[c] = nb[c] = 0u;
-	}
-	// samples of row y: region row y+2r enters, row y-1 leaves
-	auto load_row = [&](const uint32_t y) {
-		if (y < y1) {
-#pragma unroll
-			for (uint32_t c = 0u; c < Cols; c++) {
-				if (owned(c)) {
-					na[c] = __ldg(base + static_cast<uint64_t>(y + r2) * pitch + k0 + c);
-					nb[c] = __ldg(base + static_cast<uint64_t>(y - 1u) * pitch + k0 + c);
-				}
-			}
-		}
-	};
-	load_row(y0 + 1u);
-	const uint32_t side = r2 + 1u;
-	const float norm = __fdiv_rn(1.0f, static_cast<float>(side * side));
-	uint2* const bins = reinterpret_cast<uint2*>(J.bins);
-	const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-	__syncthreads(); // s_item
-
-	for (uint32_t y = y0; y < y1; y++) {
-		if (y > y0) {
-#pragma unroll
-			for (uint32_t c = 0u; c < Cols; c++) {
-				if (owned(c) && na[c] != nb[c]) {
-					hist_add(cnt[c], order[c], local_index(pal, na[c]));
-					hist_sub(cnt[c], order[c], local_index(pal, nb[c]));
-				}
-			}
-			load_row(y + 1u);
-		}
-		// counts prefix
-		uint4 run = zero;
-#pragma unroll
-		for (uint32_t c = 0u; c < Cols; c++) {
-			if (owned(c)) {
-				run = add4(run, widen(cnt[c]));
-			}
-		}
-		uint4 tot;
-		uint4 acc = block_exscan(run, wt, tot, AddOp {});
-#pragma unroll
-		for (uint32_t c = 0u; c < Cols; c++) {
-			if (owned(c)) {
-				P[k0 + c] = acc;
-				ord[k0 + c] = order[c];
-				acc = add4(acc, widen(cnt[c]));
-			}
-		}
-		if (threadIdx.x == 0u) {
-			P[NC] = tot;
-		}
-		__syncthreads();
-		if constexpr (Write) {
-			// insertion columns, as 1 + column per item, and their running maximum
-			auto inserts = [&](const uint32_t c) {
-				const uint32_t k = k0 + c;
-				const uint4 win = sub4(P[k], P[k > r2 ? k - r2 - 1u : 0u]);
-				const uint4 w = widen(cnt[c]);
-				const uint32_t kk = (k + 1u) * 0x00010001u;
-				return make_uint4(__vcmpeq2(win.x, 0u) & __vcmpne2(w.x, 0u) & kk,
-					__vcmpeq2(win.y, 0u) & __vcmpne2(w.y, 0u) & kk, __vcmpeq2(win.z, 0u) & __vcmpne2(w.z, 0u) & kk,
-					__vcmpeq2(win.w, 0u) & __vcmpne2(w.w, 0u) & kk);
-			};
-			uint4 mrun = zero;
-#pragma unroll
-			for (uint32_t c = 0u; c < Cols; c++) {
-				if (owned(c)) {
-					mrun = max4(mrun, inserts(c));
-				}
-			}
-			uint4 mtot;
-			uint4 macc = block_exscan(mrun, wt + 32u, mtot, MaxOp {});
-#pragma unroll
-			for (uint32_t c = 0u; c < Cols; c++) {
-				if (owned(c)) {
-					macc = max4(macc, inserts(c));
-					M[k0 + c] = macc;
-				}
-			}
-			__syncthreads();
-		}
-		// pixels x = k0 + c < W
-		uint32_t mine = 0u;
-#pragma unroll
-		for (uint32_t c = 0u; c < Cols; c++) {
-			const uint32_t x = k0 + c;
-			if (c < cpt && x < W) {
-				mine += __popc(present_mask(sub4(P[x + r2 + 1u], P[x])));
-			}
-		}
-		uint32_t all;
-		const uint32_t before = block_exscan_u32(mine, reinterpret_cast<uint32_t*>(wt + 64u), all);
-		if constexpr (!Write) {
-			if (threadIdx.x == 0u) {
-				J.rows[y] = all;
-			}
-		} else {
-			uint64_t o = static_cast<uint64_t>(J.rows[y]) + before;
-			uint32_t* const off_row = J.offsets + static_cast<size_t>(y) * W;
-			auto put = [&](const uint32_t j, const uint4 hc) {
-				if (o < J.bins_capacity) {
-					const float w = __fmul_rn(__uint2float_rn(field(hc, j)), norm);
-					bins[o] = make_uint2(s_item[j], __float_as_uint(w));
-				}
-				o++;
-			};
-#pragma unroll
-			for (uint32_t c = 0u; c < Cols; c++) {
-				const uint32_t x = k0 + c;
-				if (c < cpt && x < W) {
-					const uint4 hc = sub4(P[x + r2 + 1u], P[x]);
-					const uint32_t pm = present_mask(hc);
-					off_row[x] = static_cast<uint32_t>(o);
-					// a window always holds (2r+1)^2 samples, so pm != 0
-					if (pm != 0u && (pm & (pm - 1u)) == 0u) {
-						put(static_cast<uint32_t>(__ffs(pm) - 1), hc);
-					} else if (pm != 0u) {
-						// present items by (insertion column, place in its vertical histogram)
-						const uint4 m = M[x + r2];
-						uint32_t key[kShfFastItems];
-#pragma unroll
-						for (uint32_t j = 0u; j < kShfFastItems; j++) {
-							key[j] = 0xFFFFFFFFu;
-							if ((pm >> j) & 1u) {
-								// every present item has an insertion column (the clamp only keeps a
-								// broken invariant inside the tables)
-								const uint32_t kc = min(field(m, j) - 1u, NC - 1u);
-								key[j] = (kc << 3) | place_of(ord[kc], j);
-							}
-						}
-						for (uint32_t left = __popc(pm); left > 0u; left--) {
-							uint32_t best = 0u, bk = key[0];
-#pragma unroll
-							for (uint32_t j = 1u; j < kShfFastItems; j++) {
-								if (key[j] < bk) {
-									bk = key[j];
-									best = j;
-								}
-							}
-#pragma unroll
-							for (uint32_t j = 0u; j < kShfFastItems; j++) {
-								if (j == best) {
-									key[j] = 0xFFFFFFFFu;
-								}
-							}
-							put(best, hc);
-						}
-					}
-				}
-			}
-		}
-	}
-}
-
+// Thread per row y: the reference's horizontal slide (:608-679) over the
+// packed vertical histograms of the row: counts as eight 16-bit fields, the
+// accumulator's order as 4-bit indices.  A column's items enter in the order
+// of its vertical histogram when they are absent, an item whose count drops to
+// zero is erased; a step whose entering and leaving columns hold the same
+// counts changes nothing.  The row's bins (item, weight) in order are kept in
+// registers and rebuilt when the counts change.  COUNT: bins per row; WRITE:
+// offsets and bins from the row's base, offsets four at a time and bins in
+// pairs as 16-byte stores where the buffers are 16-byte aligned.
 template<bool Write>
-int launch_rows(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const ShfFastLaunch& cfg,
-	cudaStream_t stream) {
-	const dim3 grid(cfg.bands, njobs);
-	switch (cfg.cols_per_thread) {
-	case 1u:
-		shf_fast_rows<Write, 1u><<<grid, cfg.threads, cfg.smem, stream>>>(jobs, single, cfg.band_rows, cfg.max_cols);
-		break;
-	case 2u:
-		shf_fast_rows<Write, 2u><<<grid, cfg.threads, cfg.smem, stream>>>(jobs, single, cfg.band_rows, cfg.max_cols);
-		break;
-	default:
-		shf_fast_rows<Write, 4u><<<grid, cfg.threads, cfg.smem, stream>>>(jobs, single, cfg.band_rows, cfg.max_cols);
-		break;
+__global__ void __launch_bounds__(kRowBlock) shf_rows_fast(const ShfJob* __restrict__ jobs, const ShfJob single) {
+	const ShfJob& J = pick(jobs, single);
+	if (reinterpret_cast<const ShfFastRecord*>(J.fast)->mode != kShfModeFast) {
+		return;
 	}
-	STPGB_CUDA_TRY(cudaGetLastError());
-	return STPGB_OK;
-}
+	const uint32_t H = J.H, W = J.W, r2 = 2u * J.r, NC = W + r2;
+	const uint32_t y = blockIdx.x * kRowBlock + threadIdx.x;
+	if (y >= H) {
+		return;
+	}
+	const ShfFastRecord* const rec = reinterpret_cast<const ShfFastRecord*>(J.fast);
+	const uint64_t* const cv = reinterpret_cast<const uint64_t*>(J.vbuf) + static_cast<size_t>(y) * NC;
+	const uint32_t* const ov = reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint64_t*>(J.vbuf)
+								   + static_cast<size_t>(NC) * H)
+		+ static_cast<size_t>(y) * NC;
+	uint4 hc = make_uint4(0u, 0u, 0u, 0u);
+	uint32_t order = 0u, n = 0u;
+	// absent items of column k (counts wa) enter in its vertical order
+	auto insert = [&](const uint32_t k, const uint4 wa, uint32_t fresh) {
+		uint32_t vo = __ldg(ov + k);
+		for (uint32_t left = __popc(present_mask(wa)); left > 0u && fresh; left--, vo >>= 4) {
+			const uint32_t j = vo & 15u;
+			if ((fresh >> j) & 1u) {
+				order |= j << (4u * n);
+				n++;
+				fresh &= ~(1u << j);
+			}
+		}
+	};
+	auto erase = [&](uint32_t gone) {
+		while (gone) {
+			const uint32_t j = static_cast<uint32_t>(__ffs(gone) - 1);
+			gone &= gone - 1u;
+			const uint32_t low = (1u << (4u * place_of(order, j))) - 1u;
+			order = (order & low) | ((order >> 4) & ~low);
+			n--;
+		}
+	};
+	// one step: add column k's counts a, then remove counts b (b = 0 in the fill)
+	auto step = [&](const uint32_t k, const uint64_t a, const uint64_t b) {
+		const uint4 wa = widen(a), wb = widen(b);
+		const uint4 za = zero4(hc);
+		const uint4 h1 = add4(hc, wa);
+		hc = sub4(h1, wb);
+		const uint4 zw = zero4(wa), zb = zero4(wb), zh = zero4(hc);
+		// fresh: zero before, brought by a; gone: brought by b (so present after the add), zero now
+		const uint4 f = make_uint4(za.x & ~zw.x, za.y & ~zw.y, za.z & ~zw.z, za.w & ~zw.w);
+		const uint4 g = make_uint4(zh.x & ~zb.x, zh.y & ~zb.y, zh.z & ~zb.z, zh.w & ~zb.w);
+		if (f.x | f.y | f.z | f.w) {
+			insert(k, wa, present_mask(f));
+		}
+		if (g.x | g.y | g.z | g.w) {
+			erase(present_mask(g));
+		}
+	};
+	for (uint32_t k = 0u; k <= r2; k++) {
+		step(k, __ldg(cv + k), 0ull);
+	}
 
-int fast_set_smem_attributes() {
-	const int bytes = 200 * 1024;
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<false, 1u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<false, 2u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<false, 4u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<true, 1u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<true, 2u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	STPGB_CUDA_TRY(cudaFuncSetAttribute(shf_fast_rows<true, 4u>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-	return STPGB_OK;
+	uint64_t o = 0u; // running bin index
+	uint32_t* off_row = nullptr;
+	uint2* bins = nullptr;
+	bool off_vec = false, bin_vec = false;
+	uint32_t q0 = 0u, q1 = 0u, q2 = 0u, q3 = 0u; // the last four offsets
+	uint2 pend = make_uint2(0u, 0u);
+	bool has_pend = false;
+	uint4 items = make_uint4(0u, 0u, 0u, 0u); // the palette values as 16-bit fields
+	float norm = 0.0f;
+	uint2 e[kShfFastItems]; // the current bins in order
+	// read once: the bins stores below could alias the job table as far as the compiler knows
+	const uint64_t cap = J.bins_capacity;
+	if constexpr (Write) {
+		o = J.rows[y];
+		off_row = J.offsets + static_cast<size_t>(y) * W;
+		bins = reinterpret_cast<uint2*>(J.bins);
+		off_vec = (reinterpret_cast<uintptr_t>(off_row) & 15u) == 0u;
+		bin_vec = (reinterpret_cast<uintptr_t>(bins) & 15u) == 0u;
+		const uint32_t* const iw = reinterpret_cast<const uint32_t*>(rec->item);
+		items = make_uint4(iw[0], iw[1], iw[2], iw[3]);
+		const uint32_t side = r2 + 1u;
+		norm = __fdiv_rn(1.0f, static_cast<float>(side * side));
+	}
+	// the bins of the current state, n of them (most pixels hold one or two)
+	auto rebuild = [&]() {
+		if constexpr (Write) {
+			uint32_t ord = order;
+#pragma unroll
+			for (uint32_t p = 0u; p < kShfFastItems; p++, ord >>= 4) {
+				if (p >= n) {
+					break;
+				}
+				const uint32_t j = ord & 15u;
+				const float w = __fmul_rn(__uint2float_rn(field(hc, j)), norm);
+				e[p] = make_uint2(field(items, j), __float_as_uint(w));
+			}
+		}
+	};
+	auto put_bin = [&](const uint2 b) {
+		if (bin_vec && (o & 1u) && has_pend) {
+			if (o < cap) {
+				*reinterpret_cast<uint4*>(bins + o - 1u) = make_uint4(pend.x, pend.y, b.x, b.y);
+			} else if (o - 1u < cap) {
+				bins[o - 1u] = pend;
+			}
+			has_pend = false;
+		} else if (bin_vec && !(o & 1u)) {
+			pend = b;
+			has_pend = true;
+		} else if (o < cap) {
+			bins[o] = b;
+		}
+		o++;
+	};
+	auto emit = [&](const uint32_t x) {
+		if constexpr (Write) {
+			const uint32_t v = static_cast<uint32_t>(o);
+			if (off_vec) {
+				q0 = q1;
+				q1 = q2;
+				q2 = q3;
+				q3 = v;
+				if ((x & 3u) == 3u) {
+					*reinterpret_cast<uint4*>(off_row + x - 3u) = make_uint4(q0, q1, q2, q3);
+				}
+			} else {
+				off_row[x] = v;
+			}
+#pragma unroll
+			for (uint32_t p = 0u; p < kShfFastItems; p++) {
+				if (p >= n) {
+					break;
+				}
+				put_bin(e[p]);
+			}
+		} else {
+			o += n;
+		}
+	};
+	rebuild();
+	emit(0u);
+	// Step x adds column x+2r and removes column x-1.  Each row's counts are a
+	// stream of its own (16 steps per 128-byte line); the line two ahead of
+	// each stream is asked into L1 when a stream enters a line.
+	const uint64_t* pa_src = cv + r2 + 1u;
+	const uint64_t* pb_src = cv;
+	for (uint32_t x = 1u; x < W; x++, pa_src++, pb_src++) {
+		if (x + 32u < W) { // both prefetched addresses stay inside the row
+			if ((reinterpret_cast<uintptr_t>(pa_src) & 127u) == 0u) {
+				prefetch_l1(pa_src + 32);
+			}
+			if ((reinterpret_cast<uintptr_t>(pb_src) & 127u) == 0u) {
+				prefetch_l1(pb_src + 32);
+			}
+		}
+		const uint64_t a = __ldg(pa_src), b = __ldg(pb_src);
+		if (a != b) {
+			step(x + r2, a, b);
+			rebuild();
+		}
+		emit(x);
+	}
+	if constexpr (Write) {
+		// what is still held: offsets after the last full quad, and a bin without its pair
+		if (off_vec) {
+			const uint32_t rem = W & 3u;
+			if (rem >= 3u) {
+				off_row[W - 3u] = q1;
+			}
+			if (rem >= 2u) {
+				off_row[W - 2u] = q2;
+			}
+			if (rem >= 1u) {
+				off_row[W - 1u] = q3;
+			}
+		}
+		if (has_pend && o - 1u < cap) {
+			bins[o - 1u] = pend;
+		}
+	} else {
+		J.rows[y] = static_cast<uint32_t>(min(o, static_cast<uint64_t>(0xFFFFFFFFu)));
+	}
 }
 
 } // namespace
 
-ShfFastLaunch shf_fast_config(const uint32_t njobs, const uint32_t max_W, const uint32_t max_H, const uint32_t max_r) {
-	ShfFastLaunch cfg {};
-	const uint32_t ncols = std::min(max_W + 2u * max_r, kShfFastMaxCols);
-	cfg.threads = ncols <= kFastMaxThreads ? (ncols + 31u) / 32u * 32u : kFastMaxThreads;
-	const uint32_t need = (ncols + cfg.threads - 1u) / cfg.threads;
-	cfg.cols_per_thread = need <= 1u ? 1u : need <= 2u ? 2u : 4u;
-	// about three blocks per SM over the launch; bands of 4 to 64 rows
-	const uint64_t want = (3ull * current_sm_count() + njobs - 1u) / std::max(njobs, 1u);
-	const uint64_t rows = (static_cast<uint64_t>(max_H) + want - 1u) / std::max<uint64_t>(want, 1u);
-	cfg.band_rows = static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(rows, kShfFastMinBandRows), 64u));
-	cfg.bands = (max_H + cfg.band_rows - 1u) / cfg.band_rows;
-	cfg.max_cols = ncols;
-	cfg.smem = (2u * static_cast<size_t>(ncols) + 1u + 96u) * sizeof(uint4) + static_cast<size_t>(ncols) * sizeof(uint32_t);
-	return cfg;
+ShfFastPlan shf_fast_plan(const uint32_t njobs, const uint32_t max_W, const uint32_t max_H, const uint32_t max_r) {
+	ShfFastPlan plan {};
+	const uint32_t choice = shf_path_override();
+	plan.bands = choice == 2u
+		|| (choice == 0u && static_cast<uint64_t>(njobs) * max_H < kSlideRowsPerSM * current_sm_count());
+	plan.max_cols = choice == 3u ? 0u : plan.bands ? kShfBandMaxCols : 0xFFFFFFFFu;
+	if (plan.bands) {
+		plan.band = shf_band_config(njobs, max_W, max_H, max_r);
+	}
+	return plan;
 }
 
 int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const uint32_t max_W,
-	const uint32_t max_H, const uint32_t max_r, const uint32_t kcap_h, const ShfFastLaunch& cfg, cudaStream_t stream) {
+	const uint32_t max_H, const uint32_t max_r, const uint32_t kcap_h, const ShfFastPlan& plan, cudaStream_t stream) {
 	const uint32_t tiles = (max_H + 2u * max_r + kShfPaletteRows - 1u) / kShfPaletteRows;
 	shf_palette<<<dim3(tiles, njobs), kPaletteBlock, 0, stream>>>(jobs, single);
 	STPGB_CUDA_TRY(cudaGetLastError());
+	if (plan.bands) {
+		return shf_band_carry_launch(jobs, single, njobs, max_W, max_r, kcap_h, plan.max_cols, plan.band, stream);
+	}
 	const uint32_t ncols = max_W + 2u * max_r;
-	shf_carry<<<dim3((ncols + kCarryBlock - 1u) / kCarryBlock, njobs), kCarryBlock, 0, stream>>>(jobs, single, kcap_h,
-		cfg.band_rows);
+	shf_vertical_fast<<<dim3((ncols + kVertBlock - 1u) / kVertBlock, njobs), kVertBlock, 0, stream>>>(jobs, single,
+		kcap_h, plan.max_cols);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }
 
-int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const ShfFastLaunch& cfg,
-	const bool write, cudaStream_t stream) {
-	STPGB_TRY(once_per_device(SETUP_SHF_FAST_SMEM, fast_set_smem_attributes));
-	return write ? launch_rows<true>(jobs, single, njobs, cfg, stream) : launch_rows<false>(jobs, single, njobs, cfg, stream);
+int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const uint32_t max_H,
+	const ShfFastPlan& plan, const bool write, cudaStream_t stream) {
+	if (plan.bands) {
+		return shf_band_rows_launch(jobs, single, njobs, plan.band, write, stream);
+	}
+	const dim3 grid((max_H + kRowBlock - 1u) / kRowBlock, njobs);
+	if (write) {
+		shf_rows_fast<true><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+	} else {
+		shf_rows_fast<false><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+	}
+	STPGB_CUDA_TRY(cudaGetLastError());
+	return STPGB_OK;
 }
 
 } // namespace stpgb

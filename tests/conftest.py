@@ -31,3 +31,10 @@ def dev(stpgb):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return stpgb.DeviceOps()
+
+
+@pytest.fixture
+def shf_path(dev):
+    """Sets the filter's process-wide path (stpgb_shf_set_path) for one test, then back to 0."""
+    yield dev.shf_set_path
+    dev.shf_set_path(0)

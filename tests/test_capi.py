@@ -179,3 +179,12 @@ def test_header_is_plain_c(tmp_path):
                     str(src), "-L" + libdir, "-lstpgb", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out[:3] == ["0", "2", "1"]
+
+
+def test_shf_set_path_range(stpgb):
+    """The filter's process-wide path choice: 0..3 accepted, anything above refused (no GPU call)."""
+    lib = stpgb.lib()
+    for p in (1, 2, 3, 0):
+        assert lib.stpgb_shf_set_path(p) == 0
+    assert lib.stpgb_shf_set_path(4) != 0
+    assert lib.stpgb_shf_set_path(0) == 0

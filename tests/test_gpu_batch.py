@@ -39,10 +39,13 @@ def heights(b):
     return out, fixed, res
 
 
-@pytest.mark.parametrize("tune", [False, True])
-def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, tune):
+@pytest.mark.parametrize("tune,form", [(False, 0), (True, 0), (False, 1), (False, 3)])
+def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, shf_path, tune, form):
     """Inputs bit-exact, heights within 2e-6 of the oracle, with the default filter segments and
-    noise block or with the autotuner's choice of both (every candidate was timed)."""
+    noise block or with the autotuner's choice of both (every candidate was timed); the filter's
+    path by launch size (this batch of 36 chunks: the few-values row bands), forced to the
+    few-values packed slides, or forced to the general slides."""
+    shf_path(form)
     b, table = make_batch(stpgb)
     if tune:
         b.tune()
