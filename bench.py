@@ -483,20 +483,27 @@ def run_ours(args):
     stream2.synchronize()
     batch2.tune()
     pipes = [(batch, stream, out0), (batch2, stream2, host_outputs())]
-    for k in range(4):
-        b_, st_, out_ = pipes[k % 2]
-        st_.synchronize()
-        b_.upload(host_biome, host_starts, st_.cuda_stream)
-        b_.run(st_.cuda_stream)
-        b_.download(*out_, st_.cuda_stream)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
+    # the kernels of one step wait for the other stream's kernels (an event after each run): only
+    # copies overlap kernels, two erosions never share the L2
+    ran = [None]
+
+    def pipe_step(k):
         b_, st_, out_ = pipes[k % 2]
         st_.synchronize()  # this batch's previous step, and its host outputs, are done
         b_.upload(host_biome, host_starts, st_.cuda_stream)
+        if ran[0] is not None:
+            st_.wait_event(ran[0])
         b_.run(st_.cuda_stream)
+        ran[0] = torch.cuda.Event()
+        ran[0].record(st_)
         b_.download(*out_, st_.cuda_stream)
+
+    for k in range(4):
+        pipe_step(k)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        pipe_step(k)
     torch.cuda.synchronize()
     e2e_value = B * e2e_steps / (time.perf_counter() - t0)
     batch.status(sh)
@@ -572,7 +579,7 @@ def run_ours(args):
                 np.percentile(step_ms, 99)),
             "e2e": {"value": e2e_value, "unit": "chunks/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "pipelining": "two batches alternate on two streams: one step's uploads and downloads overlap "
-                                  "the other step's kernels",
+                                  "the other step's kernels; the kernels of the two run one after the other",
                     "serial_value": e2e_serial_value},
             "stage_ms": dict(zip(stage_names, stage_ms)),
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
