@@ -537,6 +537,9 @@ def run_ours(args):
                 "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": fb}
 
+    stage_roof = stage_rooflines(m, np, torch, dev, host_biome, table, stage_ms, stage_names, peak, peak_kind,
+                                 peaks)
+
     serving = None
     if rank == 0 and args.serve_requests > 0:
         log("serving")
@@ -583,7 +586,8 @@ def run_ours(args):
                     "serial_value": e2e_serial_value},
             "stage_ms": dict(zip(stage_names, stage_ms)),
             "droplet_steps_per_batch": steps_total, "erode_steps_per_batch": erode_steps,
-            "roofline": roof, "cpu_baseline": cpu, "clocks": cs, "measured_peaks": peaks,
+            "roofline": roof, "stage_roofline": stage_roof, "cpu_baseline": cpu, "clocks": cs,
+            "measured_peaks": peaks,
             "serving": serving,
             "biomemap": biomemap,
             "splatmap": splatmap,
@@ -739,6 +743,43 @@ def uneven_batch_section(m, np, torch, reps=3):
                                 "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
                                 "noise_block": stage_tune[2],
                                 "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()}}}
+
+
+def stage_rooflines(m, np, torch, dev, host_biome, table, stage_ms, stage_names, peak, peak_kind, peaks):
+    """The batch's filter and noise stages against their own bounds, from the stage times of the
+    timed region.  Filter (HBM): per chunk 2 (W+2r)(H+2r) bytes of samples read, 4 (WH+1) bytes of
+    offsets and 8 bytes per bin written.  Noise (FP32 pipe): per bin 60 flops per octave of its
+    biome + 4, and 8 per pixel (an FMA counts two).  The bins are counted by the library's filter
+    on the same 3x3 chunk neighbourhoods of each request's biome region, outside the timed region."""
+    S, r = MAP, RADIUS
+    octave = torch.from_numpy(table["Octave"].astype(np.int64)).cuda()
+    ws = dev.shf_workspace((S, S), (3, 3), r, BIOMES)
+    nbins = 0
+    noise_flops = 0
+    for region in host_biome:
+        reg = torch.from_numpy(region.view(np.int16)).cuda()
+        for c in range(9):
+            cx, cy = c % 3, c // 3
+            sub = reg[cy * S:cy * S + 3 * S, cx * S:cx * S + 3 * S].contiguous()
+            off, bins, st = dev.shf_filter(sub, (S, S), (3, 3), r, max_items=BIOMES, workspace=ws)
+            n = int(off[-1].item())
+            items = (bins[:n] & 0xFFFF).long()
+            nbins += n
+            noise_flops += int((60 * octave[items] + 4).sum().item()) + 8 * S * S
+    dev.status_check(st)
+    chunks = len(host_biome) * 9
+    shf_bytes = chunks * (2 * (S + 2 * r) ** 2 + 4 * (S * S + 1)) + 8 * nbins
+    ms = dict(zip(stage_names, stage_ms))
+    shf_gbs = shf_bytes / (ms["single_histogram_filter"] / 1000.0) / 1e9
+    noise_tf = noise_flops / (ms["multibiome_noise"] / 1000.0) / 1e12
+    fp32 = peaks["fp32_fma_tflops"]
+    return {
+        "single_histogram_filter": {"bound": "hbm", "achieved": shf_gbs, "peak": peak, "unit": "GB/s",
+                                    "frac": shf_gbs / peak, "peak_source": peak_kind,
+                                    "algorithmic_bytes_per_launch": shf_bytes, "bins_per_launch": nbins},
+        "multibiome_noise": {"bound": "fp32", "achieved": noise_tf, "peak": fp32, "unit": "TFLOP/s",
+                             "frac": noise_tf / fp32, "peak_source": "measured FP32 FMA rate (measured_peaks)",
+                             "algorithmic_flops_per_launch": noise_flops}}
 
 
 def large_field_section(m, np, torch, reps=3):
