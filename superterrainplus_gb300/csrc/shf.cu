@@ -66,7 +66,7 @@ constexpr uint32_t kResolved = 0x80000000u;
 __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict__ jobs, const ShfJob single,
 	const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
-	if (shf_job_fast(J)) {
+	if (!shf_job_general(J)) {
 		return; // filtered by the few-values path
 	}
 	const uint32_t ncols = J.W + 2u * J.r;
@@ -218,7 +218,7 @@ template<bool Write>
 __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restrict__ jobs, const ShfJob single,
 	const uint32_t kcap_v, const uint32_t kcap, const uint32_t segs, const uint32_t seg_len) {
 	const ShfJob& J = pick(jobs, single);
-	if (shf_job_fast(J)) {
+	if (!shf_job_general(J)) {
 		return;
 	}
 	const uint32_t t = blockIdx.x * kHBlock + threadIdx.x;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restrict__ jobs, const ShfJob single,
 	const uint32_t segs_slide) {
 	const ShfJob& J = pick(jobs, single);
-	const uint32_t segs = shf_job_fast(J) ? 1u : segs_slide;
+	const uint32_t segs = shf_job_general(J) ? segs_slide : 1u;
 	const uint32_t slots = J.H * segs;
 	__shared__ uint64_t warp_sum[kScanBlock / 32u];
 	__shared__ uint64_t carry_s;
@@ -753,7 +753,7 @@ int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max
 	STPGB_CUDA_TRY(cudaMemcpyAsync(&rec, static_cast<const unsigned char*>(workspace) + l.fast, sizeof(rec),
 		cudaMemcpyDeviceToHost, s));
 	STPGB_CUDA_TRY(cudaStreamSynchronize(s));
-	*path = rec.mode == kShfModeFast ? rec.pad0 : 0u;
+	*path = rec.mode == kShfModeSlide ? 0u : rec.pad0;
 	return STPGB_OK;
 }
 

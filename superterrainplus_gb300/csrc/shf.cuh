@@ -40,6 +40,7 @@ struct ShfJob {
 // column and row, or per band) overlay `vbuf`, which that chunk does not
 // otherwise use.
 constexpr uint32_t kShfFastItems = 8u;
+// A job's path: the general slides or the few-values path.
 constexpr uint32_t kShfModeSlide = 0u, kShfModeFast = 1u;
 // Rows of the read region per palette tile.
 constexpr uint32_t kShfPaletteRows = 32u;
@@ -56,8 +57,9 @@ struct ShfFastRecord {
 };
 static_assert(sizeof(ShfFastRecord) == 32u, "record is 8 words");
 
-__device__ __forceinline__ bool shf_job_fast(const ShfJob& J) {
-	return reinterpret_cast<const ShfFastRecord*>(J.fast)->mode == kShfModeFast;
+// the general slides' kernels filter only the jobs routed to them
+__device__ __forceinline__ bool shf_job_general(const ShfJob& J) {
+	return reinterpret_cast<const volatile ShfFastRecord*>(J.fast)->mode == kShfModeSlide;
 }
 
 struct ShfLayout {
@@ -90,7 +92,7 @@ struct ShfBandLaunch {
 };
 struct ShfFastPlan {
 	bool bands;
-	uint32_t max_cols; // widest chunk (W + 2r) the few-values path takes; 0: none
+	uint32_t max_cols; // widest chunk (W + 2r) the dense path takes; 0: none
 	ShfBandLaunch band;
 };
 // stpgb_shf_set_path's choice (0 = by size)
@@ -105,7 +107,7 @@ int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint
 // the row-band formulation (shf_band.cu)
 ShfBandLaunch shf_band_config(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
 int shf_band_carry_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_r,
-	uint32_t kcap_h, uint32_t max_cols, const ShfBandLaunch& cfg, cudaStream_t stream);
+	const ShfBandLaunch& cfg, cudaStream_t stream);
 int shf_band_rows_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, const ShfBandLaunch& cfg,
 	bool write, cudaStream_t stream);
 

@@ -16,10 +16,9 @@
 // over the columns of a row: one sum scan and one max scan of eight 16-bit
 // fields per column, so a block computes a whole row at once.
 //
-//   shf_band_carry thread per column: merges the palette tiles (every block
-//                  does, block 0 records the job's path), then slides the
-//                  column's vertical histogram down all rows and keeps its
-//                  state at the first row of every band.
+//   shf_band_carry thread per column: slides the column's vertical histogram
+//                  down all rows and keeps its state at the first row of
+//                  every band.
 //   shf_band_rows  block per (band of rows, job), thread per column(s): per
 //                  row, the vertical step, the count scan, the insertion scan
 //                  and the pixels' bins (COUNT: bins per row; WRITE: offsets
@@ -44,26 +43,15 @@ constexpr uint32_t kFastMaxThreads = 1024u;
 // slides it (:522-563), stored at y = 0, band_rows, 2 band_rows, ...:
 // counts [bands][W+2r] (8 bytes), then orders [bands][W+2r] (4-bit indices).
 __global__ void __launch_bounds__(kCarryBlock) shf_band_carry(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t kcap_h, const uint32_t max_cols, const uint32_t band_rows) {
+	const uint32_t band_rows) {
 	const ShfJob& J = pick(jobs, single);
-	__shared__ uint32_t s_mode, s_count, s_val[kShfFastItems];
-	if (threadIdx.x == 0u) {
-		uint32_t vals[kShfFastItems];
-		merge_palette(J, kcap_h, max_cols, s_mode, s_count, vals);
-		for (uint32_t j = 0u; j < kShfFastItems; j++) {
-			s_val[j] = vals[j];
-		}
-		if (blockIdx.x == 0u) {
-			write_record(J, s_mode, s_count, vals, kShfFormBands);
-		}
-	}
-	__syncthreads();
+	const ShfFastRecord* const rec = reinterpret_cast<const ShfFastRecord*>(J.fast);
 	const uint32_t NC = J.W + 2u * J.r;
 	const uint32_t k = blockIdx.x * kCarryBlock + threadIdx.x;
-	if (s_mode != kShfModeFast || k >= NC) {
+	if (rec->mode != kShfModeFast || k >= NC) {
 		return;
 	}
-	const Palette pal = make_palette(s_val, s_count);
+	const Palette pal = record_palette(rec);
 	const uint16_t* const col = read_region(J) + k;
 	const uint64_t pitch = J.pitch;
 	const uint32_t H = J.H, r2 = 2u * J.r;
@@ -472,11 +460,10 @@ ShfBandLaunch shf_band_config(const uint32_t njobs, const uint32_t max_W, const 
 }
 
 int shf_band_carry_launch(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const uint32_t max_W,
-	const uint32_t max_r, const uint32_t kcap_h, const uint32_t max_cols, const ShfBandLaunch& cfg,
-	cudaStream_t stream) {
+	const uint32_t max_r, const ShfBandLaunch& cfg, cudaStream_t stream) {
 	const uint32_t ncols = max_W + 2u * max_r;
 	shf_band_carry<<<dim3((ncols + kCarryBlock - 1u) / kCarryBlock, njobs), kCarryBlock, 0, stream>>>(jobs, single,
-		kcap_h, std::min(max_cols, kShfBandMaxCols), cfg.band_rows);
+		cfg.band_rows);
 	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }

@@ -16,10 +16,10 @@
 //   shf_palette       block per (32-row tile of the read region, job):
 //                     distinct values through a 65536-bit map in shared
 //                     memory.
-//   shf_vertical_fast thread per column: merges the palette tiles (every
-//                     block does, block 0 records the job's path), slides the
-//                     column's vertical histogram down all rows and writes it
-//                     to row-major planes in the job's vbuf.
+//   shf_route         thread per job: the path (few-values or general).
+//   shf_vertical_fast thread per column: slides the column's vertical
+//                     histogram down all rows and writes it to row-major
+//                     planes in the job's vbuf.
 //   shf_rows_fast     thread per row: the horizontal slide; COUNT writes the
 //                     bins per row (before the row scan), WRITE the offsets
 //                     and bins (after it).
@@ -43,6 +43,31 @@ constexpr uint32_t kRing = 256u;
 // Launches with fewer rows than this many per SM (rows of all chunks) take
 // the row bands: one thread per row would leave the SMs nearly idle.
 constexpr uint64_t kSlideRowsPerSM = 256u;
+
+// ---------------------------------------------------------------- routing --
+
+// Thread 0 per job: the union of its palette tiles decides its path -- the
+// few-values path when it holds at most kShfFastItems values, no accumulator
+// of the reference could overflow and the chunk is within the formulation's
+// column bound, else the general slides.
+__global__ void shf_route(const ShfJob* __restrict__ jobs, const ShfJob single, const uint32_t kcap_h,
+	const uint32_t dense_max_cols, const uint32_t dense_form) {
+	const ShfJob& J = pick(jobs, single);
+	if (threadIdx.x != 0u) {
+		return;
+	}
+	uint32_t vals[kShfFastItems];
+	uint32_t n = 0u;
+	const bool fits = palette_union(J, vals, n);
+	const uint64_t side = 2ull * J.r + 1u;
+	const uint64_t items = n;
+	const bool radius_ok = J.r <= kFastMaxRadius;
+	// the packed vertical histograms (12 bytes per column and row, or per band) fit in vbuf
+	// (4 * kcap_v bytes per column and row)
+	const bool dense = fits && radius_ok && J.W + 2u * J.r <= dense_max_cols
+		&& min(items, side + 1u) <= J.kcap_v && min(items, (side + 1u) * side) <= kcap_h && J.kcap_v >= 3u;
+	write_record(J, dense ? kShfModeFast : kShfModeSlide, dense ? n : 0u, vals, dense_form);
+}
 
 // ---------------------------------------------------------------- palette --
 
@@ -124,28 +149,16 @@ __global__ void __launch_bounds__(kPaletteBlock) shf_palette(const ShfJob* __res
 // that a warp's stores are consecutive.  The local indices of a column's last
 // kRing samples stay in shared memory, so only the entering sample is read
 // from global memory, kVertAhead rows early.
-__global__ void __launch_bounds__(kVertBlock) shf_vertical_fast(const ShfJob* __restrict__ jobs, const ShfJob single,
-	const uint32_t kcap_h, const uint32_t max_cols) {
+__global__ void __launch_bounds__(kVertBlock) shf_vertical_fast(const ShfJob* __restrict__ jobs, const ShfJob single) {
 	const ShfJob& J = pick(jobs, single);
-	__shared__ uint32_t s_mode, s_count, s_val[kShfFastItems];
+	const ShfFastRecord* const rec = reinterpret_cast<const ShfFastRecord*>(J.fast);
 	__shared__ uint8_t ring[kRing][kVertBlock];
-	if (threadIdx.x == 0u) {
-		uint32_t vals[kShfFastItems];
-		merge_palette(J, kcap_h, max_cols, s_mode, s_count, vals);
-		for (uint32_t j = 0u; j < kShfFastItems; j++) {
-			s_val[j] = vals[j];
-		}
-		if (blockIdx.x == 0u) {
-			write_record(J, s_mode, s_count, vals, kShfFormSlides);
-		}
-	}
-	__syncthreads();
 	const uint32_t NC = J.W + 2u * J.r;
 	const uint32_t k = blockIdx.x * kVertBlock + threadIdx.x;
-	if (s_mode != kShfModeFast || k >= NC) {
+	if (rec->mode != kShfModeFast || k >= NC) {
 		return;
 	}
-	const Palette pal = make_palette(s_val, s_count);
+	const Palette pal = record_palette(rec);
 	const uint64_t pitch = J.pitch;
 	const uint32_t H = J.H, r2 = 2u * J.r;
 	const uint16_t* src = read_region(J) + k; // the next sample to load
@@ -406,28 +419,33 @@ int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, const uint32_t nj
 	const uint32_t tiles = (max_H + 2u * max_r + kShfPaletteRows - 1u) / kShfPaletteRows;
 	shf_palette<<<dim3(tiles, njobs), kPaletteBlock, 0, stream>>>(jobs, single);
 	STPGB_CUDA_TRY(cudaGetLastError());
-	if (plan.bands) {
-		return shf_band_carry_launch(jobs, single, njobs, max_W, max_r, kcap_h, plan.max_cols, plan.band, stream);
-	}
-	const uint32_t ncols = max_W + 2u * max_r;
-	shf_vertical_fast<<<dim3((ncols + kVertBlock - 1u) / kVertBlock, njobs), kVertBlock, 0, stream>>>(jobs, single,
-		kcap_h, plan.max_cols);
+	shf_route<<<dim3(1u, njobs), 32u, 0, stream>>>(jobs, single, kcap_h, plan.max_cols,
+		plan.bands ? kShfFormBands : kShfFormSlides);
 	STPGB_CUDA_TRY(cudaGetLastError());
+	if (plan.bands) {
+		STPGB_TRY(shf_band_carry_launch(jobs, single, njobs, max_W, max_r, plan.band, stream));
+	} else {
+		const uint32_t ncols = max_W + 2u * max_r;
+		shf_vertical_fast<<<dim3((ncols + kVertBlock - 1u) / kVertBlock, njobs), kVertBlock, 0, stream>>>(jobs,
+			single);
+		STPGB_CUDA_TRY(cudaGetLastError());
+	}
 	return STPGB_OK;
 }
 
 int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, const uint32_t njobs, const uint32_t max_H,
 	const ShfFastPlan& plan, const bool write, cudaStream_t stream) {
 	if (plan.bands) {
-		return shf_band_rows_launch(jobs, single, njobs, plan.band, write, stream);
-	}
-	const dim3 grid((max_H + kRowBlock - 1u) / kRowBlock, njobs);
-	if (write) {
-		shf_rows_fast<true><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+		STPGB_TRY(shf_band_rows_launch(jobs, single, njobs, plan.band, write, stream));
 	} else {
-		shf_rows_fast<false><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+		const dim3 grid((max_H + kRowBlock - 1u) / kRowBlock, njobs);
+		if (write) {
+			shf_rows_fast<true><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+		} else {
+			shf_rows_fast<false><<<grid, kRowBlock, 0, stream>>>(jobs, single);
+		}
+		STPGB_CUDA_TRY(cudaGetLastError());
 	}
-	STPGB_CUDA_TRY(cudaGetLastError());
 	return STPGB_OK;
 }
 

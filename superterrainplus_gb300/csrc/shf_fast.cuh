@@ -86,14 +86,13 @@ __device__ __forceinline__ uint32_t local_index(const Palette p, const uint32_t 
 		>> 4;
 }
 
-// Union of a job's palette slots, ascending; kShfModeFast when it has at most
-// kShfFastItems values and the job fits the path (at most max_cols columns).
-__device__ __forceinline__ void merge_palette(const ShfJob& J, const uint32_t kcap_h, const uint32_t max_cols,
-	uint32_t& mode, uint32_t& count, uint32_t* const vals) {
+// Union of a job's palette slots, ascending, in vals[0..n) (kNoValue after);
+// false when a tile or the union holds more than kShfFastItems values.
+__device__ __forceinline__ bool palette_union(const ShfJob& J, uint32_t* const vals, uint32_t& n) {
 	const uint32_t NR = J.H + 2u * J.r;
 	const uint32_t tiles = (NR + kShfPaletteRows - 1u) / kShfPaletteRows;
-	uint32_t n = 0u;
-	bool ok = J.r <= kFastMaxRadius && J.W + 2u * J.r <= max_cols;
+	n = 0u;
+	bool ok = true;
 	for (uint32_t t = 0u; t < tiles && ok; t++) {
 		const uint32_t* const slot = J.fast + kSlotWords * (1u + t);
 		const uint32_t c = slot[0];
@@ -121,27 +120,30 @@ __device__ __forceinline__ void merge_palette(const ShfJob& J, const uint32_t kc
 			n++;
 		}
 	}
-	// No accumulator of the slides could overflow (a vertical one holds at most
-	// 2r+2 samples, a horizontal one (2r+2)(2r+1)), and 12 bytes per column and
-	// row fit in vbuf (4 * kcap_v): the packed vertical histograms of every row,
-	// or of every band's first row.
-	const uint64_t side = 2ull * J.r + 1u;
-	const uint64_t items = n;
-	ok = ok && min(items, side + 1u) <= J.kcap_v && min(items, (side + 1u) * side) <= kcap_h && J.kcap_v >= 3u;
 	for (uint32_t j = n; j < kShfFastItems; j++) {
 		vals[j] = kNoValue;
 	}
-	mode = ok ? kShfModeFast : kShfModeSlide;
-	count = n;
+	return ok;
 }
 
-// the job's path record (block 0 of the merging kernel writes it)
+// The palette of a job routed to the dense path, from its record.
+__device__ __forceinline__ Palette record_palette(const ShfFastRecord* const rec) {
+	const uint32_t n = rec->count;
+	const uint32_t* const rw = reinterpret_cast<const uint32_t*>(rec->item);
+	auto half = [&](const uint32_t j) {
+		return j < n ? ((rw[j / 2u] >> (16u * (j & 1u))) & 0xFFFFu) : 0xFFFFu;
+	};
+	return make_uint4(half(0) | (half(1) << 16), half(2) | (half(3) << 16), half(4) | (half(5) << 16),
+		half(6) | (half(7) << 16));
+}
+
+// the job's path record (the routing kernel writes it)
 __device__ __forceinline__ void write_record(const ShfJob& J, const uint32_t mode, const uint32_t count,
 	const uint32_t* const vals, const uint32_t form) {
 	ShfFastRecord* const rec = reinterpret_cast<ShfFastRecord*>(J.fast);
 	rec->mode = mode;
 	rec->count = count;
-	rec->pad0 = mode == kShfModeFast ? form : 0u;
+	rec->pad0 = mode == kShfModeSlide ? 0u : form;
 	rec->pad1 = 0u;
 	for (uint32_t j = 0u; j < kShfFastItems; j++) {
 		rec->item[j] = static_cast<uint16_t>(j < count ? vals[j] : 0u);
