@@ -383,6 +383,7 @@ def run_ours(args):
     batch.tune()
     lanes, tune_ms = batch.tuning()
     stage_tune = batch.tuning_stages()
+    filter_path = batch.tuning_filter_path()
 
     def barrier():
         torch.cuda.synchronize()
@@ -593,7 +594,11 @@ def run_ours(args):
             "splatmap": splatmap,
             "large_field": large,
             "uneven_batch": uneven,
-            "autotune": {"filter_segments": stage_tune[0],
+            "autotune": {"filter_path": filter_path[0],
+                         "filter_ms_by_path": {str(k): v for k, v in filter_path[1].items()},
+                         "filter_path_names": "0 by launch size, 1 few-values packed slides, 2 few-values "
+                                              "row bands, 3 general slides",
+                         "filter_segments": stage_tune[0],
                          "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
                          "noise_block": stage_tune[2],
                          "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()},
@@ -703,6 +708,7 @@ def uneven_batch_section(m, np, torch, reps=3):
     b.tune()
     choice, tune_ms = b.tuning()
     stage_tune = b.tuning_stages()
+    filter_path = b.tuning_filter_path()
     st = torch.cuda.current_stream()
     for _ in range(3):
         b.run()
@@ -739,7 +745,9 @@ def uneven_batch_section(m, np, torch, reps=3):
                                  stage_ms)),
             "autotune_dominant_group": {"lanes_per_droplet": choice[0], "droplets_per_group": choice[1],
                                         "brush_rows": bool(choice[2])},
-            "autotune_stages": {"filter_segments": stage_tune[0],
+            "autotune_stages": {"filter_path": filter_path[0],
+                                "filter_ms_by_path": {str(k): v for k, v in filter_path[1].items()},
+                                "filter_segments": stage_tune[0],
                                 "filter_ms_by_segments": {str(k): v for k, v in stage_tune[1].items()},
                                 "noise_block": stage_tune[2],
                                 "noise_ms_by_block": {str(k): v for k, v in stage_tune[3].items()}}}

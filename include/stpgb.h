@@ -752,6 +752,12 @@ STPGB_API int stpgb_batch_tuning(const stpgb_batch* batch, uint32_t* lanes_per_d
 STPGB_API int stpgb_batch_tuning_stages(const stpgb_batch* batch, uint32_t* shf_segments, float* shf_ms,
 	uint32_t* noise_block, float* noise_ms, uint32_t* coop_interleave);
 
+/* No counterpart in the reference.  The filter path the autotuner chose for
+ * the batch (`*path`: 0 by launch size, 1 few-values packed slides, 2 few-values
+ * row bands, 3 general slides; see stpgb_shf_set_path) and the filter stage's
+ * time with each (`path_ms`, 4 floats; zeros before tuning). */
+STPGB_API int stpgb_batch_tuning_filter_path(const stpgb_batch* batch, uint32_t* path, float* path_ms);
+
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */
 STPGB_API int stpgb_batch_counters(stpgb_batch* batch, uint64_t* realised_steps, uint64_t* erode_steps,

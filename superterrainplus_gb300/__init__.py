@@ -524,6 +524,14 @@ class Batch:
         return (seg.value, {c: sms[i] for i, c in enumerate((0, 1, 2, 4, 8, 16)) if sms[i] > 0},
                 blk.value, {c: nms[i] for i, c in enumerate((128, 256, 512)) if nms[i] > 0}, q.value)
 
+    def tuning_filter_path(self):
+        """The filter path the autotuner chose (0 by size, 1 few-values packed slides, 2 row bands,
+        3 general slides) and {path: ms} for the ones it timed."""
+        p = C.c_uint32(0)
+        ms = (C.c_float * 4)()
+        check(lib().stpgb_batch_tuning_filter_path(self._h, C.byref(p), ms))
+        return p.value, {c: ms[c] for c in range(4) if ms[c] > 0}
+
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)
         check(lib().stpgb_batch_counters(self._h, C.byref(a), C.byref(b), int(reset)))

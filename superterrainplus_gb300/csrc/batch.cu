@@ -143,13 +143,15 @@ struct stpgb_batch {
 	std::vector<ErosionJob> ero_h; // per request, request order (the plain sequence)
 	std::vector<FormatJob> fmt_h;
 	uint32_t max_S = 0u, max_r = 0u, kcap_v = 0u, kcap_h = 0u;
-	// the filter's segment count (0 = from the launch size) and the noise
-	// kernel's block size, chosen by the autotuner; its times per candidate
-	static constexpr uint32_t kShfSegCands = 6u, kNoiseBlockCands = 3u;
+	// the filter's path (0 = by size, 1 few-values packed slides, 2 row bands,
+	// 3 general slides), the general slides' segment count (0 = from the
+	// launch size) and the noise kernel's block size, chosen by the autotuner;
+	// its times per candidate
+	static constexpr uint32_t kShfPathCands = 4u, kShfSegCands = 6u, kNoiseBlockCands = 3u;
 	static constexpr uint32_t shf_seg_cands[kShfSegCands] = { 0u, 1u, 2u, 4u, 8u, 16u };
 	static constexpr uint32_t noise_block_cands[kNoiseBlockCands] = { 128u, 256u, 512u };
-	uint32_t shf_segments = 0u, noise_block = 256u;
-	float shf_tune_ms[kShfSegCands] = {}, noise_tune_ms[kNoiseBlockCands] = {};
+	uint32_t shf_path = 0u, shf_segments = 0u, noise_block = 256u;
+	float shf_path_ms[kShfPathCands] = {}, shf_tune_ms[kShfSegCands] = {}, noise_tune_ms[kNoiseBlockCands] = {};
 	// erosion variant groups (brush rows in 16-byte blocks need aligned maps:
 	// every merged map of a batch is 512-byte aligned with a pitch of
 	// 3 * MapSize, a multiple of 24 floats); group_of[n] is request n's group
@@ -273,7 +275,8 @@ struct stpgb_batch {
 		const uint32_t nchunks = static_cast<uint32_t>(shf_h.size());
 		switch (st) {
 		case 0u:
-			return shf_launch(shf_jobs, shf_h[0], nchunks, max_S, max_S, max_r, kcap_v, kcap_h, s, shf_segments);
+			return shf_launch(shf_jobs, shf_h[0], nchunks, max_S, max_S, max_r, kcap_v, kcap_h, s, shf_segments,
+				shf_path);
 		case 1u:
 			return noise_launch(noise_jobs, noise_h[0], nchunks, static_cast<uint64_t>(max_S) * max_S, permutation,
 				table, biome_count, s, noise_block);
@@ -313,6 +316,17 @@ struct stpgb_batch {
 				}
 			}
 		};
+		float best_path = 0.0f;
+		uint32_t pick_path = shf_path;
+		for (uint32_t c = 0u; c < kShfPathCands && rc == STPGB_OK; c++) {
+			shf_path = c;
+			time_stage(0u, shf_path_ms[c]);
+			if (rc == STPGB_OK && (best_path == 0.0f || shf_path_ms[c] < best_path)) {
+				best_path = shf_path_ms[c];
+				pick_path = shf_path;
+			}
+		}
+		shf_path = pick_path;
 		float best_shf = 0.0f;
 		uint32_t pick_seg = shf_segments;
 		for (uint32_t c = 0u; c < kShfSegCands && rc == STPGB_OK; c++) {
@@ -880,6 +894,19 @@ int stpgb_batch_tuning_stages(const stpgb_batch* b, uint32_t* shf_segments, floa
 	}
 	for (uint32_t c = 0u; c < stpgb_batch::kNoiseBlockCands && noise_ms; c++) {
 		noise_ms[c] = b->noise_tune_ms[c];
+	}
+	return STPGB_OK;
+}
+
+int stpgb_batch_tuning_filter_path(const stpgb_batch* b, uint32_t* path, float* path_ms) {
+	if (!b) {
+		return inval("stpgb_batch_tuning_filter_path: null batch");
+	}
+	if (path) {
+		*path = b->shf_path;
+	}
+	for (uint32_t c = 0u; c < stpgb_batch::kShfPathCands && path_ms; c++) {
+		path_ms[c] = b->shf_path_ms[c];
 	}
 	return STPGB_OK;
 }

@@ -608,7 +608,8 @@ void shf_bind_workspace(ShfJob& job, unsigned char* ws, const ShfLayout& l) {
 }
 
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
-	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, const uint32_t segments_wanted) {
+	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, const uint32_t segments_wanted,
+	const uint32_t path) {
 	STPGB_TRY(once_per_device(SETUP_SHF_SMEM, shf_set_smem_attributes));
 	const uint64_t target_threads = uint64_t { current_sm_count() } * kShfThreadsPerSM;
 	// Segments per column / row: enough threads to fill the GPU when few
@@ -637,7 +638,7 @@ int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_
 	// Every job first takes the palette of its read region: at most
 	// kShfFastItems values go the few-values path (shf_fast.cu), the others
 	// the sequential slides; each kernel returns at once for jobs of the other.
-	const ShfFastPlan fast = shf_fast_plan(njobs, max_W, max_H, max_r);
+	const ShfFastPlan fast = shf_fast_plan(njobs, max_W, max_H, max_r, path);
 	STPGB_TRY(shf_fast_prepare(jobs, single, njobs, max_W, max_H, max_r, kcap_h, fast, stream));
 	STPGB_TRY(shf_fast_pass(jobs, single, njobs, max_H, fast, false, stream));
 	shf_vertical<<<vgrid, kVBlock, vsmem, stream>>>(jobs, single, kcap_v, segs_v, len_v);

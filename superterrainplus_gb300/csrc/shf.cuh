@@ -75,10 +75,14 @@ uint32_t shf_kcap_h(uint32_t r, uint32_t max_items);
 
 // Runs the whole filter for `njobs` jobs (device array `jobs`, or `single`
 // when jobs == nullptr). max_W/max_H/max_r bound the grids.
-// `segments`: columns and rows cut into this many segments (clamped to
-// [1, kShfMaxSegments] and the slide length); 0 = chosen from the launch size.
+// `segments`: the general slides' columns and rows cut into this many
+// segments (clamped to [1, kShfMaxSegments] and the slide length); 0 = chosen
+// from the launch size.  `path`: 0 = the process-wide choice
+// (stpgb_shf_set_path, by size by default), else that choice for this launch
+// (1 packed slides, 2 row bands, 3 general slides).
 int shf_launch(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
-	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, uint32_t segments = 0u);
+	uint32_t max_r, uint32_t kcap_v, uint32_t kcap_h, cudaStream_t stream, uint32_t segments = 0u,
+	uint32_t path = 0u);
 
 // The few-values path's launches around the general slides: palette and
 // vertical histograms, then the bin count per row (before the row scan), and
@@ -99,7 +103,7 @@ struct ShfFastPlan {
 uint32_t shf_path_override();
 // the record's pad0: the formulation that filtered the job
 constexpr uint32_t kShfFormSlides = 1u, kShfFormBands = 2u;
-ShfFastPlan shf_fast_plan(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r);
+ShfFastPlan shf_fast_plan(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r, uint32_t path = 0u);
 int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,
 	uint32_t max_r, uint32_t kcap_h, const ShfFastPlan& plan, cudaStream_t stream);
 int shf_fast_pass(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_H, const ShfFastPlan& plan,

@@ -402,9 +402,10 @@ __global__ void __launch_bounds__(kRowBlock) shf_rows_fast(const ShfJob* __restr
 
 } // namespace
 
-ShfFastPlan shf_fast_plan(const uint32_t njobs, const uint32_t max_W, const uint32_t max_H, const uint32_t max_r) {
+ShfFastPlan shf_fast_plan(const uint32_t njobs, const uint32_t max_W, const uint32_t max_H, const uint32_t max_r,
+	const uint32_t path) {
 	ShfFastPlan plan {};
-	const uint32_t choice = shf_path_override();
+	const uint32_t choice = path != 0u ? path : shf_path_override();
 	plan.bands = choice == 2u
 		|| (choice == 0u && static_cast<uint64_t>(njobs) * max_H < kSlideRowsPerSM * current_sm_count());
 	plan.max_cols = choice == 3u ? 0u : plan.bands ? kShfBandMaxCols : 0xFFFFFFFFu;

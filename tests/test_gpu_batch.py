@@ -42,7 +42,8 @@ def heights(b):
 @pytest.mark.parametrize("tune,form", [(False, 0), (True, 0), (False, 1), (False, 3)])
 def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, shf_path, tune, form):
     """Inputs bit-exact, heights within 2e-6 of the oracle, with the default filter segments and
-    noise block or with the autotuner's choice of both (every candidate was timed); the filter's
+    noise block or with the autotuner's choice of them and of the filter's path (every candidate
+    was timed); the filter's
     path by launch size (this batch of 36 chunks: the few-values row bands), forced to the
     few-values packed slides, or forced to the general slides."""
     shf_path(form)
@@ -52,6 +53,8 @@ def test_batch_inputs_filter_noise_vs_oracle(stpgb, dev, oracle, shf_path, tune,
         seg, seg_ms, block, block_ms, _ = b.tuning_stages()
         assert set(seg_ms) == {0, 1, 2, 4, 8, 16} and seg in seg_ms
         assert set(block_ms) == {128, 256, 512} and block in block_ms
+        path, path_ms = b.tuning_filter_path()
+        assert set(path_ms) == {0, 1, 2, 3} and path in path_ms
     regions = [np.zeros((5 * r["MapSize"], 5 * r["MapSize"]), np.uint16) for r in REQS]
     starts = [np.zeros(2 * r["DropletCount"], np.float32) for r in REQS]
     b.download_inputs(regions, starts)
