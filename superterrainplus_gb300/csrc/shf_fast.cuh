@@ -70,13 +70,6 @@ __device__ __forceinline__ void hist_sub(uint64_t& cnt, uint32_t& order, const u
 // ascending, 0xFFFF past the count.
 using Palette = uint4;
 
-__device__ __forceinline__ Palette make_palette(const uint32_t* const vals, const uint32_t n) {
-	auto at = [&](const uint32_t j) {
-		return j < n ? (vals[j] & 0xFFFFu) : 0xFFFFu;
-	};
-	return make_uint4(at(0) | (at(1) << 16), at(2) | (at(3) << 16), at(4) | (at(5) << 16), at(6) | (at(7) << 16));
-}
-
 // local index of a palette value: the number of palette values below it
 // (a padding field, 0xFFFF, is never below a 16-bit value)
 __device__ __forceinline__ uint32_t local_index(const Palette p, const uint32_t v) {
