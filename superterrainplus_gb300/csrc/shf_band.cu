@@ -35,6 +35,10 @@ namespace {
 
 constexpr uint32_t kCarryBlock = 64u;
 constexpr uint32_t kFastMaxThreads = 1024u;
+// rows of the carry's slide whose entering samples are loaded ahead of their
+// use, and the ring of a column's last samples (>= 2r+2)
+constexpr uint32_t kAhead = 16u;
+constexpr uint32_t kRing = 256u;
 
 // ------------------------------------------------------------------ carry --
 
@@ -61,41 +65,50 @@ __global__ void __launch_bounds__(kCarryBlock) shf_band_carry(const ShfJob* __re
 	auto at = [&](const uint32_t q) {
 		return static_cast<uint32_t>(__ldg(col + static_cast<uint64_t>(q) * pitch));
 	};
+	// the local indices of the column's last kRing samples: the leaving sample
+	// of a row is read from here, only the entering one from global memory,
+	// kAhead rows early
+	__shared__ uint8_t ring[kRing][kCarryBlock];
+	uint8_t* const mine = &ring[0][threadIdx.x];
 	uint64_t cnt = 0ull;
 	uint32_t order = 0u;
 	for (uint32_t q = 0u; q <= r2; q++) {
-		hist_add(cnt, order, local_index(pal, at(q)));
+		const uint32_t li = local_index(pal, at(q));
+		mine[(q & (kRing - 1u)) * kCarryBlock] = static_cast<uint8_t>(li);
+		hist_add(cnt, order, li);
 	}
 	cvc[k] = cnt;
 	cvo[k] = order;
-	// row y adds region row y+2r and removes row y-1; the samples of the next
-	// four rows are loaded ahead (they do not depend on the histogram)
-	constexpr uint32_t kAhead = 4u;
-	uint32_t ra[kAhead], rb[kAhead];
+	// row y adds region row y+2r and removes row y-1
+	const uint16_t* src = col + static_cast<uint64_t>(r2 + 1u + kAhead) * pitch;
+	uint32_t pre[kAhead];
 #pragma unroll
 	for (uint32_t i = 0u; i < kAhead; i++) {
-		const uint32_t y = 1u + i;
-		ra[i] = y < H ? at(y + r2) : 0u;
-		rb[i] = y < H ? at(y - 1u) : 0u;
+		pre[i] = 1u + i < H ? at(r2 + 1u + i) : 0u;
 	}
+	uint32_t next_band = band_rows; // rows before the next band's first row
+	size_t band_at = NC + k;
 	for (uint32_t y = 1u; y < H; y += kAhead) {
 #pragma unroll
 		for (uint32_t i = 0u; i < kAhead; i++) {
 			const uint32_t yy = y + i;
 			if (yy < H) {
-				const uint32_t a = ra[i], b = rb[i];
+				const uint32_t li = local_index(pal, pre[i]);
 				if (yy + kAhead < H) {
-					ra[i] = at(yy + kAhead + r2);
-					rb[i] = at(yy + kAhead - 1u);
+					pre[i] = __ldg(src);
 				}
-				if (a != b) {
-					hist_add(cnt, order, local_index(pal, a));
-					hist_sub(cnt, order, local_index(pal, b));
+				src += pitch;
+				const uint32_t lo = mine[((yy - 1u) & (kRing - 1u)) * kCarryBlock];
+				mine[((yy + r2) & (kRing - 1u)) * kCarryBlock] = static_cast<uint8_t>(li);
+				if (li != lo) {
+					hist_add(cnt, order, li);
+					hist_sub(cnt, order, lo);
 				}
-				if (yy % band_rows == 0u) {
-					const size_t o = static_cast<size_t>(yy / band_rows) * NC + k;
-					cvc[o] = cnt;
-					cvo[o] = order;
+				if (--next_band == 0u) {
+					cvc[band_at] = cnt;
+					cvo[band_at] = order;
+					band_at += NC;
+					next_band = band_rows;
 				}
 			}
 		}
