@@ -754,7 +754,7 @@ int stpgb_shf_filter_path(const stpgb_nn_info* nn, uint32_t radius, uint32_t max
 	STPGB_CUDA_TRY(cudaMemcpyAsync(&rec, static_cast<const unsigned char*>(workspace) + l.fast, sizeof(rec),
 		cudaMemcpyDeviceToHost, s));
 	STPGB_CUDA_TRY(cudaStreamSynchronize(s));
-	*path = rec.mode == kShfModeSlide ? 0u : rec.pad0;
+	*path = rec.mode == kShfModeSlide ? 0u : rec.form;
 	return STPGB_OK;
 }
 

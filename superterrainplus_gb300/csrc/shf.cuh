@@ -49,10 +49,11 @@ constexpr uint32_t kShfPaletteRows = 32u;
 constexpr uint32_t kShfBandMaxCols = 4096u;
 constexpr uint32_t kShfBandMinRows = 4u;
 
-// Record of the path a job takes, written by the palette merge: words
-// {mode, distinct values, 0, 0, then the values as 8 uint16, ascending}.
+// Record of the path a job takes, written by the routing kernel: words
+// {mode, distinct values, formulation (kShfForm*, 0 for the general slides),
+// 0, then the values as 8 uint16, ascending}.
 struct ShfFastRecord {
-	uint32_t mode, count, pad0, pad1;
+	uint32_t mode, count, form, pad;
 	uint16_t item[kShfFastItems];
 };
 static_assert(sizeof(ShfFastRecord) == 32u, "record is 8 words");
@@ -101,7 +102,7 @@ struct ShfFastPlan {
 };
 // stpgb_shf_set_path's choice (0 = by size)
 uint32_t shf_path_override();
-// the record's pad0: the formulation that filtered the job
+// the record's form: the few-values formulation that filtered the job
 constexpr uint32_t kShfFormSlides = 1u, kShfFormBands = 2u;
 ShfFastPlan shf_fast_plan(uint32_t njobs, uint32_t max_W, uint32_t max_H, uint32_t max_r, uint32_t path = 0u);
 int shf_fast_prepare(const ShfJob* jobs, const ShfJob& single, uint32_t njobs, uint32_t max_W, uint32_t max_H,

@@ -136,8 +136,8 @@ __device__ __forceinline__ void write_record(const ShfJob& J, const uint32_t mod
 	ShfFastRecord* const rec = reinterpret_cast<ShfFastRecord*>(J.fast);
 	rec->mode = mode;
 	rec->count = count;
-	rec->pad0 = mode == kShfModeSlide ? 0u : form;
-	rec->pad1 = 0u;
+	rec->form = mode == kShfModeSlide ? 0u : form;
+	rec->pad = 0u;
 	for (uint32_t j = 0u; j < kShfFastItems; j++) {
 		rec->item[j] = static_cast<uint16_t>(j < count ? vals[j] : 0u);
 	}
