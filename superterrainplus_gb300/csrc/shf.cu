@@ -36,6 +36,8 @@ namespace stpgb {
 namespace {
 
 constexpr uint32_t kVBlock = 64u;
+// steps of the vertical slide whose samples are loaded ahead of their use
+constexpr uint32_t kVAhead = 8u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
 // threads per SM the segmented passes aim for
@@ -188,20 +190,32 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	emit(y_a);
 	// A step whose added and removed samples are equal leaves the accumulator
 	// as it was (the item is present throughout, so nothing is inserted or
-	// erased); the next step's two samples are loaded one step ahead.
-	uint32_t va = y_a + 1u < y_b ? at(static_cast<int>(y_a + 1u) + r) : 0u;
-	uint32_t vr = y_a + 1u < y_b ? at(static_cast<int>(y_a) - r) : 0u;
-	for (uint32_t y = y_a + 1u; y < y_b; y++) {
-		const uint32_t add = va, sub = vr;
-		if (y + 1u < y_b) {
-			va = at(static_cast<int>(y + 1u) + r);
-			vr = at(static_cast<int>(y) - r);
+	// erased); the two samples of a step are loaded kVAhead steps ahead (a
+	// ring of registers: the loads do not depend on the accumulator).
+	uint32_t va[kVAhead], vr[kVAhead];
+#pragma unroll
+	for (uint32_t i = 0u; i < kVAhead; i++) {
+		const uint32_t y = y_a + 1u + i;
+		va[i] = y < y_b ? at(static_cast<int>(y) + r) : 0u;
+		vr[i] = y < y_b ? at(static_cast<int>(y) - 1 - r) : 0u;
+	}
+	for (uint32_t y0 = y_a + 1u; y0 < y_b; y0 += kVAhead) {
+#pragma unroll
+		for (uint32_t i = 0u; i < kVAhead; i++) {
+			const uint32_t y = y0 + i;
+			if (y < y_b) {
+				const uint32_t add = va[i], sub = vr[i];
+				if (y + kVAhead < y_b) {
+					va[i] = at(static_cast<int>(y + kVAhead) + r);
+					vr[i] = at(static_cast<int>(y + kVAhead) - 1 - r);
+				}
+				if (add != sub) {
+					inc(add);
+					dec(sub);
+				}
+				emit(y);
+			}
 		}
-		if (add != sub) {
-			inc(add);
-			dec(sub);
-		}
-		emit(y);
 	}
 	if (overflow) {
 		atomicOr(J.status, STATUS_CAPACITY);
