@@ -407,13 +407,23 @@ struct stpgb_batch {
 			G.dpg = best_dpg;
 			G.rows = best_rows;
 			// the warp-cooperative kernel over several jobs: also with 1, 2, 4, 8 and 12
-			// more jobs interleaved than the rule gives (up to every job of the group)
+			// more jobs interleaved than the rule gives, and with every job of the group
+			// (a remainder group of a few jobs at the end of the launch runs dense and long)
 			if (rc == STPGB_OK && G.rows && G.lanes == 1u && G.dpg == 1u) {
 				const uint32_t base_q = G.coop_interleave();
-				for (const uint32_t extra : { 1u, 2u, 4u, 8u, 12u }) {
-					if (base_q + extra > G.h.size() || rc != STPGB_OK) {
-						break;
+				const uint32_t njob = static_cast<uint32_t>(G.h.size());
+				uint32_t extras[6];
+				uint32_t ne = 0u;
+				for (const uint32_t e : { 1u, 2u, 4u, 8u, 12u }) {
+					if (base_q + e <= njob) {
+						extras[ne++] = e;
 					}
+				}
+				if (njob > base_q && (ne == 0u || extras[ne - 1u] != njob - base_q)) {
+					extras[ne++] = njob - base_q;
+				}
+				for (uint32_t xi = 0u; xi < ne && rc == STPGB_OK; xi++) {
+					const uint32_t extra = extras[xi];
 					G.interleave_extra = extra;
 					float t = 0.0f;
 					for (int rep = 0; rep < 2 && rc == STPGB_OK; rep++) {

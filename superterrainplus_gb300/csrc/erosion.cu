@@ -940,8 +940,12 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 // that several jobs share the droplets in flight and each keeps fewer of its
 // own in flight per pixel (the blocks of a job still go out in order).
 constexpr int32_t kCoopTrip = 3; // blocks of a run per round trip
+// Blocks per SM the warp-cooperative kernel is compiled for: 8 (64 registers,
+// no spill) ran the production batch's erosion in 59.95 ms, 7 (72) in 59.91,
+// 9 (56, 32 bytes spilled) in 61.5, 10 and 12 slower still.
+constexpr uint32_t kCoopBlocksPerSM = 8u;
 
-__global__ void __launch_bounds__(kErodeBlock, 9) erosion_coop_kernel(const ErosionJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kErodeBlock, kCoopBlocksPerSM) erosion_coop_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single, const uint32_t runcap, const uint32_t njobs, const uint32_t interleave,
 	const uint32_t blocks_per_job) {
 	constexpr uint32_t kWarps = kErodeBlock / 32u;
@@ -1323,7 +1327,8 @@ uint32_t erosion_coop_interleave(const ErosionJob* jobs, const uint32_t njobs) {
 		cudaGetLastError();
 		l2 = 126 * 1024 * 1024;
 	}
-	const double resident = erosion_resident_droplets(1u, 1u);
+	// droplets the warp-cooperative kernel keeps resident (one per thread)
+	const double resident = static_cast<double>(current_sm_count()) * kCoopBlocksPerSM * kErodeBlock;
 	double worst = 0.0, map_bytes = 1.0;
 	for (uint32_t j = 0u; j < njobs; j++) {
 		const ErosionJob& J = jobs[j];
