@@ -568,7 +568,8 @@ __device__ __forceinline__ void red_add_v4(float4* addr, const float a, const fl
 // do: 9 blocks of 128 threads (56 registers) with one droplet per group,
 // 8 (64 registers) with two (measured: 10 blocks of 48 registers are 1 %
 // slower with two blocks per round trip, 12 blocks of 40 registers slower
-// still).
+// still; 7 blocks of 72 registers and 6 of 80, without the spills, are as
+// fast for two lanes and one droplet and 6-15 % slower for the others).
 template<uint32_t G, uint32_t K>
 __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_kernel(const ErosionJob* __restrict__ jobs,
 	const ErosionJob single, const uint32_t resident, const bool wide, const bool atomic_brush) {
