@@ -384,6 +384,7 @@ def run_ours(args):
     lanes, tune_ms = batch.tuning()
     stage_tune = batch.tuning_stages()
     filter_path = batch.tuning_filter_path()
+    kernels_per_step = batch.kernels_per_run()
 
     def barrier():
         torch.cuda.synchronize()
@@ -607,7 +608,7 @@ def run_ours(args):
                          "erosion_brush_rows": bool(lanes[2]),
                          "erosion_ms_by_lanes_x_droplets": {f"{a}x{b}" + ("-rows" if r else ""): v
                                                             for (a, b, r), v in tune_ms.items()}},
-            "gpu_launches": 7 * args.steps,
+            "gpu_launches": kernels_per_step * args.steps,
         }
         print(json.dumps(line), flush=True)
     if dist:

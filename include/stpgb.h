@@ -758,6 +758,11 @@ STPGB_API int stpgb_batch_tuning_stages(const stpgb_batch* batch, uint32_t* shf_
  * time with each (`path_ms`, 4 floats; zeros before tuning). */
 STPGB_API int stpgb_batch_tuning_filter_path(const stpgb_batch* batch, uint32_t* path, float* path_ms);
 
+/* No counterpart in the reference.  The kernels one stpgb_batch_run launches:
+ * the kernel nodes of the batch's CUDA graph (the filter's nine launches,
+ * noise, one erosion launch per variant group, format). */
+STPGB_API int stpgb_batch_kernels_per_run(const stpgb_batch* batch, uint32_t* kernels);
+
 /* Realised droplet steps and brush-erosion steps summed over the runs since
  * the last reset (synchronises the device). */
 STPGB_API int stpgb_batch_counters(stpgb_batch* batch, uint64_t* realised_steps, uint64_t* erode_steps,

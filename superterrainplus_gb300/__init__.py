@@ -532,6 +532,12 @@ class Batch:
         check(lib().stpgb_batch_tuning_filter_path(self._h, C.byref(p), ms))
         return p.value, {c: ms[c] for c in range(4) if ms[c] > 0}
 
+    def kernels_per_run(self):
+        """Kernels one run launches (the kernel nodes of the batch's graph)."""
+        k = C.c_uint32(0)
+        check(lib().stpgb_batch_kernels_per_run(self._h, C.byref(k)))
+        return k.value
+
     def counters(self, reset=True):
         a, b = C.c_uint64(0), C.c_uint64(0)
         check(lib().stpgb_batch_counters(self._h, C.byref(a), C.byref(b), int(reset)))

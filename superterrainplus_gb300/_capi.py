@@ -241,6 +241,7 @@ PROTOTYPES = {
     "stpgb_batch_tuning": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32), vp]),
     "stpgb_batch_tuning_stages": (C.c_int, [vp, C.POINTER(u32), vp, C.POINTER(u32), vp, C.POINTER(u32)]),
     "stpgb_batch_tuning_filter_path": (C.c_int, [vp, C.POINTER(u32), vp]),
+    "stpgb_batch_kernels_per_run": (C.c_int, [vp, C.POINTER(u32)]),
     "stpgb_batch_tune": (C.c_int, [vp]),
     "stpgb_batch_download_inputs": (C.c_int, [vp, vp, vp, vp]),
     "stpgb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(RaindropSetting), C.POINTER(SimplexSetting),

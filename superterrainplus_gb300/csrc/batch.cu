@@ -908,6 +908,29 @@ int stpgb_batch_tuning_stages(const stpgb_batch* b, uint32_t* shf_segments, floa
 	return STPGB_OK;
 }
 
+int stpgb_batch_kernels_per_run(const stpgb_batch* b, uint32_t* kernels) {
+	if (!b || !kernels) {
+		return inval("stpgb_batch_kernels_per_run: null argument");
+	}
+	if (b->graph) {
+		size_t n = 0u;
+		STPGB_CUDA_TRY(cudaGraphGetNodes(b->graph, nullptr, &n));
+		std::vector<cudaGraphNode_t> nodes(n);
+		STPGB_CUDA_TRY(cudaGraphGetNodes(b->graph, nodes.data(), &n));
+		uint32_t k = 0u;
+		for (size_t i = 0u; i < n; i++) {
+			cudaGraphNodeType t;
+			STPGB_CUDA_TRY(cudaGraphNodeGetType(nodes[i], &t));
+			k += t == cudaGraphNodeTypeKernel ? 1u : 0u;
+		}
+		*kernels = k;
+		return STPGB_OK;
+	}
+	// without a graph: the filter's nine launches, noise, one erosion launch per group, format
+	*kernels = 9u + 1u + b->ngroups + 1u;
+	return STPGB_OK;
+}
+
 int stpgb_batch_tuning_filter_path(const stpgb_batch* b, uint32_t* path, float* path_ms) {
 	if (!b) {
 		return inval("stpgb_batch_tuning_filter_path: null batch");

@@ -183,3 +183,16 @@ def test_production_batch_rms_within_reference_spread(stpgb, dev, oracle):
     print(f"production batch ({b.tuning()[0]}): RMS {got:.3g}; reference GPU build ({source}) "
           f"{min(ref_rms):.3g}..{max(ref_rms):.3g}, spread {spread:.3g}")
     assert got <= max(ref_rms) + spread
+
+
+def test_batch_kernels_per_run(stpgb, dev):
+    """The kernels a run launches: the graph's kernel nodes equal the count of the same batch run
+    without a graph (nine filter launches, noise, one erosion launch per group, format)."""
+    b, _ = make_batch(stpgb, graph=True)
+    b.run()
+    b.status()
+    p, _ = make_batch(stpgb, graph=False)
+    p.run()
+    p.status()
+    k = b.kernels_per_run()
+    assert k == p.kernels_per_run() and k >= 12
