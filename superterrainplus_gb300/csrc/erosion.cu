@@ -943,7 +943,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 constexpr int32_t kCoopTrip = 3; // blocks of a run per round trip
 // Blocks per SM the warp-cooperative kernel is compiled for: 8 (64 registers,
 // no spill) ran the production batch's erosion in 59.95 ms, 7 (72) in 59.91,
-// 9 (56, 32 bytes spilled) in 61.5, 10 and 12 slower still.
+// 6 (80) in 60.17, 9 (56, 32 bytes spilled) in 61.5, 10 and 12 slower still.
 constexpr uint32_t kCoopBlocksPerSM = 8u;
 
 __global__ void __launch_bounds__(kErodeBlock, kCoopBlocksPerSM) erosion_coop_kernel(const ErosionJob* __restrict__ jobs,
