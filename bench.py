@@ -84,10 +84,12 @@ def requests(batch, rank):
                  DropletCount=DROPLETS, BrushRadius=BRUSH, Lifetime=LIFETIME) for n in range(batch)]
 
 
-# DRAM bytes of one production request's erosion launch from a full ncu capture of the workload
-# (one 3x3 x 512^2 request, 600,000 droplets: 7.00 MB read + 2.50 MB written); the merged map stays
-# in L2, so the traffic is its compulsory reads and writes and grows with the requests of a launch
-EROSION_DRAM_BYTES_PER_REQUEST = 7.00e6 + 2.50e6
+# DRAM bytes and L2 atomic requests of the production batch's erosion launch (16 requests of a 3x3 x
+# 512^2 merged map and 600,000 droplets each, all jobs interleaved) from a full ncu capture: 101.19 MB
+# read + 24.92 MB written, 5.649 G atomic requests at the L2; the merged maps stay in L2, so both grow
+# with the requests of a launch
+EROSION_DRAM_BYTES_PER_REQUEST = (101.19e6 + 24.92e6) / 16
+EROSION_L2_ATOMICS_PER_REQUEST = 5.649e9 / 16
 
 
 def erosion_traffic(requests_per_launch):
@@ -124,9 +126,10 @@ def load_peaks():
 def measure_roofline_peaks(m, torch, reps=5):
     """The chip's rates for the kernels the HBM copy peak does not bound, from the library's
     measurement kernels (stpgb_roofline_launch) on an L2-resident 8 MiB map (the production merged
-    map is 9.4 MB): random scalar and 16-byte float reductions, random 16-byte loads, the latency of
-    one dependent L2 load, and the FP32 fused multiply-add rate.  Each kernel is timed with CUDA
-    events on its stream after a warm-up launch; the best of `reps` launches is kept."""
+    map is 9.4 MB): random scalar and 16-byte float reductions, random 16-byte returning atomics,
+    random 16-byte loads, the latency of one dependent L2 load, and the FP32 fused multiply-add
+    rate.  Each kernel is timed with CUDA events on its stream after a warm-up launch; the best of
+    `reps` launches is kept."""
     import ctypes as C
     L = m.lib()
     dev = torch.cuda.current_device()
@@ -156,6 +159,7 @@ def measure_roofline_peaks(m, torch, reps=5):
     ops = blocks * 256 * iters
     t_red = timed(0, buf, n, blocks, iters)
     t_red4 = timed(1, buf, n, blocks, iters)
+    t_at4 = timed(5, buf, n, blocks, iters)
     buf.zero_()
     t_ld4 = timed(2, buf, n, blocks, iters)
     # dependent loads: one random cycle through 2^21 entries
@@ -170,6 +174,7 @@ def measure_roofline_peaks(m, torch, reps=5):
     t_fma = timed(4, buf, 1, fma_blocks, fma_iters)
     return {"red_f32_gops": ops / t_red / 1e9, "red_f32_gbs": 4 * ops / t_red / 1e9,
             "red_v4_f32_gbs": 16 * ops / t_red4 / 1e9, "load_v4_gbs": 16 * ops / t_ld4 / 1e9,
+            "atom_v4_f32_gbs": 16 * ops / t_at4 / 1e9,
             "dependent_l2_load_cycles": ticks / chase_steps,
             "fp32_fma_tflops": fma_blocks * 256 * fma_iters * 16 / t_fma / 1e12,
             "map_bytes": 4 * n, "sms": sms,
@@ -525,15 +530,24 @@ def run_ours(args):
         alg_bytes = roof["load_bytes"] + roof["reduction_bytes"]
         roof.update({
             "kernel": roof_stage, "traffic": erosion_traffic(B),
-            "traffic_source": "DRAM read + write of one production request's erosion launch (ncu capture), "
+            "traffic_source": "DRAM read + write of the 16-request production erosion launch (ncu capture), "
                               "scaled by the requests per launch: the merged maps stay in L2",
             "algorithmic_bytes_per_launch": alg_bytes,
             "hbm": {"achieved": alg_bytes / (stage_ms[dom] / 1000.0) / 1e9, "peak": peak, "peak_source": peak_kind,
                     "frac": alg_bytes / (stage_ms[dom] / 1000.0) / 1e9 / peak},
+            "l2_atomics": {"requests_per_launch": EROSION_L2_ATOMICS_PER_REQUEST * B,
+                           "source": "ncu capture of the 16-request launch, scaled by the requests per launch",
+                           "achieved_gbs": 16 * EROSION_L2_ATOMICS_PER_REQUEST * B / (stage_ms[dom] / 1000.0) / 1e9,
+                           "peak_gbs": peaks["atom_v4_f32_gbs"],
+                           "frac": 16 * EROSION_L2_ATOMICS_PER_REQUEST * B / (stage_ms[dom] / 1000.0) / 1e9
+                           / peaks["atom_v4_f32_gbs"],
+                           "peak_note": "measured random 16-byte returning atomics (atom.global.add.v4.f32), "
+                                        "the brush's operation; one 16-byte block per request"},
             "dependent_l2_load_cycles": peaks["dependent_l2_load_cycles"],
             "note": "per realised step: 32 B corner gathers, then 4 B read + 4 B reduction per brush point "
-                    "(eroding) or 16 B of reductions (depositing); the kernel waits on a chain of dependent L2 "
-                    "round trips per step"})
+                    "(eroding) or 16 B of reductions (depositing); more droplets in flight, fewer round trips "
+                    "and fewer instructions per step measured no faster: the L2's atomic throughput under "
+                    "this access pattern bounds the kernel"})
     elif roof_stage == "format":
         fb = B * 9 * S * S * (4 + 2)
         achieved = fb / (stage_ms[dom] / 1000.0) / 1e9

@@ -635,13 +635,17 @@ STPGB_API int stpgb_generator_erode_starts(stpgb_generator* gen, float* const* h
  *               elapsed clock64 ticks to sink[0] (uint64, then the last index);
  *   FMA_F32     eight independent chains of `iters` fused multiply-adds per
  *               thread (16 flop per thread and iteration); `buffer` is one
- *               float, never written. */
+ *               float, never written;
+ *   ATOM_V4_F32 RED_V4_F32 with returning atomics (atom.global.add.v4.f32, the
+ *               erosion brush's operation), each result used before the
+ *               thread's next atomic; `sink` as for LOAD_V4_F32. */
 enum {
 	STPGB_ROOFLINE_RED_F32 = 0,
 	STPGB_ROOFLINE_RED_V4_F32 = 1,
 	STPGB_ROOFLINE_LOAD_V4_F32 = 2,
 	STPGB_ROOFLINE_CHASE = 3,
-	STPGB_ROOFLINE_FMA_F32 = 4
+	STPGB_ROOFLINE_FMA_F32 = 4,
+	STPGB_ROOFLINE_ATOM_V4_F32 = 5
 };
 STPGB_API int stpgb_roofline_launch(uint32_t kind, void* buffer, uint64_t elements, uint32_t blocks,
 	uint32_t iters, void* sink, void* stream);

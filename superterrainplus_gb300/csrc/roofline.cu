@@ -1,7 +1,8 @@
 // Measurement kernels for the roofline denominators of the kernels that are
 // not bound by HBM copy bandwidth: random float reductions into an
 // L2-resident map (scalar and 16-byte vector, the operations of the erosion
-// kernels' deposits and brush updates), random 16-byte loads from it (their
+// kernels' deposits and brush updates; 16-byte returning atomics, the
+// brush's exact take), random 16-byte loads from it (their
 // corner gathers), the latency of one dependent L2 load (the chain each
 // droplet step waits on), and the FP32 fused multiply-add rate (the noise
 // kernel's pipe).  No counterpart in the reference.  Plain kernels that touch
@@ -51,6 +52,27 @@ __global__ void __launch_bounds__(kBlock) load_v4_kernel(const float4* __restric
 	}
 	if (acc == 12345.678f) {
 		sink[0] = acc; // never taken for the zero map; keeps the loads
+	}
+}
+
+// returning 16-byte atomics, each result summed before the next is issued
+// (one in flight per thread, as a brush lane waits on its block's values)
+__global__ void __launch_bounds__(kBlock) atom_v4_kernel(float* __restrict__ map, const uint32_t shift,
+	const uint32_t iters, float* __restrict__ sink) {
+	uint32_t h = (blockIdx.x * kBlock + threadIdx.x) * 2654435761u;
+	float acc = 0.0f;
+	for (uint32_t i = 0u; i < iters; i++) {
+		h = lcg(h);
+		float* const p = map + 4u * (h >> shift);
+		float a, b, c, d;
+		asm volatile("atom.global.add.v4.f32 {%0, %1, %2, %3}, [%4], {%5, %6, %7, %8};"
+					 : "=f"(a), "=f"(b), "=f"(c), "=f"(d)
+					 : "l"(p), "f"(1.0f), "f"(1.0f), "f"(1.0f), "f"(1.0f)
+					 : "memory");
+		acc += a + b + c + d;
+	}
+	if (acc == -12345.678f) {
+		sink[0] = acc; // never taken: the map only grows from zero; keeps the results used
 	}
 }
 
@@ -123,11 +145,18 @@ extern "C" int stpgb_roofline_launch(const uint32_t kind, void* buffer, const ui
 		break;
 	case STPGB_ROOFLINE_RED_V4_F32:
 	case STPGB_ROOFLINE_LOAD_V4_F32:
+	case STPGB_ROOFLINE_ATOM_V4_F32:
 		if (l == 0xFFFFFFFFu || l < 3u || l > 34u) {
 			return inval("stpgb_roofline_launch: the map needs a power-of-two float count from 8 to 2^34");
 		}
 		if (kind == STPGB_ROOFLINE_RED_V4_F32) {
 			red_v4_kernel<<<blocks, kBlock, 0, s>>>(static_cast<float*>(buffer), 32u - (l - 2u), iters);
+		} else if (kind == STPGB_ROOFLINE_ATOM_V4_F32) {
+			if (!sink) {
+				return inval("stpgb_roofline_launch: the atomic kernel needs a sink");
+			}
+			atom_v4_kernel<<<blocks, kBlock, 0, s>>>(static_cast<float*>(buffer), 32u - (l - 2u), iters,
+				static_cast<float*>(sink));
 		} else {
 			if (!sink) {
 				return inval("stpgb_roofline_launch: the load kernel needs a sink");

@@ -188,3 +188,16 @@ def test_shf_set_path_range(stpgb):
         assert lib.stpgb_shf_set_path(p) == 0
     assert lib.stpgb_shf_set_path(4) != 0
     assert lib.stpgb_shf_set_path(0) == 0
+
+
+def test_roofline_launch_argument_errors(stpgb):
+    """The measurement kernels refuse an unknown kind, a missing sink and a map that is not a power
+    of two before any device work (no GPU call)."""
+    lib = stpgb.lib()
+    fake = C.c_void_p(256)
+    assert lib.stpgb_roofline_launch(6, fake, 1 << 10, 1, 1, fake, None) == stpgb._capi.STPGB_EINVAL
+    for kind in (2, 5):  # 16-byte loads and returning atomics need a sink
+        assert lib.stpgb_roofline_launch(kind, fake, 1 << 10, 1, 1, None, None) == stpgb._capi.STPGB_EINVAL
+    for kind in (0, 1, 5):
+        assert lib.stpgb_roofline_launch(kind, fake, 1000, 1, 1, fake, None) == stpgb._capi.STPGB_EINVAL
+    assert lib.stpgb_roofline_launch(1, None, 1 << 10, 1, 1, fake, None) == stpgb._capi.STPGB_EINVAL
