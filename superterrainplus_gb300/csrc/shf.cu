@@ -40,6 +40,8 @@ constexpr uint32_t kVBlock = 64u;
 constexpr uint32_t kVAhead = 8u;
 constexpr uint32_t kHBlock = 32u;
 constexpr uint32_t kScanBlock = 256u;
+// consecutive (row, segment) counts a scan thread takes per pass
+constexpr uint32_t kScanPer = 16u;
 // threads per SM the segmented passes aim for
 constexpr uint64_t kShfThreadsPerSM = 1024u;
 
@@ -532,10 +534,21 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 	}
 	__syncthreads();
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-	for (uint32_t base = 0u; base < slots; base += kScanBlock) {
-		const uint32_t i = base + threadIdx.x;
-		const uint64_t v = i < slots ? J.rows[i] : 0u;
-		uint64_t s = v;
+	// kScanPer consecutive slots per thread and pass: the thread's own running sum, then one
+	// block-wide scan of the threads' totals
+	for (uint32_t base = 0u; base < slots; base += kScanBlock * kScanPer) {
+		const uint32_t first = base + threadIdx.x * kScanPer;
+		uint32_t v[kScanPer];
+#pragma unroll
+		for (uint32_t k = 0u; k < kScanPer; k++) {
+			v[k] = first + k < slots ? J.rows[first + k] : 0u;
+		}
+		uint64_t mine = 0u;
+#pragma unroll
+		for (uint32_t k = 0u; k < kScanPer; k++) {
+			mine += v[k];
+		}
+		uint64_t s = mine;
 #pragma unroll
 		for (uint32_t d = 1u; d < 32u; d <<= 1) {
 			const uint64_t t = __shfl_up_sync(0xFFFFFFFFu, s, d);
@@ -552,9 +565,13 @@ __global__ void __launch_bounds__(kScanBlock) shf_rowscan(const ShfJob* __restri
 			wbase += warp_sum[w];
 		}
 		const uint64_t carry = carry_s;
-		const uint64_t excl = carry + wbase + s - v;
-		if (i < slots) {
-			J.rows[i] = static_cast<uint32_t>(min(excl, static_cast<uint64_t>(0xFFFFFFFFu)));
+		uint64_t excl = carry + wbase + s - mine;
+#pragma unroll
+		for (uint32_t k = 0u; k < kScanPer; k++) {
+			if (first + k < slots) {
+				J.rows[first + k] = static_cast<uint32_t>(min(excl, static_cast<uint64_t>(0xFFFFFFFFu)));
+			}
+			excl += v[k];
 		}
 		__syncthreads();
 		if (threadIdx.x == kScanBlock - 1u) {

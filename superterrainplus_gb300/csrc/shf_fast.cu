@@ -80,20 +80,27 @@ __global__ void __launch_bounds__(kPaletteBlock) shf_palette(const ShfJob* __res
 	}
 	const uint32_t r1 = min(NR, r0 + kShfPaletteRows);
 	__shared__ uint32_t bits[2048];
-	__shared__ uint32_t total, fill;
+	// distinct values found so far: every bit is counted once, by the thread whose atomicOr set it
+	__shared__ uint32_t seen, fill;
 	__shared__ uint32_t vals[kShfFastItems];
 	for (uint32_t i = threadIdx.x; i < 2048u; i += kPaletteBlock) {
 		bits[i] = 0u;
 	}
 	if (threadIdx.x == 0u) {
-		total = 0u;
+		seen = 0u;
 		fill = 0u;
 	}
 	__syncthreads();
 	const uint16_t* const base = read_region(J);
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t span = (NC + kPaletteBlock - 1u) / kPaletteBlock * kPaletteBlock;
+	const volatile uint32_t& seen_now = seen;
 	for (uint32_t row = r0; row < r1; row++) {
+		// a tile past kShfFastItems values sends its job to the general slides: stop reading
+		// (warp-uniform, so every lane of a warp leaves the match below together)
+		if (__any_sync(0xFFFFFFFFu, seen_now > kShfFastItems)) {
+			break;
+		}
 		const uint16_t* const src = base + static_cast<uint64_t>(row) * J.pitch;
 		for (uint32_t c = threadIdx.x; c < span; c += kPaletteBlock) {
 			const uint32_t v = c < NC ? static_cast<uint32_t>(__ldg(src + c)) : kNoValue;
@@ -101,22 +108,14 @@ __global__ void __launch_bounds__(kPaletteBlock) shf_palette(const ShfJob* __res
 			const uint32_t same = __match_any_sync(0xFFFFFFFFu, v);
 			if (v != kNoValue && static_cast<uint32_t>(__ffs(same) - 1) == lane) {
 				const uint32_t bit = 1u << (v & 31u);
-				if (!(bits[v >> 5] & bit)) {
-					atomicOr(&bits[v >> 5], bit);
+				if (!(bits[v >> 5] & bit) && !(atomicOr(&bits[v >> 5], bit) & bit)) {
+					atomicAdd(&seen, 1u);
 				}
 			}
 		}
 	}
 	__syncthreads();
-	uint32_t mine = 0u;
-	for (uint32_t i = threadIdx.x; i < 2048u; i += kPaletteBlock) {
-		mine += __popc(bits[i]);
-	}
-	if (mine) {
-		atomicAdd(&total, mine);
-	}
-	__syncthreads();
-	const uint32_t n = total;
+	const uint32_t n = seen;
 	if (n <= kShfFastItems) {
 		for (uint32_t i = threadIdx.x; i < 2048u; i += kPaletteBlock) {
 			uint32_t w = bits[i];
