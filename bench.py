@@ -85,11 +85,13 @@ def requests(batch, rank):
 
 
 # DRAM bytes and L2 atomic requests of the production batch's erosion launch (16 requests of a 3x3 x
-# 512^2 merged map and 600,000 droplets each, all jobs interleaved) from a full ncu capture: 101.19 MB
-# read + 24.92 MB written, 5.649 G atomic requests at the L2; the merged maps stay in L2, so both grow
-# with the requests of a launch
-EROSION_DRAM_BYTES_PER_REQUEST = (101.19e6 + 24.92e6) / 16
-EROSION_L2_ATOMICS_PER_REQUEST = 5.649e9 / 16
+# 512^2 merged map and 600,000 droplets each, all jobs interleaved) from a full ncu capture: 101.04 MB
+# read + 25.90 MB written; 5.106 G atomic requests at the L2 (the brush's returning 16-byte atomics
+# and the scalar deposits) and 0.272 G vector reductions (the deposits whose row pair shares a
+# 16-byte block); the merged maps stay in L2, so all of it grows with the requests of a launch
+EROSION_DRAM_BYTES_PER_REQUEST = (101.04e6 + 25.90e6) / 16
+EROSION_L2_ATOMICS_PER_REQUEST = 5.106e9 / 16
+EROSION_L2_REDUCTIONS_PER_REQUEST = 0.272e9 / 16
 
 
 def erosion_traffic(requests_per_launch):
@@ -197,6 +199,24 @@ def erosion_l2_roofline(peaks, steps_total, erode_steps, brush_size, stage_ms):
             "frac": t_min / t, "load_bytes": loads, "reduction_bytes": reds,
             "peak_note": "mix-weighted: L2 loads at the measured random 16-byte load rate, reductions at the "
                          "measured random 16-byte vector reduction rate"}
+
+
+def l2_atomic_roofline(peaks, requests, stage_ms):
+    """The erosion launch's L2 atomic work against the measured random 16-byte rates: the
+    captured returning-atomic and reduction requests (scaled by the requests per launch), each
+    counted as a 16-byte operation; frac = their time at the measured returning-atomic and
+    reduction rates / the launch's time."""
+    atom = EROSION_L2_ATOMICS_PER_REQUEST * requests
+    red = EROSION_L2_REDUCTIONS_PER_REQUEST * requests
+    t = stage_ms / 1000.0
+    t_min = 16 * atom / (peaks["atom_v4_f32_gbs"] * 1e9) + 16 * red / (peaks["red_v4_f32_gbs"] * 1e9)
+    return {"atomic_requests_per_launch": atom, "reduction_requests_per_launch": red,
+            "achieved_gbs": 16 * (atom + red) / t / 1e9, "peak_gbs": 16 * (atom + red) / t_min / 1e9,
+            "frac": t_min / t,
+            "source": "ncu capture of the 16-request launch, scaled by the requests per launch",
+            "peak_note": "mix-weighted: returning atomics at the measured random 16-byte returning-atomic "
+                         "rate (atom.global.add.v4.f32, the brush's operation), reductions at the measured "
+                         "random 16-byte reduction rate; one request per 16-byte block"}
 
 
 class ClockSampler:
@@ -535,14 +555,7 @@ def run_ours(args):
             "algorithmic_bytes_per_launch": alg_bytes,
             "hbm": {"achieved": alg_bytes / (stage_ms[dom] / 1000.0) / 1e9, "peak": peak, "peak_source": peak_kind,
                     "frac": alg_bytes / (stage_ms[dom] / 1000.0) / 1e9 / peak},
-            "l2_atomics": {"requests_per_launch": EROSION_L2_ATOMICS_PER_REQUEST * B,
-                           "source": "ncu capture of the 16-request launch, scaled by the requests per launch",
-                           "achieved_gbs": 16 * EROSION_L2_ATOMICS_PER_REQUEST * B / (stage_ms[dom] / 1000.0) / 1e9,
-                           "peak_gbs": peaks["atom_v4_f32_gbs"],
-                           "frac": 16 * EROSION_L2_ATOMICS_PER_REQUEST * B / (stage_ms[dom] / 1000.0) / 1e9
-                           / peaks["atom_v4_f32_gbs"],
-                           "peak_note": "measured random 16-byte returning atomics (atom.global.add.v4.f32), "
-                                        "the brush's operation; one 16-byte block per request"},
+            "l2_atomics": l2_atomic_roofline(peaks, B, stage_ms[dom]),
             "dependent_l2_load_cycles": peaks["dependent_l2_load_cycles"],
             "note": "per realised step: 32 B corner gathers, then 4 B read + 4 B reduction per brush point "
                     "(eroding) or 16 B of reductions (depositing); more droplets in flight, fewer round trips "

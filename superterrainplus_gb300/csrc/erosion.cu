@@ -555,6 +555,29 @@ __device__ __forceinline__ void red_add_v4(float4* addr, const float a, const fl
 		: "memory");
 }
 
+// A deposit's two corners of one map row, c0[0] += d0 and c0[1] += d1: one
+// 16-byte reduction when both lie in one aligned block (-0.0 to the block's
+// other cells leaves them unchanged), else two scalar ones.  The L2 takes a
+// reduction per request whatever its width, so this is 1.25 requests per row
+// on average instead of 2.  Needs a map whose rows start 16-byte aligned.
+__device__ __forceinline__ void deposit_row(float* const c0, const float d0, const float d1) {
+	const uint32_t at = (static_cast<uint32_t>(reinterpret_cast<uintptr_t>(c0)) >> 2) & 3u;
+	if (at != 3u) {
+		float v[4] = { -0.0f, -0.0f, -0.0f, -0.0f };
+#pragma unroll
+		for (uint32_t k = 0u; k < 3u; k++) {
+			if (k == at) {
+				v[k] = d0;
+				v[k + 1u] = d1;
+			}
+		}
+		red_add_v4(reinterpret_cast<float4*>(c0 - at), v[0], v[1], v[2], v[3]);
+	} else {
+		atomicAdd(c0, d0);
+		atomicAdd(c0 + 1, d1);
+	}
+}
+
 // K droplets (1 or 2) per group of G lanes (2 or 4) as erosion_multi_kernel,
 // with the erosion step done run by run in aligned 16-byte blocks: one
 // vector read of four cells, then one vector reduction that subtracts
@@ -756,8 +779,7 @@ __global__ void __launch_bounds__(kErodeBlock, K == 2u ? 8 : 9) erosion_rows_ker
 						atomicAdd(map + mi[k] + corner_off, dep * wx * wy);
 					} else {
 						const float wy = g ? oy[k] : 1.0f - oy[k];
-						atomicAdd(map + mi[k] + corner_off, dep * (1.0f - ox[k]) * wy);
-						atomicAdd(map + mi[k] + corner_off + 1u, dep * ox[k] * wy);
+						deposit_row(map + mi[k] + corner_off, dep * (1.0f - ox[k]) * wy, dep * ox[k] * wy);
 					}
 				} else {
 					erode[k] = true;
@@ -1078,9 +1100,9 @@ __global__ void __launch_bounds__(kErodeBlock, kCoopBlocksPerSM) erosion_coop_ke
 					const float dep = (dh > 0.0f) ? fminf(dh, sed) : (sed - cap) * P.DepositSpeed;
 					sed -= dep;
 #pragma unroll
-					for (uint32_t c = 0u; c < 4u; c++) {
-						const float wx = (c & 1u) ? ox : 1.0f - ox, wy = (c & 2u) ? oy : 1.0f - oy;
-						atomicAdd(map + mi + ((c & 2u) ? pitch : 0u) + (c & 1u), dep * wx * wy);
+					for (uint32_t row = 0u; row < 2u; row++) {
+						const float wy = row ? oy : 1.0f - oy;
+						deposit_row(map + mi + (row ? pitch : 0u), dep * (1.0f - ox) * wy, dep * ox * wy);
 					}
 				} else {
 					erode = true;
