@@ -39,6 +39,8 @@ constexpr uint32_t kVBlock = 64u;
 // steps of the vertical slide whose samples are loaded ahead of their use
 constexpr uint32_t kVAhead = 8u;
 constexpr uint32_t kHBlock = 32u;
+// columns (rows) a segment's start sweep loads ahead of their use
+constexpr uint32_t kSweepAhead = 8u;
 constexpr uint32_t kScanBlock = 256u;
 // consecutive (row, segment) counts a scan thread takes per pass
 constexpr uint32_t kScanPer = 16u;
@@ -158,21 +160,39 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 				key[(n - 1u) * kVBlock] = static_cast<uint32_t>(q + r);
 			}
 		}
-		// upward sweep: extend each run while its occurrences stay within 2r+1 rows
+		// upward sweep: extend each run while its occurrences stay within 2r+1
+		// rows; the samples are loaded kSweepAhead rows ahead
 		uint32_t open = n;
-		for (int q = static_cast<int>(y_a) - r - 1; q >= -r && open > 0u; q--) {
-			const uint32_t v = at(q), qk = static_cast<uint32_t>(q + r);
-			for (uint32_t j = 0u; j < n; j++) {
-				const uint32_t kj = key[j * kVBlock];
-				if (kj & kResolved) {
-					continue;
-				}
-				if (kj - qk >= 2u * J.r + 2u) {
-					// 2r+1 rows without the item: an earlier occurrence starts another run
-					key[j * kVBlock] = kj | kResolved;
-					open--;
-				} else if ((acc[j * kVBlock] >> 16) == v) {
-					key[j * kVBlock] = qk;
+		uint32_t sv[kSweepAhead];
+		const int q_top = static_cast<int>(y_a) - r - 1;
+#pragma unroll
+		for (uint32_t u = 0u; u < kSweepAhead; u++) {
+			if (q_top - static_cast<int>(u) >= -r) {
+				sv[u] = at(q_top - static_cast<int>(u));
+			}
+		}
+		for (int q0 = q_top; q0 >= -r && open > 0u; q0 -= static_cast<int>(kSweepAhead)) {
+#pragma unroll
+			for (uint32_t u = 0u; u < kSweepAhead; u++) {
+				const int q = q0 - static_cast<int>(u);
+				if (q >= -r && open > 0u) {
+					const uint32_t v = sv[u], qk = static_cast<uint32_t>(q + r);
+					if (q - static_cast<int>(kSweepAhead) >= -r) {
+						sv[u] = at(q - static_cast<int>(kSweepAhead));
+					}
+					for (uint32_t j = 0u; j < n; j++) {
+						const uint32_t kj = key[j * kVBlock];
+						if (kj & kResolved) {
+							continue;
+						}
+						if (kj - qk >= 2u * J.r + 2u) {
+							// 2r+1 rows without the item: an earlier occurrence starts another run
+							key[j * kVBlock] = kj | kResolved;
+							open--;
+						} else if ((acc[j * kVBlock] >> 16) == v) {
+							key[j * kVBlock] = qk;
+						}
+					}
 				}
 			}
 		}
@@ -315,6 +335,20 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 		}
 	};
 
+	// A column's entry count and first two entries (ColData): entry slots past
+	// the count hold stale data and are not used.
+	struct ColData {
+		uint32_t n, e0, e1;
+	};
+	const bool two = kcap_v >= 2u;
+	auto fetch = [&](const uint32_t kc) {
+		ColData c;
+		c.n = vn_at(kc);
+		c.e0 = ent(kc, 0u);
+		c.e1 = two ? ent(kc, 1u) : 0u;
+		return c;
+	};
+
 	const uint32_t side = 2u * J.r + 1u;
 	if (x_a == 0u) {
 		for (uint32_t kc = 0u; kc < side; kc++) {
@@ -333,26 +367,45 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 				}
 			}
 		}
-		// leftward sweep: extend each run while its columns stay within 2r+1
+		// leftward sweep: extend each run while its columns stay within 2r+1;
+		// the columns' data is loaded kSweepAhead columns ahead (their loads do
+		// not depend on the sweep), so the sweep is not a chain of round trips
 		uint32_t open = n;
-		for (int kc = static_cast<int>(x_a) - 1; kc >= 0 && open > 0u; kc--) {
-			const uint32_t nv = vn_at(static_cast<uint32_t>(kc));
-			for (uint32_t i = 0u; i < n; i++) {
-				const uint32_t ki = key[i * kHBlock];
-				if (ki & kResolved) {
-					continue;
-				}
-				if ((ki >> 12) - static_cast<uint32_t>(kc) >= 2u * J.r + 2u) {
-					// 2r+1 columns without the item: an earlier one starts another run
-					key[i * kHBlock] = ki | kResolved;
-					open--;
-					continue;
-				}
-				const uint32_t v = item[i * kHBlock];
-				for (uint32_t j = 0u; j < nv; j++) {
-					if ((ent(static_cast<uint32_t>(kc), j) >> 16) == v) {
-						key[i * kHBlock] = (static_cast<uint32_t>(kc) << 12) | j;
-						break;
+		ColData sw[kSweepAhead];
+#pragma unroll
+		for (uint32_t u = 0u; u < kSweepAhead; u++) {
+			if (x_a >= 1u + u) {
+				sw[u] = fetch(x_a - 1u - u);
+			}
+		}
+		for (int kc0 = static_cast<int>(x_a) - 1; kc0 >= 0 && open > 0u; kc0 -= static_cast<int>(kSweepAhead)) {
+#pragma unroll
+			for (uint32_t u = 0u; u < kSweepAhead; u++) {
+				const int kc = kc0 - static_cast<int>(u);
+				if (kc >= 0 && open > 0u) {
+					const ColData c = sw[u];
+					if (kc >= static_cast<int>(kSweepAhead)) {
+						sw[u] = fetch(static_cast<uint32_t>(kc) - kSweepAhead);
+					}
+					for (uint32_t i = 0u; i < n; i++) {
+						const uint32_t ki = key[i * kHBlock];
+						if (ki & kResolved) {
+							continue;
+						}
+						if ((ki >> 12) - static_cast<uint32_t>(kc) >= 2u * J.r + 2u) {
+							// 2r+1 columns without the item: an earlier one starts another run
+							key[i * kHBlock] = ki | kResolved;
+							open--;
+							continue;
+						}
+						const uint32_t v = item[i * kHBlock];
+						for (uint32_t j = 0u; j < c.n; j++) {
+							const uint32_t e = j == 0u ? c.e0 : (j == 1u ? c.e1 : ent(static_cast<uint32_t>(kc), j));
+							if ((e >> 16) == v) {
+								key[i * kHBlock] = (static_cast<uint32_t>(kc) << 12) | j;
+								break;
+							}
+						}
 					}
 				}
 			}
@@ -453,18 +506,6 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	// accumulator, so they are loaded kAhead steps early (a ring of register
 	// slots) and the loads overlap the steps in between; entries past the
 	// second (few columns hold more than two items) are loaded when applied.
-	// Entry slots past a column's count hold stale data and are not used.
-	struct ColData {
-		uint32_t n, e0, e1;
-	};
-	const bool two = kcap_v >= 2u;
-	auto fetch = [&](const uint32_t kc) {
-		ColData c;
-		c.n = vn_at(kc);
-		c.e0 = ent(kc, 0u);
-		c.e1 = two ? ent(kc, 1u) : 0u;
-		return c;
-	};
 	auto apply = [&](const uint32_t kc, const ColData& c, const bool add) {
 		if (c.n > 0u) {
 			add ? inc(c.e0 >> 16, c.e0 & 0xFFFFu) : dec(c.e0 >> 16, c.e0 & 0xFFFFu);
