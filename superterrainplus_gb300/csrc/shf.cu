@@ -146,20 +146,42 @@ __global__ void __launch_bounds__(kVBlock) shf_vertical(const ShfJob* __restrict
 	};
 
 	const int r = static_cast<int>(J.r);
-	if (y_a == 0u) {
-		for (int q = -r; q <= r; q++) {
-			inc(at(q));
+	// The window of the segment's first row, rows [y_a - r, y_a + r], its
+	// samples loaded kSweepAhead rows ahead (a ring of registers).
+	auto for_window = [&](auto&& f) {
+		const int q_a = static_cast<int>(y_a) - r, q_b = static_cast<int>(y_a) + r;
+		uint32_t sv[kSweepAhead];
+#pragma unroll
+		for (uint32_t u = 0u; u < kSweepAhead; u++) {
+			if (q_a + static_cast<int>(u) <= q_b) {
+				sv[u] = at(q_a + static_cast<int>(u));
+			}
 		}
+		for (int q0 = q_a; q0 <= q_b; q0 += static_cast<int>(kSweepAhead)) {
+#pragma unroll
+			for (uint32_t u = 0u; u < kSweepAhead; u++) {
+				const int q = q0 + static_cast<int>(u);
+				if (q <= q_b) {
+					const uint32_t v = sv[u];
+					if (q + static_cast<int>(kSweepAhead) <= q_b) {
+						sv[u] = at(q + static_cast<int>(kSweepAhead));
+					}
+					f(q, v);
+				}
+			}
+		}
+	};
+	if (y_a == 0u) {
+		for_window([&](const int, const uint32_t v) { inc(v); });
 	} else {
 		// counts of the window, each item keyed by its topmost row in it (+r, >= 0)
-		for (int q = static_cast<int>(y_a) - r; q <= static_cast<int>(y_a) + r; q++) {
-			const uint32_t v = at(q);
+		for_window([&](const int q, const uint32_t v) {
 			const uint32_t before = n;
 			inc(v);
 			if (n > before) {
 				key[(n - 1u) * kVBlock] = static_cast<uint32_t>(q + r);
 			}
-		}
+		});
 		// upward sweep: extend each run while its occurrences stay within 2r+1
 		// rows; the samples are loaded kSweepAhead rows ahead
 		uint32_t open = n;
@@ -320,20 +342,6 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	auto ent = [&](const uint32_t kc, const uint32_t j) {
 		return vcol[(kc * static_cast<uint64_t>(kcap_v) + j) * H];
 	};
-	auto add_col = [&](const uint32_t kc) {
-		const uint32_t nv = vn_at(kc);
-		for (uint32_t j = 0u; j < nv; j++) {
-			const uint32_t e = ent(kc, j);
-			inc(e >> 16, e & 0xFFFFu);
-		}
-	};
-	auto sub_col = [&](const uint32_t kc) {
-		const uint32_t nv = vn_at(kc);
-		for (uint32_t j = 0u; j < nv; j++) {
-			const uint32_t e = ent(kc, j);
-			dec(e >> 16, e & 0xFFFFu);
-		}
-	};
 
 	// A column's entry count and first two entries (ColData): entry slots past
 	// the count hold stale data and are not used.
@@ -350,23 +358,45 @@ __global__ void __launch_bounds__(kHBlock) shf_horizontal(const ShfJob* __restri
 	};
 
 	const uint32_t side = 2u * J.r + 1u;
-	if (x_a == 0u) {
-		for (uint32_t kc = 0u; kc < side; kc++) {
-			add_col(kc);
+	// The window of the segment's first column, columns [x_a, x_a + 2r], with
+	// each column's data loaded kSweepAhead columns ahead (a ring of registers);
+	// f(kc, j, entry) for every entry in column then entry order.
+	auto for_window = [&](auto&& f) {
+		const uint32_t k_b = x_a + side;
+		ColData sw[kSweepAhead];
+#pragma unroll
+		for (uint32_t u = 0u; u < kSweepAhead; u++) {
+			if (x_a + u < k_b) {
+				sw[u] = fetch(x_a + u);
+			}
 		}
-	} else {
-		// counts of the window, each item keyed by (first column, place in its histogram)
-		for (uint32_t kc = x_a; kc < x_a + side; kc++) {
-			const uint32_t nv = vn_at(kc);
-			for (uint32_t j = 0u; j < nv; j++) {
-				const uint32_t e = ent(kc, j);
-				const uint32_t before = n;
-				inc(e >> 16, e & 0xFFFFu);
-				if (n > before) {
-					key[(n - 1u) * kHBlock] = (kc << 12) | j;
+		for (uint32_t k0 = x_a; k0 < k_b; k0 += kSweepAhead) {
+#pragma unroll
+			for (uint32_t u = 0u; u < kSweepAhead; u++) {
+				const uint32_t kc = k0 + u;
+				if (kc < k_b) {
+					const ColData c = sw[u];
+					if (kc + kSweepAhead < k_b) {
+						sw[u] = fetch(kc + kSweepAhead);
+					}
+					for (uint32_t j = 0u; j < c.n; j++) {
+						f(kc, j, j == 0u ? c.e0 : (j == 1u ? c.e1 : ent(kc, j)));
+					}
 				}
 			}
 		}
+	};
+	if (x_a == 0u) {
+		for_window([&](const uint32_t, const uint32_t, const uint32_t e) { inc(e >> 16, e & 0xFFFFu); });
+	} else {
+		// counts of the window, each item keyed by (first column, place in its histogram)
+		for_window([&](const uint32_t kc, const uint32_t j, const uint32_t e) {
+			const uint32_t before = n;
+			inc(e >> 16, e & 0xFFFFu);
+			if (n > before) {
+				key[(n - 1u) * kHBlock] = (kc << 12) | j;
+			}
+		});
 		// leftward sweep: extend each run while its columns stay within 2r+1;
 		// the columns' data is loaded kSweepAhead columns ahead (their loads do
 		// not depend on the sweep), so the sweep is not a chain of round trips
